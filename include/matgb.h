@@ -1,0 +1,145 @@
+/*
+ * matgb.h -- GB300 extensions to the mat.h API.
+ *
+ * None of these have a counterpart in the reference (libmat is a synchronous
+ * host library with no device, stream or error channel); each says which
+ * reference routine it generalises.  Everything here is C ABI: plain
+ * pointers, sizes and integer status codes.  Functions named *_dev take
+ * DEVICE pointers (column-major, explicit leading dimension) and are
+ * asynchronous on the library stream; everything else is synchronous.
+ * Status: 0 on success, < 0 on error (message in matgb_last_error()).
+ */
+#ifndef MATGB_H_
+#define MATGB_H_
+
+#include "mat.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Status codes -------------------------------------------------------- */
+#define MATGB_OK 0
+#define MATGB_ERR_CUDA (-1)     /* a CUDA call failed (message recorded)     */
+#define MATGB_ERR_ARG (-2)      /* bad size / pointer / option               */
+#define MATGB_ERR_NOMEM (-3)    /* device allocation failed                  */
+#define MATGB_ERR_TIMEOUT (-4)  /* a bounded device wait gave up             */
+#define MATGB_ERR_NOT_SPD (-5)  /* Cholesky met a diagonal <= 0              */
+#define MATGB_ERR_NO_DEVICE (-6)
+
+/* ---- Runtime ------------------------------------------------------------- */
+/* Select the device and create the library stream (called implicitly by the
+ * first API call with device 0).  The reference has no device state; this is
+ * the GPU counterpart of its scratch-arena initialisation (mat.h:865-895). */
+int matgb_init(int device);
+/* Element size of this build: 4 (libmatgb_f32) or 8 (libmatgb_f64). */
+int matgb_elem_size(void);
+/* Last error message ("" if none) and clear.  The void mat_* functions have
+ * no error channel in the reference; they record here and, unless
+ * matgb_set_abort_on_error(0) was called, print and abort like MAT_ASSERT. */
+const char *matgb_last_error(void);
+void matgb_clear_error(void);
+void matgb_set_abort_on_error(int on);
+/* Wait for all work on the library stream. */
+int matgb_sync(void);
+/* The library stream (a cudaStream_t). */
+void *matgb_stream(void);
+/* Kernels launched by this library since load (host-side counter). */
+unsigned long long matgb_launch_count(void);
+/* Number of SMs on the current device. */
+int matgb_sm_count(void);
+
+/* ---- Memory helpers for device-resident callers ------------------------- */
+void *matgb_device_alloc(size_t bytes);
+int matgb_device_free(void *p);
+void *matgb_host_alloc(size_t bytes); /* page-locked host memory */
+int matgb_host_free(void *p);
+int matgb_memcpy_h2d(void *dst, const void *src, size_t bytes); /* async */
+int matgb_memcpy_d2h(void *dst, const void *src, size_t bytes); /* async */
+int matgb_memcpy_d2d(void *dst, const void *src, size_t bytes); /* async */
+int matgb_memset_dev(void *dst, int value, size_t bytes);       /* async */
+
+/* ---- Timing on the library stream (CUDA events, 16 slots) --------------- */
+int matgb_event_record(int slot);
+/* Milliseconds between two recorded slots (synchronises on slot1). */
+double matgb_event_elapsed_ms(int slot0, int slot1);
+
+/* Per-kernel timing: while enabled, every library launch is bracketed by
+ * CUDA events on the library stream and tagged with its algorithmic FLOPs
+ * and bytes.  matgb_ktime_get(i, ...) returns the i-th kernel name with its
+ * launch count, total milliseconds, FLOPs and bytes (synchronises); non-zero
+ * when i is past the end.  Enabling clears previous records. */
+int matgb_ktime_enable(int on);
+int matgb_ktime_get(int i, char *name, int cap, long long *launches,
+                    double *ms, double *flops, double *bytes);
+/* Peak issue rate of the SIMT FMA pipes, measured with a dependent-chain-free
+ * FMA kernel: which = 0 for FP32 (FFMA), 1 for FP64 (DFMA).  TFLOP/s. */
+double matgb_measure_fma_peak(int which);
+
+/* ---- Seeded input generation on the device ------------------------------ */
+/* A[i] = lo + (hi-lo)*u_i with u_i = splitmix64(seed, i) mapped to [0,1). */
+int matgb_fill_uniform_dev(mat_elem_t *A, size_t count, uint64_t seed,
+                           double lo, double hi);
+/* A[i] ~ N(0,1) by Box-Muller over the same stream. */
+int matgb_fill_normal_dev(mat_elem_t *A, size_t count, uint64_t seed);
+/* A[i*lda+i] += shift for i < n. */
+int matgb_add_diag_dev(mat_elem_t *A, size_t n, size_t lda, double shift);
+
+/* ---- Device-resident hot path ------------------------------------------- */
+/* C = alpha*op(A)*op(B) + beta*C, op per trans flag ('N' or 'T'); C is m x n.
+ * Generalises mat__gemm_strided_ (mat.h:2719-2741) / mat_gemm. */
+int matgb_gemm_dev(char transa, char transb, size_t m, size_t n, size_t k,
+                   mat_elem_t alpha, const mat_elem_t *A, size_t lda,
+                   const mat_elem_t *B, size_t ldb, mat_elem_t beta,
+                   mat_elem_t *C, size_t ldc);
+/* One triangle ('L'/'U') of C (n x n) = alpha*op(A)*op(A)^T + beta*C, with
+ * trans 'N' (A n x k) or 'T' (A k x n).  Generalises mat__syrk_lower_
+ * (mat.h:5474-5486), mat_syrk and mat_syrk_t. */
+int matgb_syrk_dev(char uplo, char trans, size_t n, size_t k,
+                   mat_elem_t alpha, const mat_elem_t *A, size_t lda,
+                   mat_elem_t beta, mat_elem_t *C, size_t ldc);
+/* In-place P*A = L*U with partial pivoting, the same pivot rule as
+ * mat__plu_blocked_ (mat.h:4201-4289: first index of max |a|, pivots with
+ * |a| < MAT_DEFAULT_EPSILON swapped but not divided by).  ipiv (device, n
+ * int32) receives the row swapped into position k at step k; perm (device,
+ * n int32, may be NULL) receives mat_plu's permutation: perm[i] = source row
+ * of row i (mat.h:4227-4229). */
+int matgb_getrf_dev(size_t n, mat_elem_t *A, size_t lda, int32_t *ipiv,
+                    int32_t *perm);
+/* X (n x nrhs) = A^{-1} B from getrf output: X = B[perm] then unit-lower and
+ * upper triangular solves (mat_solve's steps, mat.h:4825-4830, for many
+ * columns).  B is not modified; X must not alias B. */
+int matgb_getrs_dev(size_t n, size_t nrhs, const mat_elem_t *LU, size_t lda,
+                    const int32_t *perm, const mat_elem_t *B, size_t ldb,
+                    mat_elem_t *X, size_t ldx);
+/* In-place lower Cholesky of A (upper triangle not referenced).  info
+ * (device int32) gets 0, or j+1 for the first column j whose diagonal was
+ * <= 0 (mat.h:6046-6048 returns -1 there). */
+int matgb_potrf_dev(size_t n, mat_elem_t *A, size_t lda, int32_t *info);
+/* B <- A^{-1} B from the potrf factor: L y = b then L^T x = y
+ * (mat_solve_spd's steps, mat.h:4862-4865).  Skips all work when *info != 0
+ * (info may be NULL). */
+int matgb_potrs_dev(size_t n, size_t nrhs, const mat_elem_t *L, size_t lda,
+                    mat_elem_t *B, size_t ldb, const int32_t *info);
+/* Triangular solve with many right-hand sides, in place on B (n x nrhs):
+ * uplo 'L'/'U', trans 'N'/'T', diag 'N'/'U'.  Covers mat_solve_tril ('L','N',
+ * 'N'), _tril_unit ('L','N','U'), _triu ('U','N','N') and _trilt ('L','T',
+ * 'N'), mat.h:4580-4803.  Non-unit diagonals are divided by, as there. */
+int matgb_trsm_dev(char uplo, char trans, char diag, size_t n, size_t nrhs,
+                   const mat_elem_t *T, size_t ldt, mat_elem_t *B, size_t ldb);
+/* y = alpha*A*x + beta*y (A m x n).  Generalises mat_gemv (mat.h:2137). */
+int matgb_gemv_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
+                   size_t lda, const mat_elem_t *x, mat_elem_t beta,
+                   mat_elem_t *y);
+
+/* ---- Host (Mat) superset ------------------------------------------------- */
+/* AX = B for every column of B (mat_solve reads only column 0, mat.h:4825). */
+void matgb_solve_multi(Mat *X, const Mat *A, const Mat *B);
+/* SPD variant; returns 0 or -1 like mat_solve_spd. */
+int matgb_solve_spd_multi(Mat *X, const Mat *A, const Mat *B);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MATGB_H_ */

@@ -1,0 +1,202 @@
+"""Generate the golden fixtures in tests/golden/ from the REFERENCE ITSELF.
+
+Runs only where the reference source tree is present: it builds
+oracle/_ref/libref_{f32,f64}.so from the reference's own mat.h (oracle/Makefile)
+and records, for each fixture input, the reference's outputs.
+
+Fixtures:
+  kat_<prec>.npz  -- the known-answer inputs of the reference's unit tests
+                     (tests/test_mat_{plu,solve,chol,solve_spd,solve_tri,mul}.c)
+                     with the reference's outputs.
+  rand_<prec>.npz -- the reference tests' srand(42) random inputs, regenerated
+                     with the same glibc rand() call sequence, plus outputs.
+  c1_<prec>.npz   -- the 256x256 plain config: A ~ U[-1,1] (seed 1000),
+                     b ~ N(0,1) (seed 2000); mat_mul(A, A), mat_plu(A),
+                     mat_solve(A, b).
+
+Usage: python tests/golden/make_golden.py [reference_dir]
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import loader  # noqa: E402
+from libmat_gb300 import rng  # noqa: E402
+
+
+def rm(rows, cols, vals, dt):
+    """mat_from: row-major C initialiser -> column-major array."""
+    return np.array(vals, dtype=dt).reshape(rows, cols)
+
+
+def kat(R, dt):
+    out = {}
+    # tests/test_mat_plu.c:17-80
+    for name, A in (("plu_2x2", rm(2, 2, [4, 3, 6, 3], dt)),
+                    ("plu_3x3", rm(3, 3, [1, 2, 3, 0, 1, 4, 5, 6, 0], dt))):
+        L, U, p, s = R.plu(A)
+        out.update({name + "_A": A, name + "_L": L, name + "_U": U,
+                    name + "_p": p, name + "_s": np.int64(s)})
+    # tests/test_mat_solve.c:7-77, 120-136
+    solves = {
+        "solve_1x1": (rm(1, 1, [5], dt), [15]),
+        "solve_identity": (np.eye(3, dtype=dt), [1, 2, 3]),
+        "solve_2x2": (rm(2, 2, [2, 3, 4, 5], dt), [8, 14]),
+        "solve_3x3": (rm(3, 3, [1, 2, 3, 0, 1, 4, 5, 6, 0], dt), [14, 14, 17]),
+    }
+    for name, (A, b) in solves.items():
+        b = np.array(b, dt)
+        out.update({name + "_A": A, name + "_b": b, name + "_x": R.solve(A, b)})
+    # tests/test_mat_chol.c:45-151
+    chols = {
+        "chol_2x2_identity": np.eye(2, dtype=dt),
+        "chol_2x2_known": rm(2, 2, [4, 2, 2, 5], dt),
+        "chol_3x3_known": rm(3, 3, [4, 12, -16, 12, 37, -43, -16, -43, 98], dt),
+        "chol_not_spd": rm(2, 2, [1, 2, 2, 1], dt),
+    }
+    for name, A in chols.items():
+        L, r = R.chol(A)
+        out.update({name + "_A": A, name + "_L": L, name + "_r": np.int64(r)})
+    # tests/test_mat_solve_spd.c:28-122, 157-174
+    spds = {
+        "spd_1x1": (rm(1, 1, [4], dt), [12]),
+        "spd_identity": (np.eye(3, dtype=dt), [1, 2, 3]),
+        "spd_2x2": (rm(2, 2, [4, 2, 2, 3], dt), [8, 8]),
+        "spd_3x3": (rm(3, 3, [5, 4, 1, 4, 6, 4, 1, 4, 5], dt), [16, 28, 24]),
+        "spd_not_spd": (rm(2, 2, [1, 2, 2, 1], dt), [1, 1]),
+    }
+    for name, (A, b) in spds.items():
+        b = np.array(b, dt)
+        x, r = R.solve_spd(A, b)
+        out.update({name + "_A": A, name + "_b": b, name + "_x": x,
+                    name + "_r": np.int64(r)})
+    # tests/test_mat_solve_tri.c:7-123
+    tris = {
+        "tril_2x2": ("solve_tril", rm(2, 2, [2, 0, 3, 4], dt), [2, 11]),
+        "tril_unit_2x2": ("solve_tril_unit", rm(2, 2, [1, 0, 3, 1], dt), [1, 5]),
+        "triu_2x2": ("solve_triu", rm(2, 2, [2, 3, 0, 4], dt), [8, 8]),
+        "trilt_2x2": ("solve_trilt", rm(2, 2, [2, 0, 3, 4], dt), [8, 8]),
+        "tril_3x3": ("solve_tril", rm(3, 3, [2, 0, 0, 1, 3, 0, 4, 2, 5], dt),
+                     [2, 7, 23]),
+    }
+    for name, (fn, T, b) in tris.items():
+        b = np.array(b, dt)
+        out.update({name + "_T": T, name + "_b": b,
+                    name + "_x": getattr(R, fn)(T, b)})
+    # tests/test_mat_mul.c:6-90
+    muls = {
+        "mul_basic": (rm(2, 2, [1, 2, 3, 4], dt), rm(2, 2, [5, 6, 7, 8], dt)),
+        "mul_identity": (rm(2, 2, [1, 2, 3, 4], dt), np.eye(2, dtype=dt)),
+        "mul_rect": (rm(2, 3, [1, 2, 3, 4, 5, 6], dt),
+                     rm(3, 2, [7, 8, 9, 10, 11, 12], dt)),
+        "mul_vector": (rm(2, 2, [1, 2, 3, 4], dt), rm(2, 1, [5, 6], dt)),
+    }
+    for name, (a, b) in muls.items():
+        out.update({name + "_a": a, name + "_b": b, name + "_c": R.mul(a, b)})
+    return out
+
+
+def crand(R, dt, div, sub):
+    return dt(dt(R.rand() % 100) / dt(div) - dt(sub))
+
+
+def diag_dominant(R, n, dt):
+    """tests/test_mat_plu.c:85-94 and tests/test_mat_solve.c:82-91"""
+    A = np.zeros((n, n), dt, order="F")
+    for i in range(n):
+        s = dt(0)
+        for j in range(n):
+            v = crand(R, dt, 10.0, 5.0)
+            A[i, j] = v
+            if i != j:
+                s = dt(s + abs(v))
+        A[i, i] = dt(s + dt(1.0))
+    return A
+
+
+def rand_fixtures(R, dt):
+    out = {}
+    # tests/test_mat_plu.c:157-167 (srand(42); sizes 10, 50, 100)
+    R.srand(42)
+    for n in (10, 50, 100):
+        A = diag_dominant(R, n, dt)
+        L, U, p, s = R.plu(A)
+        out.update({f"plu{n}_A": A, f"plu{n}_L": L, f"plu{n}_U": U,
+                    f"plu{n}_p": p, f"plu{n}_s": np.int64(s)})
+    # tests/test_mat_solve.c:151-163
+    R.srand(42)
+    for n in (10, 50, 100):
+        A = diag_dominant(R, n, dt)
+        b = np.array([crand(R, dt, 10.0, 0.0) for _ in range(n)], dt)
+        out.update({f"solve{n}_A": A, f"solve{n}_b": b,
+                    f"solve{n}_x": R.solve(A, b)})
+    # tests/test_mat_chol.c:8-29, 203-217: A = B B^T + n I, B filled linearly
+    R.srand(42)
+    for n in (10, 50, 100, 128, 200):
+        B = np.zeros(n * n, dt)
+        for i in range(n * n):
+            B[i] = crand(R, dt, 10.0, 5.0)
+        B = B.reshape(n, n, order="F")
+        A = R.mul(B, np.asfortranarray(B.T))
+        A[np.arange(n), np.arange(n)] += dt(n)
+        L, r = R.chol(A)
+        out.update({f"chol{n}_A": A, f"chol{n}_L": L, f"chol{n}_r": np.int64(r)})
+    # tests/test_mat_solve_spd.c:8-26, 176-186: A = M M^T + 0.1 I
+    R.srand(42)
+    for n in (10, 50, 100):
+        M = np.zeros((n, n), dt, order="F")
+        for i in range(n):
+            for j in range(n):
+                M[i, j] = crand(R, dt, 10.0, 5.0)
+        A = R.mul(M, np.asfortranarray(M.T))
+        A[np.arange(n), np.arange(n)] += dt(0.1)
+        b = np.array([crand(R, dt, 10.0, 0.0) for _ in range(n)], dt)
+        x, r = R.solve_spd(A, b)
+        out.update({f"spd{n}_A": A, f"spd{n}_b": b, f"spd{n}_x": x,
+                    f"spd{n}_r": np.int64(r)})
+    # tests/test_mat_solve_tri.c:125-148, 172-181
+    R.srand(42)
+    for n in (10, 50, 100):
+        L = np.zeros((n, n), dt, order="F")
+        for i in range(n):
+            s = dt(0)
+            for j in range(i):
+                v = crand(R, dt, 100.0, 0.5)
+                L[i, j] = v
+                s = dt(s + abs(v))
+            L[i, i] = dt(s + dt(1.0))
+        b = np.array([crand(R, dt, 10.0, 0.0) for _ in range(n)], dt)
+        out.update({f"trilt{n}_L": L, f"trilt{n}_b": b,
+                    f"trilt{n}_x": R.solve_trilt(L, b)})
+    return out
+
+
+def c1(R, dt):
+    n = 256
+    A = rng.uniform(1000, (n, n), -1.0, 1.0, dt)
+    b = rng.normal(2000, (n,), dt)
+    L, U, p, s = R.plu(A)
+    LU = np.tril(L, -1) + U
+    return {"A": A, "b": b, "AA": R.mul(A, A), "LU": LU, "p": p,
+            "s": np.int64(s), "x": R.solve(A, b)}
+
+
+def main():
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    loader.build(ref_dir)
+    for prec, dt in (("f32", np.float32), ("f64", np.float64)):
+        R = loader.Oracle(prec, "ref")
+        np.savez_compressed(os.path.join(HERE, f"kat_{prec}.npz"), **kat(R, dt))
+        np.savez_compressed(os.path.join(HERE, f"rand_{prec}.npz"),
+                            **rand_fixtures(R, dt))
+        np.savez_compressed(os.path.join(HERE, f"c1_{prec}.npz"), **c1(R, dt))
+        print(prec, "ok")
+
+
+if __name__ == "__main__":
+    main()

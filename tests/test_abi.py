@@ -1,0 +1,125 @@
+"""CPU: the C-ABI libraries load without a GPU and export every function that
+include/*.h declares; the headers compile as C and C++."""
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def declared_functions():
+    names = set()
+    for h in ("mat.h", "matgb.h"):
+        src = open(os.path.join(INCLUDE, h)).read()
+        src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", " ", src)
+        # drop preprocessor lines (with continuations)
+        src = re.sub(r"^\s*#(?:[^\n]*\\\n)*[^\n]*", " ", src, flags=re.M)
+        src = re.sub(r"typedef[^;]*;", " ", src)
+        for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b([A-Za-z_]\w*)\s*\(([^;{}]*)\)\s*;",
+                             src):
+            names.add(m.group(2))
+    names.discard("if")
+    return sorted(names)
+
+
+def test_headers_declare_the_hot_path():
+    names = declared_functions()
+    for f in ("mat_mul", "mat_rmul", "mat_gemm", "mat_syrk", "mat_syrk_t",
+              "mat_plu", "mat_chol", "mat_solve", "mat_solve_spd",
+              "mat_solve_tril", "mat_solve_tril_unit", "mat_solve_triu",
+              "mat_solve_trilt", "matgb_getrf_dev", "matgb_potrf_dev"):
+        assert f in names, f
+
+
+@pytest.fixture(scope="module")
+def libs():
+    import libmat_gb300 as mg
+    out = {}
+    for prec in ("f32", "f64"):
+        path = mg.lib_path(prec)
+        if not os.path.exists(path):
+            mg_build = __import__("libmat_gb300.build", fromlist=["build"])
+            mg_build.build()
+        out[prec] = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
+    return out
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_library_exports_every_declared_symbol(libs, prec):
+    missing = [f for f in declared_functions() if not hasattr(libs[prec], f)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("prec,size", [("f32", 4), ("f64", 8)])
+def test_element_size(libs, prec, size):
+    assert libs[prec].matgb_elem_size() == size
+
+
+def test_host_helpers_without_gpu():
+    """Construction helpers are plain host code (no device needed)."""
+    import libmat_gb300 as mg
+    L = mg.load("f32")
+    c = L.c
+    c.mat_from.restype = ctypes.POINTER(mg.MatStruct)
+    c.mat_from.argtypes = [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p]
+    c.mat_rt.restype = ctypes.POINTER(mg.MatStruct)
+    c.mat_rt.argtypes = [ctypes.POINTER(mg.MatStruct)]
+    c.mat_at.restype = ctypes.c_float
+    c.mat_at.argtypes = [ctypes.POINTER(mg.MatStruct), ctypes.c_size_t,
+                         ctypes.c_size_t]
+    vals = np.array([1, 2, 3, 4, 5, 6], np.float32)  # row-major 2x3
+    m = c.mat_from(2, 3, vals.ctypes.data)
+    assert c.mat_at(m, 0, 2) == 3 and c.mat_at(m, 1, 0) == 4
+    t = c.mat_rt(m)
+    assert t.contents.rows == 3 and c.mat_at(t, 2, 1) == 6
+    c.mat_free_mat(m)
+    c.mat_free_mat(t)
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_headers_compile_as_c_and_cpp(tmp_path):
+    src = tmp_path / "t.c"
+    src.write_text('#include "matgb.h"\nint main(void){Mat m={0,0,0};(void)m;'
+                   'return mat_solve_spd==0;}\n')
+    for cc, flags in (("gcc", ["-std=c99"]), ("g++", ["-x", "c++"])):
+        if shutil.which(cc) is None:
+            continue
+        r = subprocess.run([cc] + flags + ["-I", INCLUDE, "-fsyntax-only",
+                                           str(src)], capture_output=True,
+                           text=True)
+        assert r.returncode == 0, r.stderr
+    src2 = tmp_path / "t2.c"
+    src2.write_text('#define MAT_DOUBLE_PRECISION\n#include "mat.h"\n'
+                    'int main(void){mat_elem_t x=0;return sizeof(x)!=8;}\n')
+    r = subprocess.run(["gcc", "-I", INCLUDE, "-fsyntax-only", str(src2)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+REF_TESTS = ["test_mat_solve.c", "test_mat_chol.c", "test_mat_solve_spd.c",
+             "test_mat_solve_tri.c", "test_mat_mul.c"]
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/tests"),
+                    reason="reference source tree not present on this host")
+@pytest.mark.parametrize("name", REF_TESTS)
+def test_reference_unit_tests_link_against_libmatgb(libs, tmp_path, name):
+    """Drop-in at the source level: the reference's own unit tests for the hot
+    path (they #define MATDEF static inline + MAT_IMPLEMENTATION) compile
+    against include/mat.h and link against libmatgb_f32 unchanged."""
+    import libmat_gb300 as mg
+    out = tmp_path / name.replace(".c", "")
+    r = subprocess.run(
+        ["gcc", "-std=gnu99", "-I", INCLUDE, "-I", "/root/reference/tests",
+         os.path.join("/root/reference/tests", name), "-o", str(out),
+         os.path.join(mg.LIBDIR, "libmatgb_f32.so"), "-lm",
+         "-Wl,-rpath," + mg.LIBDIR], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -1,0 +1,134 @@
+"""CPU: pin the oracle (C restatement of the reference's scalar path) against
+the reference's own outputs -- the committed golden fixtures everywhere, and
+the reference compiled in place (oracle/_ref) where its source tree exists."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle.loader import Oracle, available
+
+PRECS = [("f32", np.float32), ("f64", np.float64)]
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_matches_golden_kat(prec, dt):
+    O = Oracle(prec, "port")
+    g = golden(f"kat_{prec}.npz")
+    for name in ("plu_2x2", "plu_3x3"):
+        L, U, p, s = O.plu(g[name + "_A"])
+        assert np.array_equal(L, g[name + "_L"]) and np.array_equal(U, g[name + "_U"])
+        assert np.array_equal(p, g[name + "_p"]) and s == g[name + "_s"]
+    for name in ("solve_1x1", "solve_identity", "solve_2x2", "solve_3x3"):
+        assert np.array_equal(O.solve(g[name + "_A"], g[name + "_b"]), g[name + "_x"])
+    for name in ("chol_2x2_identity", "chol_2x2_known", "chol_3x3_known",
+                 "chol_not_spd"):
+        L, r = O.chol(g[name + "_A"])
+        assert r == g[name + "_r"] and np.array_equal(L, g[name + "_L"])
+    for name in ("spd_1x1", "spd_identity", "spd_2x2", "spd_3x3", "spd_not_spd"):
+        x, r = O.solve_spd(g[name + "_A"], g[name + "_b"])
+        assert r == g[name + "_r"]
+        if r == 0:
+            assert np.array_equal(x, g[name + "_x"])
+    fns = {"tril_2x2": "solve_tril", "tril_unit_2x2": "solve_tril_unit",
+           "triu_2x2": "solve_triu", "trilt_2x2": "solve_trilt",
+           "tril_3x3": "solve_tril"}
+    for name, fn in fns.items():
+        assert np.array_equal(getattr(O, fn)(g[name + "_T"], g[name + "_b"]),
+                              g[name + "_x"])
+    for name in ("mul_basic", "mul_identity", "mul_rect", "mul_vector"):
+        assert np.array_equal(O.mul(g[name + "_a"], g[name + "_b"]), g[name + "_c"])
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_golden_kat_meets_reference_test_expectations(prec, dt):
+    """The fixtures satisfy the reference tests' own asserts (e.g.
+    tests/test_mat_solve.c:30-31 expects x = [1, 2] within 1e-5)."""
+    g = golden(f"kat_{prec}.npz")
+    assert np.allclose(g["solve_2x2_x"], [1, 2], atol=1e-5)
+    assert np.allclose(g["solve_3x3_x"], [1, 2, 3], atol=1e-4)
+    assert np.allclose(g["solve_1x1_x"], [3], atol=1e-6)
+    assert np.allclose(g["chol_2x2_known_L"], [[2, 0], [1, 2]], atol=1e-5)
+    assert g["chol_not_spd_r"] == -1 and g["spd_not_spd_r"] == -1
+    assert np.allclose(g["tril_3x3_x"], [1, 2, 3], atol=1e-5)
+    assert np.array_equal(g["mul_rect_c"], [[58, 64], [139, 154]])
+    for name in ("plu_2x2", "plu_3x3"):
+        A, L, U, p = (g[name + s] for s in ("_A", "_L", "_U", "_p"))
+        assert np.allclose(A[p], L @ U, atol=1e-5)
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_matches_golden_random(prec, dt):
+    O = Oracle(prec, "port")
+    g = golden(f"rand_{prec}.npz")
+    for n in (10, 50, 100):
+        L, U, p, s = O.plu(g[f"plu{n}_A"])
+        assert np.array_equal(L, g[f"plu{n}_L"]) and np.array_equal(U, g[f"plu{n}_U"])
+        assert np.array_equal(p, g[f"plu{n}_p"]) and s == g[f"plu{n}_s"]
+        assert np.array_equal(O.solve(g[f"solve{n}_A"], g[f"solve{n}_b"]),
+                              g[f"solve{n}_x"])
+        x, r = O.solve_spd(g[f"spd{n}_A"], g[f"spd{n}_b"])
+        assert r == 0 and np.array_equal(x, g[f"spd{n}_x"])
+        assert np.array_equal(O.solve_trilt(g[f"trilt{n}_L"], g[f"trilt{n}_b"]),
+                              g[f"trilt{n}_x"])
+    for n in (10, 50, 100, 128, 200):
+        L, r = O.chol(g[f"chol{n}_A"])
+        assert r == 0 and np.array_equal(L, g[f"chol{n}_L"])
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_matches_golden_c1(prec, dt):
+    """256x256 plain config (U[-1,1] A, N(0,1) b): bit-exact."""
+    O = Oracle(prec, "port")
+    g = golden(f"c1_{prec}.npz")
+    L, U, p, s = O.plu(g["A"])
+    assert np.array_equal(np.tril(L, -1) + U, g["LU"])
+    assert np.array_equal(p, g["p"]) and s == g["s"]
+    assert np.array_equal(O.solve(g["A"], g["b"]), g["x"])
+    assert np.array_equal(O.mul(g["A"], g["A"]), g["AA"])
+
+
+@pytest.mark.skipif(not available("f32", "ref"),
+                    reason="reference source tree not present on this host")
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_matches_reference_live(prec, dt):
+    """Bit-exact against the reference compiled from its own header, on
+    ragged sizes that straddle its 24-column LU blocks."""
+    P, R = Oracle(prec, "port"), Oracle(prec, "ref")
+    rs = np.random.default_rng(7)
+    for n in (1, 2, 5, 23, 24, 25, 47, 49, 97):
+        A = rs.uniform(-1, 1, (n, n)).astype(dt)
+        b = rs.standard_normal(n).astype(dt)
+        a1, a2 = P.plu(A), R.plu(A)
+        for u, v in zip(a1, a2):
+            assert np.array_equal(u, v)
+        assert np.array_equal(P.solve(A, b), R.solve(A, b))
+        S = (A @ A.T + n * np.eye(n)).astype(dt)
+        assert np.array_equal(P.chol(S)[0], R.chol(S)[0])
+        assert np.array_equal(P.solve_spd(S, b)[0], R.solve_spd(S, b)[0])
+        C = rs.standard_normal((n, n)).astype(dt)
+        for up in "LU":
+            assert np.array_equal(P.syrk(C, A, -1.0, 1.0, up), R.syrk(C, A, -1.0, 1.0, up))
+            assert np.array_equal(P.syrk_t(C, A, 2.0, 0.5, up),
+                                  R.syrk_t(C, A, 2.0, 0.5, up))
+        assert np.array_equal(P.gemm(1.5, A, C, 0.5, C), R.gemm(1.5, A, C, 0.5, C))
+        assert np.array_equal(P.gemv(1.0, A, b, 0.0, b), R.gemv(1.0, A, b, 0.0, b))
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_pivot_rules(prec, dt):
+    """Edge cases of the reference's pivot rule (mat.h:1247-1262, 4235): first
+    index on ties, NaN at the top wins, NaN below is ignored, tiny pivots are
+    swapped in but not divided by."""
+    O = Oracle(prec, "port")
+    A = np.array([[1, 1], [-1, 2]], dt)        # |1| == |-1|: keep row 0
+    _, _, p, s = O.plu(A)
+    assert list(p) == [0, 1] and s == 0
+    A = np.array([[np.nan, 1], [5, 2]], dt)    # NaN at the top: pivot 0
+    _, _, p, _ = O.plu(A)
+    assert list(p) == [0, 1]
+    A = np.array([[1, 1], [np.nan, 2]], dt)    # NaN below: ignored
+    _, _, p, _ = O.plu(A)
+    assert list(p) == [0, 1]
+    A = np.array([[1, 2, 3], [2, 4, 6], [3, 6, 10]], dt)  # singular minor
+    M, p, ipiv, s = O.plu_inplace(A)
+    assert list(ipiv) == [2, 2, 2] or ipiv[0] == 2
