@@ -132,6 +132,53 @@ int matgb_gemv_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
                    size_t lda, const mat_elem_t *x, mat_elem_t beta,
                    mat_elem_t *y);
 
+/* ---- Mixed precision: tensor-core LU + iterative refinement -------------- */
+/* Generalises mat_solve (mat.h:4807-4837): the LU runs with FP32 panels and
+ * FP32 trailing matrix, its trailing updates (mat.h:4277-4283) on the tensor
+ * cores in BF16 or FP16 with FP32 accumulation; the residual, correction
+ * update and convergence test run on the GPU in the library's element type
+ * (FP64 in libmatgb_f64). */
+typedef struct {
+  int lp_format; /* 1 = BF16 (default), 0 = FP16 (per-block power-of-2 scale) */
+  int max_iter;  /* refinement solves (default 30)                            */
+  double tol;    /* target backward error; <= 0: n * unit roundoff of the
+                    element type (n * 2^-53 in libmatgb_f64)                   */
+} MatIROpts;
+
+typedef struct {
+  int iterations;        /* LU solves done (1 = no refinement needed)        */
+  int converged;         /* backward_error <= tol                             */
+  int lp_format;
+  double backward_error; /* |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf)      */
+  double residual_inf, x_inf, a_inf, b_inf, tol;
+  double ms_factor;      /* GPU time of the conversion + factorisation        */
+  double ms_refine;      /* GPU time of solves, residuals and updates         */
+} MatIRReport;
+
+void matgb_ir_default_opts(MatIROpts *o);
+/* Solve A x = b (device pointers, A n x n column-major). */
+int matgb_gesv_ir_dev(size_t n, const mat_elem_t *A, size_t lda,
+                      const mat_elem_t *b, mat_elem_t *x,
+                      const MatIROpts *opts, MatIRReport *rep);
+/* Host Mat form; returns 0 or a negative status. */
+int mat_solve_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,
+                 MatIRReport *rep);
+/* The FP32 LU alone (device, in place) with trailing updates on the tensor
+ * cores (lp_format 1 BF16, 0 FP16) or, for lp_format -1, the FP32 SIMT GEMM.
+ * ipiv/perm as matgb_getrf_dev.  Pivots are never skipped (threshold 0). */
+int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
+                       int32_t *perm, int lp_format);
+/* C (fp32, column-major, M x N) = beta*C + alpha * A * B^T with A (M x K) and
+ * B (N x K) K-contiguous BF16 (bf16 != 0) or FP16, K a multiple of 64 and at
+ * most 128, lda/ldb multiples of 8: the tensor-core rank-K update
+ * (tcgen05.mma, TMEM accumulators, TMA-fed) behind the mixed LU. */
+int matgb_tc_gemm_dev(int bf16, size_t M, size_t N, size_t K, const void *A,
+                      size_t lda, const void *B, size_t ldb, float alpha,
+                      float beta, float *C, size_t ldc);
+/* 0, or MATGB_ERR_TIMEOUT if a tensor-core kernel gave up a bounded wait
+ * since the last call (clears the flag; synchronises). */
+int matgb_tc_status(void);
+
 /* ---- Host (Mat) superset ------------------------------------------------- */
 /* AX = B for every column of B (mat_solve reads only column 0, mat.h:4825). */
 void matgb_solve_multi(Mat *X, const Mat *A, const Mat *B);

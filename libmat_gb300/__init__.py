@@ -27,6 +27,23 @@ class PermStruct(C.Structure):
     _fields_ = [("data", C.c_void_p), ("size", C.c_size_t)]
 
 
+class MatIROpts(C.Structure):
+    _fields_ = [("lp_format", C.c_int), ("max_iter", C.c_int),
+                ("tol", C.c_double)]
+
+
+class MatIRReport(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int),
+                ("lp_format", C.c_int), ("backward_error", C.c_double),
+                ("residual_inf", C.c_double), ("x_inf", C.c_double),
+                ("a_inf", C.c_double), ("b_inf", C.c_double),
+                ("tol", C.c_double), ("ms_factor", C.c_double),
+                ("ms_refine", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class MatGBError(RuntimeError):
     pass
 
@@ -122,6 +139,16 @@ class Lib:
             "mat_solve_triu": (None, [MP, MP, MP]),
             "mat_solve_trilt": (None, [MP, MP, MP]),
             "mat_free_mat": (None, [MP]),
+            "matgb_tc_gemm_dev": (_I, [_I, _S, _S, _S, _P, _S, _P, _S,
+                                       C.c_float, C.c_float, _P, _S]),
+            "matgb_tc_status": (_I, []),
+            "matgb_getrf_lp_dev": (_I, [_S, _P, _S, _P, _P, _I]),
+            "matgb_ir_default_opts": (None, [C.POINTER(MatIROpts)]),
+            "matgb_gesv_ir_dev": (_I, [_S, _P, _S, _P, _P,
+                                       C.POINTER(MatIROpts),
+                                       C.POINTER(MatIRReport)]),
+            "mat_solve_ir": (_I, [MP, MP, MP, C.POINTER(MatIROpts),
+                                  C.POINTER(MatIRReport)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(c, name)
@@ -260,6 +287,17 @@ class Lib:
         r = f(C.byref(self.mat(X)), C.byref(self.mat(A)), C.byref(self.mat(B)))
         self.check(0, "solve_multi")
         return (X, int(r)) if spd else X
+
+    def mat_solve_ir(self, A, b, lp_format=1, max_iter=30, tol=0.0):
+        """Mixed-precision LU + refinement; returns (x, report dict)."""
+        A, b = self.arr(A), self.arr(b)
+        x = np.zeros((A.shape[1], 1), self.dtype, order="F")
+        o = MatIROpts(lp_format, max_iter, tol)
+        rep = MatIRReport()
+        rc = self.c.mat_solve_ir(C.byref(self.mat(x)), C.byref(self.mat(A)),
+                                 C.byref(self.mat(b)), C.byref(o), C.byref(rep))
+        self.check(rc, "mat_solve_ir")
+        return x.reshape(-1), rep.as_dict()
 
     # --------------------------------------------------- device helpers
     def dalloc(self, nbytes):

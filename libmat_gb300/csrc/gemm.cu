@@ -138,38 +138,37 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
   }
 }
 
-template <bool TA, bool TB, int TRI>
-static int launch_gemm(int64_t m, int64_t n, int64_t k, elem_t alpha,
-                       const elem_t *A, int64_t lda, const elem_t *B,
-                       int64_t ldb, elem_t beta, elem_t *C, int64_t ldc,
-                       const int32_t *skip) {
-  using G = GemmCfg<elem_t>;
+template <typename T, bool TA, bool TB, int TRI>
+static int launch_gemm(int64_t m, int64_t n, int64_t k, T alpha, const T *A,
+                       int64_t lda, const T *B, int64_t ldb, T beta, T *C,
+                       int64_t ldc, const int32_t *skip) {
+  using G = GemmCfg<T>;
   Ctx *c = ctx();
   dim3 grid((unsigned)((m + G::BM - 1) / G::BM),
             (unsigned)((n + G::BN - 1) / G::BN));
   constexpr int threads = (G::BM / G::TM) * (G::BN / G::TN);
   const double fl = 2.0 * m * n * k * (TRI ? 0.5 : 1.0);
-  const double by = (double)sizeof(elem_t) *
-                    (m * k + k * n + (beta != elem_t(0) ? 2.0 : 1.0) * m * n *
+  const double by = (double)sizeof(T) *
+                    (m * k + k * n + (beta != T(0) ? 2.0 : 1.0) * m * n *
                                          (TRI ? 0.5 : 1.0));
-  KtScope kt("gemm_simt", fl, by);
-  gemm_kernel<elem_t, G::BM, G::BN, G::BK, G::TM, G::TN, TA, TB, TRI>
+  KtScope kt(sizeof(T) == 4 ? "gemm_simt_f32" : "gemm_simt_f64", fl, by);
+  gemm_kernel<T, G::BM, G::BN, G::BK, G::TM, G::TN, TA, TB, TRI>
       <<<grid, threads, 0, c->stream>>>(m, n, k, alpha, A, lda, B, ldb, beta,
                                         C, ldc, skip);
   MGB_LAUNCHED("gemm_simt");
   return 0;
 }
 
-int gemm_skip(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
-              const elem_t *A, int64_t lda, const elem_t *B, int64_t ldb,
-              elem_t beta, elem_t *C, int64_t ldc, int tri,
-              const int32_t *skip) {
+template <typename T>
+int gemm_skip_t(bool ta, bool tb, int64_t m, int64_t n, int64_t k, T alpha,
+                const T *A, int64_t lda, const T *B, int64_t ldb, T beta, T *C,
+                int64_t ldc, int tri, const int32_t *skip) {
   if (!ctx()) return MATGB_ERR_NO_DEVICE;
   if (m <= 0 || n <= 0) return 0;
 #define MGB_G(TA_, TB_, TRI_)                                                  \
   if (ta == TA_ && tb == TB_ && tri == TRI_)                                   \
-    return launch_gemm<TA_, TB_, TRI_>(m, n, k, alpha, A, lda, B, ldb, beta,   \
-                                       C, ldc, skip);
+    return launch_gemm<T, TA_, TB_, TRI_>(m, n, k, alpha, A, lda, B, ldb,      \
+                                          beta, C, ldc, skip);
   MGB_G(false, false, 0)
   MGB_G(true, false, 0)
   MGB_G(false, true, 0)
@@ -180,6 +179,22 @@ int gemm_skip(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
   MGB_G(true, false, 2)
 #undef MGB_G
   return set_error(MATGB_ERR_ARG, "gemm: unsupported variant");
+}
+
+template int gemm_skip_t<float>(bool, bool, int64_t, int64_t, int64_t, float,
+                                const float *, int64_t, const float *, int64_t,
+                                float, float *, int64_t, int, const int32_t *);
+template int gemm_skip_t<double>(bool, bool, int64_t, int64_t, int64_t, double,
+                                 const double *, int64_t, const double *,
+                                 int64_t, double, double *, int64_t, int,
+                                 const int32_t *);
+
+int gemm_skip(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
+              const elem_t *A, int64_t lda, const elem_t *B, int64_t ldb,
+              elem_t beta, elem_t *C, int64_t ldc, int tri,
+              const int32_t *skip) {
+  return gemm_skip_t<elem_t>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C,
+                             ldc, tri, skip);
 }
 
 int gemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
@@ -194,34 +209,37 @@ int gemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
 // so the result does not depend on scheduling.
 constexpr int kGemvRows = 256;
 
+template <typename T>
 __global__ void __launch_bounds__(kGemvRows)
     gemv_partial_kernel(int64_t m, int64_t n, int64_t cols_per,
-                        const elem_t *__restrict__ A, int64_t lda,
-                        const elem_t *__restrict__ x, elem_t *__restrict__ P) {
+                        const T *__restrict__ A, int64_t lda,
+                        const T *__restrict__ x, T *__restrict__ P) {
   const int64_t i = (int64_t)blockIdx.x * kGemvRows + threadIdx.x;
   const int64_t j0 = (int64_t)blockIdx.y * cols_per;
   int64_t j1 = j0 + cols_per;
   if (j1 > n) j1 = n;
   if (i >= m) return;
-  elem_t s = 0;
+  T s = 0;
   for (int64_t j = j0; j < j1; j++) s = fma(A[j * lda + i], x[j], s);
   P[(int64_t)blockIdx.y * m + i] = s;
 }
 
-__global__ void gemv_reduce_kernel(int64_t m, int chunks, elem_t alpha,
-                                   const elem_t *__restrict__ P, elem_t beta,
-                                   elem_t *__restrict__ y) {
+template <typename T>
+__global__ void gemv_reduce_kernel(int64_t m, int chunks, T alpha,
+                                   const T *__restrict__ P, T beta,
+                                   T *__restrict__ y) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  elem_t s = 0;
+  T s = 0;
   for (int c = 0; c < chunks; c++) s += P[(int64_t)c * m + i];
-  elem_t v = alpha * s;
-  if (beta != elem_t(0)) v = beta * y[i] + v;
+  T v = alpha * s;
+  if (beta != T(0)) v = beta * y[i] + v;
   y[i] = v;
 }
 
-int gemv(int64_t m, int64_t n, elem_t alpha, const elem_t *A, int64_t lda,
-         const elem_t *x, elem_t beta, elem_t *y) {
+template <typename T>
+int gemv_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda, const T *x,
+           T beta, T *y) {
   Ctx *c = ctx();
   if (!c) return MATGB_ERR_NO_DEVICE;
   if (m <= 0) return 0;
@@ -232,19 +250,28 @@ int gemv(int64_t m, int64_t n, elem_t alpha, const elem_t *A, int64_t lda,
   if (chunks > 1024) chunks = 1024;
   int64_t cols_per = n > 0 ? (n + chunks - 1) / chunks : 0;
   chunks = cols_per > 0 ? (n + cols_per - 1) / cols_per : 1;
-  elem_t *P = (elem_t *)ws(WS_T3, (size_t)(chunks * m) * sizeof(elem_t));
+  T *P = (T *)ws(WS_T3, (size_t)(chunks * m) * sizeof(T));
   if (!P) return MATGB_ERR_NOMEM;
   if (n > 0) {
-    gemv_partial_kernel<<<dim3((unsigned)rb, (unsigned)chunks), kGemvRows, 0,
+    gemv_partial_kernel<T><<<dim3((unsigned)rb, (unsigned)chunks), kGemvRows, 0,
                           c->stream>>>(m, n, cols_per, A, lda, x, P);
     MGB_LAUNCHED("gemv_partial");
   } else {
-    MGB_CUDA(cudaMemsetAsync(P, 0, (size_t)m * sizeof(elem_t), c->stream));
+    MGB_CUDA(cudaMemsetAsync(P, 0, (size_t)m * sizeof(T), c->stream));
   }
-  gemv_reduce_kernel<<<(unsigned)((m + 255) / 256), 256, 0, c->stream>>>(
+  gemv_reduce_kernel<T><<<(unsigned)((m + 255) / 256), 256, 0, c->stream>>>(
       m, (int)chunks, alpha, P, beta, y);
   MGB_LAUNCHED("gemv_reduce");
   return 0;
+}
+template int gemv_t<float>(int64_t, int64_t, float, const float *, int64_t,
+                           const float *, float, float *);
+template int gemv_t<double>(int64_t, int64_t, double, const double *, int64_t,
+                            const double *, double, double *);
+
+int gemv(int64_t m, int64_t n, elem_t alpha, const elem_t *A, int64_t lda,
+         const elem_t *x, elem_t beta, elem_t *y) {
+  return gemv_t<elem_t>(m, n, alpha, A, lda, x, beta, y);
 }
 
 }  // namespace mgb

@@ -49,7 +49,7 @@ struct KtScope {
 // counterpart of the reference's scratch arena, mat.h:865-895).
 enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
-  WS_T0, WS_T1, WS_T2, WS_T3, WS_NSLOTS
+  WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_NSLOTS
 };
 void *ws(int slot, size_t bytes);
 
@@ -87,6 +87,42 @@ int gemm_skip(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
               const int32_t *skip);
 int gemv(int64_t m, int64_t n, elem_t alpha, const elem_t *A, int64_t lda,
          const elem_t *x, elem_t beta, elem_t *y);
+// Element-type templates (float and double are instantiated in every build;
+// the mixed-precision solvers use the float ones inside the double library).
+template <typename T>
+int gemm_skip_t(bool ta, bool tb, int64_t m, int64_t n, int64_t k, T alpha,
+                const T *A, int64_t lda, const T *B, int64_t ldb, T beta, T *C,
+                int64_t ldc, int tri, const int32_t *skip);
+template <typename T>
+int gemv_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda, const T *x,
+           T beta, T *y);
+template <typename T>
+int trsm_left_t(bool lower, bool trans, bool unit, int64_t n, int64_t nrhs,
+                const T *Tm, int64_t ldt, T *B, int64_t ldb,
+                const int32_t *info);
+template <typename T>
+int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
+            const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm);
+template <typename T>
+int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
+               T eps, int *w_used);
+// lp: -1 = trailing updates by the SIMT GEMM in T; 0 = FP16, 1 = BF16
+// tensor-core updates (T = float only; FP32 panels and trailing matrix).
+template <typename T>
+int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
+            int lp);
+// Tensor-core trailing update of columns [c0,c1) after outer block [kb,ke)
+// (mixed.cu); pack = pack L21 and all of U12[:, ke:n] to 16 bits first.
+int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
+                       int64_t ke, int64_t c0, int64_t c1, int lp, bool pack);
+template <typename T>
+int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
+            const int32_t *perm, const T *B, int64_t ldb, T *X, int64_t ldx);
+// Tensor-core rank-K update (tc_gemm.cu).
+int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
+            int64_t lda, const void *B, int64_t ldb, float alpha,
+            const float *alpha_scale, float beta, float *C, int64_t ldc);
+int tc_error_flag(int clear);
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm);
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,
           const int32_t *perm, const elem_t *B, int64_t ldb, elem_t *X,

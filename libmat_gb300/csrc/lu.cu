@@ -17,10 +17,15 @@
 //    (DSMEM stores), one hardware cluster barrier, then every CTA picks the
 //    winner, swaps, scales and updates its own rows.  Two barriers per column
 //    (one CTA-local, one cluster-wide); no global-memory round trip.
-//  * Outer blocks of 96 columns: after each inner panel the swaps go to the
-//    rest of the outer block, then a TRSM and a skinny GEMM; after each outer
-//    block the swaps go to all other columns (and to the permutation vector),
-//    then TRSM for U12 and the big GEMM (K = 96) for the trailing matrix.
+//  * Row swaps (laswp): one warp turns a block's swap sequence into a net
+//    row mapping (touched rows -> source rows); every CTA then gathers the
+//    touched rows of 32 columns into shared memory with all loads in flight
+//    and writes them back permuted.
+//  * U12 = L11^{-1} A12: one thread per right-hand-side column, the column in
+//    registers and L11 in shared memory (no block barriers).
+//  * Outer blocks of 96 columns with look-ahead: the panel chain runs on a
+//    high-priority stream while the previous block's trailing GEMM runs on
+//    the library stream; events order the two.
 #include <cooperative_groups.h>
 #include <limits.h>
 
@@ -33,45 +38,50 @@ namespace mgb {
 constexpr int kPanelThreads = 512;
 constexpr int kPanelWarps = kPanelThreads / 32;
 constexpr int kRefBlock = 24;  // MAT_PLU_BLOCK_SIZE, mat.h:4196
-constexpr int kOuterBlock = 96;
+constexpr int kOuterBlock = 96;   // plain path (SIMT trailing GEMM)
+constexpr int kOuterBlockLp = 128;  // tensor-core path (K of tc_gemm)
 constexpr int kSmemMax = 227 * 1024;
 
-__device__ __forceinline__ elem_t piv_key(elem_t v, bool first) {
+template <typename T>
+__device__ __forceinline__ T piv_key(T v, bool first) {
   // Reproduces mat__amax_scalar + mat__iamax on NaNs: a NaN at the first
   // position wins (max becomes NaN, no index compares equal, index 0 is
   // returned); NaNs elsewhere never win.
-  elem_t a = fabs(v);
-  if (a != a) return first ? (elem_t)INFINITY : (elem_t)-1;
+  T a = fabs(v);
+  if (a != a) return first ? (T)INFINITY : (T)-1;
   return a;
 }
 
-__device__ __forceinline__ bool better(elem_t k1, int i1, elem_t k2, int i2) {
+template <typename T>
+__device__ __forceinline__ bool better(T k1, int i1, T k2, int i2) {
   return k1 > k2 || (k1 == k2 && i1 < i2);
 }
 
+template <typename T>
 static size_t panel_smem(int cs, int w, int rpc) {
   size_t t = (size_t)w * rpc + kPanelWarps + 2 * cs + 2 * (size_t)cs * w +
              2 * (size_t)w;
-  return t * sizeof(elem_t) + (kPanelWarps + 2 * cs) * sizeof(int);
+  return t * sizeof(T) + (kPanelWarps + 2 * cs) * sizeof(int);
 }
 
 // Factor rows [k0, n) x columns [k0, k0+w) of A in place.  ipiv[k0+kk] gets
 // the global row swapped into row k0+kk.  One cluster; CTA c holds panel rows
 // [c*rpc, (c+1)*rpc).  Thread tid owns local rows tid, tid+512, ...
+template <typename T>
 __global__ void __launch_bounds__(kPanelThreads, 1)
-    lu_panel_kernel(elem_t *__restrict__ A, int64_t lda, int64_t n, int64_t k0,
-                    int w, int rpc, int32_t *__restrict__ ipiv) {
+    lu_panel_kernel(T *__restrict__ A, int64_t lda, int64_t n, int64_t k0,
+                    int w, int rpc, int32_t *__restrict__ ipiv, T eps) {
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
   const int c = (int)cluster.block_rank();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t m = n - k0;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  elem_t *P = (elem_t *)smem_raw;
-  elem_t *wkey = P + (size_t)w * rpc;
-  elem_t *xkey = wkey + kPanelWarps;
-  elem_t *xval = xkey + 2 * CS;
-  elem_t *kval = xval + 2 * (size_t)CS * w;
+  T *P = (T *)smem_raw;
+  T *wkey = P + (size_t)w * rpc;
+  T *xkey = wkey + kPanelWarps;
+  T *xval = xkey + 2 * CS;
+  T *kval = xval + 2 * (size_t)CS * w;
   int *widx = (int *)(kval + 2 * w);
   int *xidx = widx + kPanelWarps;
 
@@ -79,18 +89,18 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
   for (int r = tid; r < rpc; r += kPanelThreads) {
     const int64_t pr = rbase + r;
     for (int j = 0; j < w; j++)
-      P[(size_t)j * rpc + r] = pr < m ? A[(k0 + pr) + (k0 + j) * lda] : elem_t(0);
+      P[(size_t)j * rpc + r] = pr < m ? A[(k0 + pr) + (k0 + j) * lda] : T(0);
   }
 
   for (int kk = 0; kk < w; kk++) {
     const int buf = kk & 1;
     // 1. arg-max of |P[kk][r]| over my rows with panel row >= kk
-    elem_t bk = (elem_t)-2;
+    T bk = (T)-2;
     int bi = INT_MAX;
     for (int r = tid; r < rpc; r += kPanelThreads) {
       const int64_t pr = rbase + r;
       if (pr >= kk && pr < m) {
-        elem_t key = piv_key(P[(size_t)kk * rpc + r], pr == kk);
+        T key = piv_key(P[(size_t)kk * rpc + r], pr == kk);
         if (better(key, (int)pr, bk, bi)) {
           bk = key;
           bi = (int)pr;
@@ -99,7 +109,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      elem_t ok = __shfl_down_sync(0xffffffffu, bk, off);
+      T ok = __shfl_down_sync(0xffffffffu, bk, off);
       int oi = __shfl_down_sync(0xffffffffu, bi, off);
       if (better(ok, oi, bk, bi)) {
         bk = ok;
@@ -111,7 +121,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
       widx[warp] = bi;
     }
     __syncthreads();
-    elem_t ck = wkey[0];
+    T ck = wkey[0];
     int ci = widx[0];
 #pragma unroll
     for (int q = 1; q < kPanelWarps; q++)
@@ -126,26 +136,26 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
     for (int t = tid; t < total; t += kPanelThreads) {
       if (t < nval) {
         const int q = t / w, j = t % w;
-        elem_t v = (ci != INT_MAX) ? P[(size_t)j * rpc + (ci - rbase)] : elem_t(0);
-        elem_t *dst = cluster.map_shared_rank(xval, q);
+        T v = (ci != INT_MAX) ? P[(size_t)j * rpc + (ci - rbase)] : T(0);
+        T *dst = cluster.map_shared_rank(xval, q);
         dst[((size_t)buf * CS + c) * w + j] = v;
       } else if (t < nval + CS) {
         const int q = t - nval;
-        elem_t *dk = cluster.map_shared_rank(xkey, q);
+        T *dk = cluster.map_shared_rank(xkey, q);
         int *di = cluster.map_shared_rank(xidx, q);
         dk[buf * CS + c] = ck;
         di[buf * CS + c] = ci;
       } else {
         const int u = t - nval - CS;
         const int q = u / w, j = u % w;
-        elem_t *dst = cluster.map_shared_rank(kval, q);
+        T *dst = cluster.map_shared_rank(kval, q);
         dst[(size_t)buf * w + j] = P[(size_t)j * rpc + (kk - rbase)];
       }
     }
     cluster.sync();
     // 3. winner over the cluster (every thread, same answer)
     int wc = 0;
-    elem_t gk = xkey[buf * CS];
+    T gk = xkey[buf * CS];
     int gi = xidx[buf * CS];
     for (int q = 1; q < CS; q++)
       if (better(xkey[buf * CS + q], xidx[buf * CS + q], gk, gi)) {
@@ -153,8 +163,8 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
         gi = xidx[buf * CS + q];
         wc = q;
       }
-    const elem_t *u = xval + ((size_t)buf * CS + wc) * w;
-    const elem_t *kv = kval + (size_t)buf * w;
+    const T *u = xval + ((size_t)buf * CS + wc) * w;
+    const T *kv = kval + (size_t)buf * w;
     const int p = gi;
     if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
     // 4. swap rows kk and p (only the owning threads touch them)
@@ -165,13 +175,13 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
         for (int j = 0; j < w; j++) P[(size_t)j * rpc + (kk - rbase)] = u[j];
     }
     // 5. scale column kk and rank-1 update of the panel's later columns
-    const elem_t piv = u[kk];
-    if (!(fabs(piv) < kPivotEps)) {
-      const elem_t inv = elem_t(1) / piv;
+    const T piv = u[kk];
+    if (!(fabs(piv) < eps)) {
+      const T inv = T(1) / piv;
       for (int r = tid; r < rpc; r += kPanelThreads) {
         const int64_t pr = rbase + r;
         if (pr > kk && pr < m) {
-          const elem_t l = P[(size_t)kk * rpc + r] * inv;
+          const T l = P[(size_t)kk * rpc + r] * inv;
           P[(size_t)kk * rpc + r] = l;
           for (int j = kk + 1; j < w; j++)
             P[(size_t)j * rpc + r] = fma(-u[j], l, P[(size_t)j * rpc + r]);
@@ -187,42 +197,170 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
   }
 }
 
-// Apply the swaps ipiv[k1..k2) (global row indices) in order to columns
-// [c0,c1) and [c2,c3), and, if perm is given, to the permutation vector.
-__global__ void laswp_kernel(elem_t *__restrict__ A, int64_t lda, int64_t c0,
-                             int64_t c1, int64_t c2, int64_t c3,
-                             const int32_t *__restrict__ ipiv, int64_t k1,
-                             int64_t k2, int32_t *__restrict__ perm) {
-  __shared__ int32_t sp[kOuterBlock];
+// ---- row swaps ----------------------------------------------------------------
+// Net effect of the swap sequence ipiv[k1..k2) (global row indices, each
+// ipiv[k] >= k) on rows: after it, row pos[t] holds the original row src[t]
+// for t < cnt; every other row is unchanged.  Built by one warp in shared
+// memory: positions [k1,k2) are indexed directly, pivot rows beyond k2 are
+// found by a warp-wide search.
+constexpr int kSwapMax = 128;
+
+struct SwapMap {
+  int32_t pos[2 * kSwapMax];
+  int32_t src[2 * kSwapMax];
+  int cnt;
+};
+
+__device__ void build_swap_map(SwapMap &sm, const int32_t *__restrict__ ipiv,
+                               int64_t k1, int64_t k2) {
+  const int lane = threadIdx.x & 31;
   const int nk = (int)(k2 - k1);
-  for (int i = threadIdx.x; i < nk; i += blockDim.x) sp[i] = ipiv[k1 + i];
-  __syncthreads();
-  const int64_t na = c1 - c0, nb = c3 - c2;
-  const int64_t total = na + nb + (perm ? 1 : 0);
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    if (t < na + nb) {
-      const int64_t col = t < na ? c0 + t : c2 + (t - na);
-      elem_t *a = A + col * lda;
-      for (int i = 0; i < nk; i++) {
-        const int64_t k = k1 + i, p = sp[i];
-        if (p != k) {
-          elem_t x = a[k];
-          a[k] = a[p];
-          a[p] = x;
-        }
-      }
-    } else {
-      for (int i = 0; i < nk; i++) {
-        const int64_t k = k1 + i, p = sp[i];
-        if (p != k) {
-          int32_t x = perm[k];
-          perm[k] = perm[p];
-          perm[p] = x;
-        }
-      }
-    }
+  for (int i = lane; i < nk; i += 32) {
+    sm.pos[i] = (int32_t)(k1 + i);
+    sm.src[i] = (int32_t)(k1 + i);
   }
+  __syncwarp();
+  int nx = 0;  // extra rows (>= k2) at pos[nk .. nk+nx)
+  for (int i = 0; i < nk; i++) {
+    const int32_t k = (int32_t)(k1 + i);
+    const int32_t p = ipiv[k1 + i];
+    if (p == k) continue;
+    int slot;
+    if (p < k2) {
+      slot = p - (int32_t)k1;
+    } else {
+      int found = -1;
+      for (int base = 0; base < nx; base += 32) {
+        const int t = base + lane;
+        unsigned m = __ballot_sync(0xffffffffu, t < nx && sm.pos[nk + t] == p);
+        if (m) {
+          found = base + __ffs(m) - 1;
+          break;
+        }
+      }
+      if (found < 0) {
+        if (lane == 0) {
+          sm.pos[nk + nx] = p;
+          sm.src[nk + nx] = p;
+        }
+        __syncwarp();
+        found = nx++;
+      }
+      slot = nk + found;
+    }
+    if (lane == 0) {
+      int32_t t = sm.src[i];
+      sm.src[i] = sm.src[slot];
+      sm.src[slot] = t;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) sm.cnt = nk + nx;
+}
+
+// Apply the row mapping to columns [c0,c1) and [c2,c3) (LC per CTA) and, on
+// CTA 0, to the permutation vector.
+template <typename T>
+struct SwapCols {
+  static constexpr int LC = sizeof(T) == 4 ? 16 : 8;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    laswp_kernel(T *__restrict__ A, int64_t lda, int64_t c0, int64_t c1,
+                 int64_t c2, int64_t c3, const int32_t *__restrict__ ipiv,
+                 int64_t k1, int64_t k2, int32_t *__restrict__ perm) {
+  constexpr int LC = SwapCols<T>::LC;
+  constexpr int RG = 256 / LC;
+  __shared__ SwapMap sm;
+  __shared__ T vals[2 * kSwapMax][LC + 1];
+  __shared__ int32_t pv[2 * kSwapMax];
+  if (threadIdx.x < 32) build_swap_map(sm, ipiv, k1, k2);
+  __syncthreads();
+  const int cnt = sm.cnt;
+  const int64_t na = c1 - c0, nb = c3 - c2;
+  const int tid = threadIdx.x, lc = tid % LC, rg = tid / LC;
+  const int64_t t = (int64_t)blockIdx.x * LC + lc;
+  const bool ok = t < na + nb;
+  T *colp = ok ? A + (t < na ? c0 + t : c2 + (t - na)) * lda : nullptr;
+  for (int r = rg; r < cnt; r += RG)
+    if (ok) vals[r][lc] = colp[sm.src[r]];
+  if (blockIdx.x == 0 && perm)
+    for (int r = tid; r < cnt; r += 256) pv[r] = perm[sm.src[r]];
+  __syncthreads();
+  for (int r = rg; r < cnt; r += RG)
+    if (ok) colp[sm.pos[r]] = vals[r][lc];
+  if (blockIdx.x == 0 && perm)
+    for (int r = tid; r < cnt; r += 256) perm[sm.pos[r]] = pv[r];
+}
+
+template <typename T>
+int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
+            const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm) {
+  const int64_t ncol = (c1 - c0) + (c3 - c2);
+  if (k2 <= k1 || (ncol <= 0 && !perm)) return 0;
+  if (k2 - k1 > kSwapMax) return set_error(MATGB_ERR_ARG, "laswp: block > 128");
+  constexpr int LC = SwapCols<T>::LC;
+  int64_t blocks = (ncol + LC - 1) / LC;
+  if (blocks < 1) blocks = 1;
+  KtScope kt("laswp", 0.0, 4.0 * (k2 - k1) * ncol * sizeof(T));
+  laswp_kernel<T><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
+      A, lda, c0, c1, c2, c3, ipiv, k1, k2, perm);
+  MGB_LAUNCHED("laswp");
+  return 0;
+}
+
+// ---- U12 = L11^{-1} A12 with L11 unit lower (TB x TB) ----------------------
+// One thread per right-hand-side column; the column lives in registers and
+// the substitution runs in the reference's axpy order (mat.h:4264-4271).
+template <typename T, int TB>
+__global__ void __launch_bounds__(64)
+    trsm_unit_reg_kernel(const T *__restrict__ L, int64_t ldl, T *__restrict__ B,
+                         int64_t ldb, int64_t ncols) {
+  __shared__ T Ls[TB][TB + 1];
+  for (int e = threadIdx.x; e < TB * TB; e += 64) {
+    const int i = e % TB, j = e / TB;
+    Ls[j][i] = L[i + (int64_t)j * ldl];
+  }
+  __syncthreads();
+  const int64_t col = (int64_t)blockIdx.x * 64 + threadIdx.x;
+  if (col >= ncols) return;
+  T *b = B + col * ldb;
+  T x[TB];
+#pragma unroll
+  for (int i = 0; i < TB; i++) x[i] = b[i];
+#pragma unroll
+  for (int k = 0; k < TB; k++)
+#pragma unroll
+    for (int i = k + 1; i < TB; i++) x[i] = fma(-Ls[k][i], x[k], x[i]);
+#pragma unroll
+  for (int i = 1; i < TB; i++) b[i] = x[i];
+}
+
+template <typename T>
+static int trsm_unit_lower(int tb, int64_t ncols, const T *L, int64_t ldl, T *B,
+                           int64_t ldb) {
+  if (ncols <= 0 || tb <= 1) return 0;
+  const unsigned grid = (unsigned)((ncols + 63) / 64);
+  if (tb == kOuterBlock && sizeof(T) == 4) {
+    KtScope kt("trsm_lu", (double)tb * tb * ncols, (double)sizeof(T) * 2.0 * tb * ncols);
+    trsm_unit_reg_kernel<T, kOuterBlock><<<grid, 64, 0, ctx()->stream>>>(L, ldl, B, ldb, ncols);
+    MGB_LAUNCHED("trsm_lu");
+    return 0;
+  }
+  if (tb == kRefBlock) {
+    KtScope kt("trsm_lu", (double)tb * tb * ncols, (double)sizeof(T) * 2.0 * tb * ncols);
+    trsm_unit_reg_kernel<T, kRefBlock><<<grid, 64, 0, ctx()->stream>>>(L, ldl, B, ldb, ncols);
+    MGB_LAUNCHED("trsm_lu");
+    return 0;
+  }
+  if (tb == kOuterBlockLp && sizeof(T) == 4) {
+    KtScope kt("trsm_lu", (double)tb * tb * ncols, (double)sizeof(T) * 2.0 * tb * ncols);
+    trsm_unit_reg_kernel<T, kOuterBlockLp><<<grid, 64, 0, ctx()->stream>>>(L, ldl, B, ldb, ncols);
+    MGB_LAUNCHED("trsm_lu");
+    return 0;
+  }
+  return trsm_left_t<T>(true, false, true, tb, ncols, L, ldl, B, ldb, nullptr);
 }
 
 __global__ void iota_kernel(int32_t *p, int64_t n) {
@@ -232,10 +370,11 @@ __global__ void iota_kernel(int32_t *p, int64_t n) {
 }
 
 // X[i, c] = B[perm[i], c]  (pb[i] = b[p[i]] of mat_solve, mat.h:4825-4827)
+template <typename T>
 __global__ void gather_rows_kernel(int64_t n, int64_t nrhs,
                                    const int32_t *__restrict__ perm,
-                                   const elem_t *__restrict__ B, int64_t ldb,
-                                   elem_t *__restrict__ X, int64_t ldx) {
+                                   const T *__restrict__ B, int64_t ldb,
+                                   T *__restrict__ X, int64_t ldx) {
   const int64_t tot = n * nrhs;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (int64_t)gridDim.x * blockDim.x) {
@@ -244,41 +383,29 @@ __global__ void gather_rows_kernel(int64_t n, int64_t nrhs,
   }
 }
 
-static int laswp_perm(elem_t *A, int64_t lda, int64_t c0, int64_t c1,
-                      int64_t c2, int64_t c3, const int32_t *ipiv, int64_t k1,
-                      int64_t k2, int32_t *perm) {
-  const int64_t total = (c1 - c0) + (c3 - c2) + (perm ? 1 : 0);
-  if (total <= 0 || k2 <= k1) return 0;
-  const int threads = 128;
-  int64_t blocks = (total + threads - 1) / threads;
-  KtScope kt("laswp", 0.0, 4.0 * (k2 - k1) * total * sizeof(elem_t));
-  laswp_kernel<<<(unsigned)blocks, threads, 0, ctx()->stream>>>(
-      A, lda, c0, c1, c2, c3, ipiv, k1, k2, perm);
-  MGB_LAUNCHED("laswp");
-  return 0;
-}
-
-int laswp(elem_t *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2,
-          int64_t c3, const int32_t *ipiv, int64_t k1, int64_t k2) {
-  return laswp_perm(A, lda, c0, c1, c2, c3, ipiv, k1, k2, nullptr);
-}
-
 struct PanelPlan {
   int cs, w, rpc;
   size_t smem;
 };
 
-static bool g_panel_ready = false;
-static int g_panel_maxcs = 8;
+template <typename T>
+struct PanelState {
+  static bool ready;
+  static int maxcs;
+};
+template <typename T>
+bool PanelState<T>::ready = false;
+template <typename T>
+int PanelState<T>::maxcs = 8;
 
+template <typename T>
 static int panel_setup() {
-  if (g_panel_ready) return 0;
-  MGB_CUDA(cudaFuncSetAttribute(lu_panel_kernel,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (PanelState<T>::ready) return 0;
+  auto kern = lu_panel_kernel<T>;
+  MGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kSmemMax));
   // 16-CTA clusters are non-portable: use them only if the device accepts one.
-  if (cudaFuncSetAttribute(lu_panel_kernel,
-                           cudaFuncAttributeNonPortableClusterSizeAllowed,
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed,
                            1) == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(16);
@@ -292,32 +419,32 @@ static int panel_setup() {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, lu_panel_kernel, &cfg) ==
-            cudaSuccess &&
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess &&
         nclusters > 0)
-      g_panel_maxcs = 16;
+      PanelState<T>::maxcs = 16;
   }
   cudaGetLastError();
-  g_panel_ready = true;
+  PanelState<T>::ready = true;
   return 0;
 }
 
 // Smallest cluster that holds the panel with at most 2 rows per thread;
 // the full reference width (24) unless even the largest cluster cannot hold
 // it, then the widest divisor of 24 that fits.
+template <typename T>
 static int plan_panel(int64_t m, int wmax, PanelPlan *pl) {
   static const int widths[] = {24, 12, 8, 6, 4, 3, 2, 1};
+  const int maxcs = PanelState<T>::maxcs;
   for (int wi = 0; wi < 8; wi++) {
     int w = widths[wi];
     if (w > wmax) continue;
-    for (int cs = 1; cs <= g_panel_maxcs; cs *= 2) {
+    for (int cs = 1; cs <= maxcs; cs *= 2) {
       int64_t rpc = (m + cs - 1) / cs;
-      size_t sm = panel_smem(cs, w, (int)rpc);
+      size_t sm = panel_smem<T>(cs, w, (int)rpc);
       if (sm > (size_t)kSmemMax) continue;
-      if (rpc > 2 * kPanelThreads && cs < g_panel_maxcs) {
-        // prefer more CTAs while that still fits
+      if (rpc > 2 * kPanelThreads && cs < maxcs) {
         int64_t rpc2 = (m + 2 * cs - 1) / (2 * cs);
-        if (panel_smem(2 * cs, w, (int)rpc2) <= (size_t)kSmemMax) continue;
+        if (panel_smem<T>(2 * cs, w, (int)rpc2) <= (size_t)kSmemMax) continue;
       }
       pl->cs = cs;
       pl->w = w;
@@ -330,8 +457,13 @@ static int plan_panel(int64_t m, int wmax, PanelPlan *pl) {
                    (long long)m);
 }
 
-static int launch_panel(elem_t *A, int64_t lda, int64_t n, int64_t k0,
-                        const PanelPlan &pl, int32_t *ipiv) {
+// Factor the panel rows [k0,n) x cols [k0, k0+w'), w' <= w chosen to fit.
+template <typename T>
+int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
+               T eps, int *w_used) {
+  MGB_TRY(panel_setup<T>());
+  PanelPlan pl;
+  MGB_TRY(plan_panel<T>(n - k0, w, &pl));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(pl.cs);
   cfg.blockDim = dim3(kPanelThreads);
@@ -345,71 +477,164 @@ static int launch_panel(elem_t *A, int64_t lda, int64_t n, int64_t k0,
   cfg.attrs = at;
   cfg.numAttrs = 1;
   const double m = (double)(n - k0);
-  KtScope kt("lu_panel", m * pl.w * pl.w, 2.0 * m * pl.w * sizeof(elem_t));
-  MGB_CUDA(cudaLaunchKernelEx(&cfg, lu_panel_kernel, A, lda, n, k0, pl.w,
-                              pl.rpc, ipiv));
+  KtScope kt("lu_panel", m * pl.w * pl.w, 2.0 * m * pl.w * sizeof(T));
+  MGB_CUDA(cudaLaunchKernelEx(&cfg, lu_panel_kernel<T>, A, lda, n, k0, pl.w,
+                              pl.rpc, ipiv, eps));
   MGB_LAUNCHED("lu_panel");
+  *w_used = pl.w;
   return 0;
 }
 
-int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm) {
+// Factor the outer block columns [kb, ke) (rows [kb, n)) with 24-column
+// panels: swaps, U12 solve and update restricted to the block's columns.
+template <typename T>
+static int factor_block(int64_t n, T *A, int64_t lda, int64_t kb, int64_t ke,
+                        int32_t *ipiv, T eps) {
+  for (int64_t jb = kb; jb < ke;) {
+    int wmax = (int)((ke - jb) < kRefBlock ? (ke - jb) : kRefBlock);
+    int w = 0;
+    MGB_TRY(lu_panel_t<T>(A, lda, n, jb, wmax, ipiv, eps, &w));
+    const int64_t je = jb + w;
+    MGB_TRY(laswp_t<T>(A, lda, kb, jb, je, ke, ipiv, jb, je, nullptr));
+    if (je < ke) {
+      MGB_TRY(trsm_unit_lower<T>(w, ke - je, A + jb + jb * lda, lda,
+                                 A + jb + je * lda, lda));
+      MGB_TRY(gemm_skip_t<T>(false, false, n - je, ke - je, w, T(-1),
+                             A + je + jb * lda, lda, A + jb + je * lda, lda,
+                             T(1), A + je + je * lda, lda, 0, nullptr));
+    }
+    jb = je;
+  }
+  return 0;
+}
+
+// Library stream + a high-priority stream for the panel chain, and a ring
+// of events ordering them.
+struct LookAhead {
+  cudaStream_t hi = nullptr;
+  cudaEvent_t ev[4] = {};
+  bool ready = false;
+};
+static LookAhead g_la;
+
+static int lookahead_setup() {
+  if (g_la.ready) return 0;
+  int lo = 0, hi = 0;
+  MGB_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  MGB_CUDA(cudaStreamCreateWithPriority(&g_la.hi, cudaStreamNonBlocking, hi));
+  for (auto &e : g_la.ev)
+    MGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  g_la.ready = true;
+  return 0;
+}
+
+// Temporarily route library launches to another stream.
+struct StreamSwap {
+  cudaStream_t saved;
+  explicit StreamSwap(cudaStream_t s) : saved(ctx()->stream) { ctx()->stream = s; }
+  ~StreamSwap() { ctx()->stream = saved; }
+};
+
+// Trailing update C[ke:n, c0:c1] -= L21 * U12[:, c0:c1] for outer block
+// [kb, ke): SIMT GEMM in T (lp < 0) or the tensor-core path (lp >= 0, float
+// only: L21/U12 packed to 16 bits once per block, see mixed.cu).
+template <typename T>
+static int trailing_update(int64_t n, T *A, int64_t lda, int64_t kb,
+                           int64_t ke, int64_t c0, int64_t c1, int lp,
+                           bool pack) {
+  if (c1 <= c0 || ke >= n) return 0;
+  if (lp < 0)
+    return gemm_skip_t<T>(false, false, n - ke, c1 - c0, ke - kb, T(-1),
+                          A + ke + kb * lda, lda, A + kb + c0 * lda, lda, T(1),
+                          A + ke + c0 * lda, lda, 0, nullptr);
+  if (sizeof(T) != 4) return set_error(MATGB_ERR_ARG, "tensor-core LU is float");
+  return lp_trailing_update(n, (float *)A, lda, kb, ke, c0, c1, lp, pack);
+}
+
+template <typename T>
+int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
+            int lp) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (n <= 0) return 0;
   if (n > INT_MAX / 2) return set_error(MATGB_ERR_ARG, "n too large");
-  MGB_TRY(panel_setup());
+  MGB_TRY(lookahead_setup());
+  cudaStream_t main = cx->stream, hi = g_la.hi;
   if (perm) {
     iota_kernel<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096),
-                  256, 0, cx->stream>>>(perm, n);
+                  256, 0, main>>>(perm, n);
     MGB_LAUNCHED("iota");
   }
-  for (int64_t kb = 0; kb < n; kb += kOuterBlock) {
-    const int64_t nb = (n - kb) < kOuterBlock ? (n - kb) : kOuterBlock;
+  // main -> hi: everything queued so far (input copies, perm init)
+  MGB_CUDA(cudaEventRecord(g_la.ev[0], main));
+  MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[0], 0));
+  const int64_t NB = lp >= 0 ? kOuterBlockLp : kOuterBlock;
+  for (int64_t kb = 0; kb < n; kb += NB) {
+    const int64_t nb = (n - kb) < NB ? (n - kb) : NB;
     const int64_t ke = kb + nb;
-    for (int64_t jb = kb; jb < ke;) {
-      PanelPlan pl;
-      int wmax = (int)((ke - jb) < kRefBlock ? (ke - jb) : kRefBlock);
-      MGB_TRY(plan_panel(n - jb, wmax, &pl));
-      if (pl.w > wmax) pl.w = wmax;
-      const int64_t je = jb + pl.w;
-      MGB_TRY(launch_panel(A, lda, n, jb, pl, ipiv));
-      MGB_TRY(laswp_perm(A, lda, kb, jb, je, ke, ipiv, jb, je, nullptr));
-      if (je < ke) {
-        MGB_TRY(trsm_left(true, false, true, pl.w, ke - je, A + jb + jb * lda,
-                          lda, A + jb + je * lda, lda, nullptr));
-        MGB_TRY(gemm(false, false, n - je, ke - je, pl.w, elem_t(-1),
-                     A + je + jb * lda, lda, A + jb + je * lda, lda, elem_t(1),
-                     A + je + je * lda, lda, 0));
-      }
-      jb = je;
+    {
+      StreamSwap sw(hi);
+      MGB_TRY(factor_block<T>(n, A, lda, kb, ke, ipiv, eps));
     }
-    MGB_TRY(laswp_perm(A, lda, 0, kb, ke, n, ipiv, kb, ke, perm));
+    MGB_CUDA(cudaEventRecord(g_la.ev[1], hi));
+    MGB_CUDA(cudaStreamWaitEvent(main, g_la.ev[1], 0));
+    MGB_TRY(laswp_t<T>(A, lda, 0, kb, ke, n, ipiv, kb, ke, perm));
     if (ke < n) {
-      MGB_TRY(trsm_left(true, false, true, nb, n - ke, A + kb + kb * lda, lda,
-                        A + kb + ke * lda, lda, nullptr));
-      MGB_TRY(gemm(false, false, n - ke, n - ke, nb, elem_t(-1),
-                   A + ke + kb * lda, lda, A + kb + ke * lda, lda, elem_t(1),
-                   A + ke + ke * lda, lda, 0));
+      MGB_TRY(trsm_unit_lower<T>((int)nb, n - ke, A + kb + kb * lda, lda,
+                                 A + kb + ke * lda, lda));
+      // look-ahead: the next block's columns first, then signal the panel
+      const int64_t nn = (n - ke) < NB ? (n - ke) : NB;
+      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true));
+      MGB_CUDA(cudaEventRecord(g_la.ev[2], main));
+      MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[2], 0));
+      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, n, lp, false));
     }
   }
   return 0;
 }
 
-int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,
-          const int32_t *perm, const elem_t *B, int64_t ldb, elem_t *X,
-          int64_t ldx) {
+template <typename T>
+int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
+            const int32_t *perm, const T *B, int64_t ldb, T *X, int64_t ldx) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (n <= 0 || nrhs <= 0) return 0;
   int64_t tot = n * nrhs;
   int64_t blocks = (tot + 255) / 256;
   if (blocks > (int64_t)cx->sms * 16) blocks = (int64_t)cx->sms * 16;
-  gather_rows_kernel<<<(unsigned)blocks, 256, 0, cx->stream>>>(n, nrhs, perm, B,
-                                                               ldb, X, ldx);
+  gather_rows_kernel<T><<<(unsigned)blocks, 256, 0, cx->stream>>>(n, nrhs, perm,
+                                                                  B, ldb, X, ldx);
   MGB_LAUNCHED("gather_rows");
-  MGB_TRY(trsm_left(true, false, true, n, nrhs, LU, lda, X, ldx, nullptr));
-  MGB_TRY(trsm_left(false, false, false, n, nrhs, LU, lda, X, ldx, nullptr));
+  MGB_TRY(trsm_left_t<T>(true, false, true, n, nrhs, LU, lda, X, ldx, nullptr));
+  MGB_TRY(trsm_left_t<T>(false, false, false, n, nrhs, LU, lda, X, ldx, nullptr));
   return 0;
+}
+
+#define MGB_LU_INST(T)                                                         \
+  template int laswp_t<T>(T *, int64_t, int64_t, int64_t, int64_t, int64_t,    \
+                          const int32_t *, int64_t, int64_t, int32_t *);       \
+  template int lu_panel_t<T>(T *, int64_t, int64_t, int64_t, int, int32_t *,  \
+                             T, int *);                                        \
+  template int getrf_t<T>(int64_t, T *, int64_t, int32_t *, int32_t *, T, int); \
+  template int getrs_t<T>(int64_t, int64_t, const T *, int64_t,               \
+                          const int32_t *, const T *, int64_t, T *, int64_t);
+MGB_LU_INST(float)
+MGB_LU_INST(double)
+#undef MGB_LU_INST
+
+int laswp(elem_t *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2,
+          int64_t c3, const int32_t *ipiv, int64_t k1, int64_t k2) {
+  return laswp_t<elem_t>(A, lda, c0, c1, c2, c3, ipiv, k1, k2, nullptr);
+}
+
+int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm) {
+  return getrf_t<elem_t>(n, A, lda, ipiv, perm, kPivotEps, -1);
+}
+
+int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,
+          const int32_t *perm, const elem_t *B, int64_t ldb, elem_t *X,
+          int64_t ldx) {
+  return getrs_t<elem_t>(n, nrhs, LU, lda, perm, B, ldb, X, ldx);
 }
 
 }  // namespace mgb

@@ -1,0 +1,248 @@
+// Tensor-core rank-K update for the mixed-precision factorisations:
+//     C (fp32, column-major) = beta*C + alpha * A * B^T
+// with A (M x K) and B (N x K) in BF16 or FP16, both K-contiguous.
+//
+// This is the low-precision form of the LU trailing update A22 -= L21*U12
+// (mat__gemm_strided_ call at mat.h:4277-4283) and of the Cholesky SYRK
+// update (mat.h:6021-6023): the bulk of the FLOPs run on the 5th-generation
+// tensor cores with FP32 accumulation in TMEM, the trailing matrix stays FP32.
+//
+// One CTA computes one 128 x 256 tile (UMMA M=128, N=256, K=16, cta_group::1):
+//   warp 8  : TMA producer -- K/64 loads of a 128x64 A box and a 256x64 B box
+//             (128-byte swizzle), one mbarrier per 64-wide K block;
+//   warp 9  : TMEM allocator and single-thread MMA issuer (4 MMAs per K block),
+//             then tcgen05.commit to the "accumulator ready" mbarrier;
+//   warps 0-7: epilogue -- tcgen05.ld 32 columns at a time from TMEM (warp w
+//             reads lane quarter w%4, column half w/4), then a coalesced
+//             read-modify-write of C (consecutive lanes = consecutive rows).
+// K <= 128 keeps the whole K extent resident (96 KB of smem), so two CTAs fit
+// per SM and one CTA's epilogue overlaps the other's loads and MMAs.
+// Every wait is bounded; on a timeout the CTA records an error flag, stops
+// issuing work, still frees its TMEM and returns.
+#include <cudaTypedefs.h>
+
+#include "internal.cuh"
+#include "tc_ptx.cuh"
+
+namespace mgb {
+
+constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 64;
+constexpr int kTcMaxK = 128;
+constexpr int kTcKB = kTcMaxK / kTcBK;
+constexpr int kTcThreads = 320;
+constexpr uint32_t kTcWaitLimit = 1u << 24;  // ~1.5 s of polling
+
+struct TcSmem {
+  // 1024-byte aligned swizzle atoms
+  uint16_t a[kTcKB][kTcBM * kTcBK];
+  uint16_t b[kTcKB][kTcBN * kTcBK];
+  uint64_t full[kTcKB];
+  uint64_t done;
+  uint32_t tmem_base;
+  int timeout;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                   const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+                   float alpha, const float *__restrict__ alpha_scale,
+                   float beta, float *__restrict__ C, int64_t ldc,
+                   uint32_t idesc, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // align the carve-out to 1024 B (the swizzle atom)
+  TcSmem &s = *reinterpret_cast<TcSmem *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
+  const int nkb = K / kTcBK;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kTcKB; i++) tc::mbar_init(&s.full[i], 1);
+    tc::mbar_init(&s.done, 1);
+    s.timeout = 0;
+    tc::fence_barrier_init();
+  }
+  if (warp == 9) tc::tmem_alloc(&s.tmem_base, kTcBN);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = s.tmem_base;
+
+  if (warp == 8 && lane == 0) {
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+    for (int kb = 0; kb < nkb; kb++) {
+      tc::mbar_arrive_expect_tx(&s.full[kb],
+                                (kTcBM + kTcBN) * kTcBK * 2);
+      tc::tma_load_2d(s.a[kb], &tmA, kb * kTcBK, m0, &s.full[kb]);
+      tc::tma_load_2d(s.b[kb], &tmB, kb * kTcBK, n0, &s.full[kb]);
+    }
+  } else if (warp == 9 && lane == 0) {
+    bool ok = true;
+    for (int kb = 0; kb < nkb && ok; kb++) {
+      if (!tc::mbar_wait(&s.full[kb], 0, kTcWaitLimit)) {
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t a0 = tc::smem_u32(s.a[kb]), b0 = tc::smem_u32(s.b[kb]);
+#pragma unroll
+      for (int kk = 0; kk < kTcBK / 16; kk++) {
+        // advance 16 elements (32 bytes) along K inside the 128-byte atom
+        const uint64_t ad = tc::desc_k_sw128(a0 + kk * 32);
+        const uint64_t bd = tc::desc_k_sw128(b0 + kk * 32);
+        tc::mma_f16(tmem, ad, bd, idesc, (kb | kk) ? 1u : 0u);
+      }
+    }
+    if (ok) {
+      tc::mma_commit(&s.done);
+    } else {
+      s.timeout = 1;
+      atomicExch(err, 1);
+      // wait (bounded) for the TMA copies still in flight before leaving
+      for (int kb = 0; kb < nkb; kb++) tc::mbar_wait(&s.full[kb], 0, kTcWaitLimit);
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                       tc::smem_u32(&s.done))
+                   : "memory");
+    }
+  } else if (warp < 8) {
+    const bool ready = tc::mbar_wait(&s.done, 0, kTcWaitLimit);
+    tc::tc_fence_after();
+    if (ready && !s.timeout) {
+      const int q = warp & 3, half = warp >> 2;
+      const int row = m0 + q * 32 + lane;
+      const float al = alpha_scale ? alpha * (*alpha_scale) : alpha;
+#pragma unroll 1
+      for (int cc = 0; cc < kTcBN / 2; cc += 32) {
+        const int col0 = half * (kTcBN / 2) + cc;
+        float v[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col0, v);
+        if (row < M) {
+          float *cp = C + (int64_t)(n0 + col0) * ldc + row;
+          const int ncol = min(32, N - (n0 + col0));
+          if (beta != 0.f) {
+            float old[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+              if (j < ncol) old[j] = cp[(int64_t)j * ldc];
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+              if (j < ncol) cp[(int64_t)j * ldc] = fmaf(al, v[j], beta * old[j]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+              if (j < ncol) cp[(int64_t)j * ldc] = al * v[j];
+          }
+        }
+      }
+    } else if (!ready) {
+      atomicExch(err, 2);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 9) {
+    __syncwarp();
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, kTcBN);
+  }
+}
+
+// ---- host side ----------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static int *g_tc_err = nullptr;
+static bool g_tc_ready = false;
+
+static int tc_setup() {
+  if (g_tc_ready) return 0;
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  MGB_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn,
+                                            12000, cudaEnableDefault, &q));
+  if (!fn || q != cudaDriverEntryPointSuccess)
+    return set_error(MATGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  MGB_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
+  MGB_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(TcSmem) + 1024));
+  g_tc_ready = true;
+  return 0;
+}
+
+static int make_map(CUtensorMap *m, const void *ptr, int bf16, int64_t rows,
+                    int64_t k, int64_t ld, int box_rows) {
+  cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(
+      m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+      2, const_cast<void *>(ptr), dims, strides, box, estr,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return set_error(MATGB_ERR_ARG, "tensor map encode failed (%d)", (int)r);
+  return 0;
+}
+
+// C = beta*C + alpha*(*alpha_scale if given)*A*B^T.  A: M x K, B: N x K,
+// K-contiguous 16-bit (bf16 != 0: BF16, else FP16); K a multiple of 64 and
+// <= 128; lda, ldb multiples of 8 elements; 16-byte aligned bases.
+int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
+            int64_t lda, const void *B, int64_t ldb, float alpha,
+            const float *alpha_scale, float beta, float *C, int64_t ldc) {
+  Ctx *cx = ctx();
+  if (!cx) return MATGB_ERR_NO_DEVICE;
+  if (M <= 0 || N <= 0) return 0;
+  if (K <= 0 || K % kTcBK || K > kTcMaxK || lda % 8 || ldb % 8 ||
+      ((uintptr_t)A & 15) || ((uintptr_t)B & 15) || M > INT32_MAX ||
+      N > INT32_MAX)
+    return set_error(MATGB_ERR_ARG, "tc_gemm: unsupported shape/alignment");
+  MGB_TRY(tc_setup());
+  CUtensorMap ma, mb;
+  MGB_TRY(make_map(&ma, A, bf16, M, K, lda, kTcBM));
+  MGB_TRY(make_map(&mb, B, bf16, N, K, ldb, kTcBN));
+  dim3 grid((unsigned)((M + kTcBM - 1) / kTcBM), (unsigned)((N + kTcBN - 1) / kTcBN));
+  const uint32_t idesc = tc::idesc_f16(bf16 ? 1 : 0, kTcBM, kTcBN);
+  KtScope kt("tc_gemm", 2.0 * M * N * K,
+             4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N + 2.0 * (M + N) * K);
+  tc_gemm_kernel<<<grid, kTcThreads, sizeof(TcSmem) + 1024, cx->stream>>>(
+      ma, mb, (int)M, (int)N, (int)K, alpha, alpha_scale, beta, C, ldc, idesc,
+      g_tc_err);
+  MGB_LAUNCHED("tc_gemm");
+  return 0;
+}
+
+int tc_error_flag(int clear) {
+  if (!g_tc_err) return 0;
+  int h = 0;
+  MGB_CUDA(cudaMemcpy(&h, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (clear && h) MGB_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
+  return h;
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+extern "C" {
+
+int matgb_tc_gemm_dev(int bf16, size_t M, size_t N, size_t K, const void *A,
+                      size_t lda, const void *B, size_t ldb, float alpha,
+                      float beta, float *C, size_t ldc) {
+  if (ldc < M) return set_error(MATGB_ERR_ARG, "tc_gemm: ldc < M");
+  return tc_gemm(bf16, (int64_t)M, (int64_t)N, (int64_t)K, A, (int64_t)lda, B,
+                 (int64_t)ldb, alpha, nullptr, beta, C, (int64_t)ldc);
+}
+
+int matgb_tc_status(void) {
+  int f = tc_error_flag(1);
+  if (f < 0) return f;
+  return f ? set_error(MATGB_ERR_TIMEOUT,
+                       "tensor-core kernel gave up waiting (flag %d)", f)
+           : 0;
+}
+
+}  // extern "C"

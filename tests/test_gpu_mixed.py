@@ -1,0 +1,187 @@
+"""GPU: the tensor-core rank-K update (tcgen05/TMEM/TMA) and the
+mixed-precision LU + iterative refinement, through the C ABI.
+
+Tolerances:
+  tc_gemm: FP32 accumulation of exactly representable 16-bit products;
+           max |err| <= 2e-6 * K * max|ref| against an FP64 product of the
+           same rounded inputs.
+  LU factors with 16-bit trailing updates: |PA - LU|_max / |A|_max <= 5e-2
+           (BF16, unit roundoff 2^-8) / 1e-2 (FP16, 2^-11) / 1e-5 (FP32).
+  Refined solutions: normwise backward error <= n * 2^-53 (libmatgb_f64) or
+           n * 2^-24 (libmatgb_f32), the refinement target.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from libmat_gb300 import rng
+
+pytestmark = pytest.mark.gpu
+
+
+def to_bf16_bits(x):
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) >> 16
+    return b.astype(np.uint16)
+
+
+def bf16_bits_to_f64(b):
+    return (b.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def lp_pack(x, bf16):
+    """Row-major (K contiguous) 16-bit operand and its exact float64 value."""
+    x = np.ascontiguousarray(x, np.float32)
+    if bf16:
+        bits = to_bf16_bits(x)
+        return bits, bf16_bits_to_f64(bits)
+    h = x.astype(np.float16)
+    return h.view(np.uint16), h.astype(np.float64)
+
+
+@pytest.mark.parametrize("bf16", [1, 0])
+@pytest.mark.parametrize("mnk", [(128, 256, 64), (200, 300, 128), (1000, 700, 128),
+                                 (1, 1, 64), (129, 257, 64), (4096, 512, 128)])
+def test_tc_gemm_vs_fp64(gpu, bf16, mnk):
+    L = gpu["f32"]
+    M, N, K = mnk
+    A = rng.normal(101, (M, K), np.float32)
+    B = rng.normal(102, (N, K), np.float32)
+    C0 = rng.normal(103, (M, N), np.float32)
+    Ab, Ad = lp_pack(A, bf16)
+    Bb, Bd = lp_pack(B, bf16)
+    ref = C0.astype(np.float64) - 0.75 * (Ad @ Bd.T)
+    dA, dB = L.dalloc(Ab.nbytes), L.dalloc(Bb.nbytes)
+    dC = L.dalloc(C0.nbytes)
+    try:
+        L.h2d(dA, Ab)
+        L.h2d(dB, Bb)
+        L.h2d(dC, C0)
+        rc = L.c.matgb_tc_gemm_dev(bf16, M, N, K, dA, K, dB, K, -0.75, 1.0,
+                                   dC, M)
+        L.check(rc, "tc_gemm")
+        out = np.empty((M, N), np.float32, order="F")
+        L.d2h(out, dC)
+        L.check(L.c.matgb_tc_status(), "tc_status")
+    finally:
+        for p in (dA, dB, dC):
+            L.dfree(p)
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err <= 2e-6 * K, err
+
+
+def factor_lp(L, A, lp):
+    n = A.shape[0]
+    dA = L.dalloc(A.nbytes)
+    dp = L.dalloc(8 * n)
+    try:
+        L.h2d(dA, np.asfortranarray(A, np.float32))
+        L.check(L.c.matgb_getrf_lp_dev(n, dA, n, dp, dp + 4 * n, lp), "getrf_lp")
+        LU = np.empty((n, n), np.float32, order="F")
+        L.d2h(LU, dA)
+        pv = np.empty(2 * n, np.int32)
+        L.d2h(pv, dp)
+        L.check(L.c.matgb_tc_status(), "tc_status")
+    finally:
+        L.dfree(dA)
+        L.dfree(dp)
+    return LU, pv[n:]
+
+
+def round_lp(x, lp):
+    if lp == 1:
+        return bf16_bits_to_f64(to_bf16_bits(x))
+    if lp == 0:
+        return x.astype(np.float16).astype(np.float64)
+    return x.astype(np.float64)
+
+
+def emulate_lp_lu(A, lp, nb=128):
+    """numpy model of the mixed LU: FP32 panels and FP32 trailing matrix, the
+    trailing products of each nb-column block formed from 16-bit-rounded
+    L21/U12 (FP16 with the per-block power-of-two scale of U12).  Returns the
+    normwise factorisation error |PA - LU|_max / |A|_max it reaches."""
+    M = np.array(A, np.float32)
+    n = M.shape[0]
+    perm = np.arange(n)
+    for kb in range(0, n, nb):
+        ke = min(kb + nb, n)
+        for k in range(kb, ke):
+            p = k + int(np.argmax(np.abs(M[k:, k])))
+            if p != k:
+                M[[k, p]] = M[[p, k]]
+                perm[[k, p]] = perm[[p, k]]
+            if M[k, k] != 0:
+                M[k + 1:, k] *= np.float32(1) / M[k, k]
+            M[k + 1:, k + 1:ke] -= np.outer(M[k + 1:, k], M[k, k + 1:ke])
+        if ke < n:
+            L11 = np.tril(M[kb:ke, kb:ke].astype(np.float64), -1) + np.eye(ke - kb)
+            M[kb:ke, ke:] = np.linalg.solve(L11, M[kb:ke, ke:].astype(np.float64))
+            U12 = M[kb:ke, ke:].astype(np.float64)
+            s = 1.0
+            if lp == 0 and np.abs(U12).max() > 0:
+                s = 2.0 ** (14 - np.frexp(np.abs(U12).max())[1])
+            upd = round_lp(M[ke:, kb:ke], lp) @ round_lp((U12 * s).astype(np.float32), lp)
+            M[ke:, ke:] = (M[ke:, ke:].astype(np.float64) - upd / s).astype(np.float32)
+    Lm = np.tril(M.astype(np.float64), -1) + np.eye(n)
+    Um = np.triu(M.astype(np.float64))
+    return np.abs(A[perm].astype(np.float64) - Lm @ Um).max() / np.abs(A).max()
+
+
+@pytest.mark.parametrize("lp", [1, 0, -1])
+@pytest.mark.parametrize("n", [300, 1000, 1537])
+def test_lp_lu_reconstructs(gpu, lp, n):
+    """|PA - LU| of the GPU factorisation stays within 3x of what the numpy
+    model of the same precision scheme reaches (plus an FP32 floor)."""
+    L = gpu["f32"]
+    A = rng.uniform(200 + n, (n, n), -1, 1, np.float32)
+    LU, perm = factor_lp(L, A, lp)
+    assert np.array_equal(np.sort(perm), np.arange(n))
+    Lm = np.tril(LU.astype(np.float64), -1) + np.eye(n)
+    Um = np.triu(LU.astype(np.float64))
+    err = np.abs(A[perm].astype(np.float64) - Lm @ Um).max() / np.abs(A).max()
+    model = emulate_lp_lu(A, lp)
+    assert err <= 3 * model + 1e-5, (err, model)
+    assert np.abs(Lm).max() <= 1.0 + 1e-6  # partial pivoting bound
+
+
+def conditioned(n, kappa, seed):
+    rs = np.random.default_rng(seed)
+    U, _ = np.linalg.qr(rs.standard_normal((n, n)))
+    V, _ = np.linalg.qr(rs.standard_normal((n, n)))
+    s = np.geomspace(1.0, 1.0 / kappa, n)
+    return np.asfortranarray((U * s) @ V.T)
+
+
+@pytest.mark.parametrize("lp", [1, 0])
+@pytest.mark.parametrize("n,kappa", [(512, 1e2), (1024, 1e2), (1000, 1e3)])
+def test_ir_f64_reaches_fp64_backward_error(gpu, lp, n, kappa):
+    L = gpu["f64"]
+    A = conditioned(n, kappa, 7 + n)
+    b = np.random.default_rng(n).standard_normal(n)
+    x, rep = L.mat_solve_ir(A, b, lp_format=lp)
+    assert rep["converged"] == 1, rep
+    eta = np.abs(b - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
+                                     + np.abs(b).max())
+    assert eta <= n * 2.0 ** -53, (eta, rep)
+    xr = np.linalg.solve(A, b)
+    assert np.abs(x - xr).max() / np.abs(xr).max() <= kappa * n * 2.0 ** -50
+
+
+def test_ir_f32_reaches_fp32_backward_error(gpu):
+    L = gpu["f32"]
+    n = 800
+    A = rng.uniform(55, (n, n), -1, 1, np.float32) + n * np.eye(n, dtype=np.float32) / 8
+    b = rng.normal(56, (n,), np.float32)
+    x, rep = L.mat_solve_ir(A, b, lp_format=1)
+    assert rep["converged"] == 1 and rep["backward_error"] <= n * 2.0 ** -24, rep
+
+
+def test_ir_reports_nonconvergence_for_singular(gpu):
+    L = gpu["f64"]
+    n = 256
+    A = np.ones((n, n))
+    b = np.arange(n, dtype=np.float64)
+    x, rep = L.mat_solve_ir(A, b, lp_format=1, max_iter=5)
+    assert rep["converged"] == 0 and rep["iterations"] <= 5
