@@ -179,6 +179,24 @@ int matgb_tc_gemm_dev(int bf16, size_t M, size_t N, size_t K, const void *A,
  * since the last call (clears the flag; synchronises). */
 int matgb_tc_status(void);
 
+/* y = alpha*A*x + beta*y like matgb_gemv_dev, for callers that must not
+ * allocate device memory -- e.g. code that runs inside another runtime's
+ * memory pool (where a raw cudaMalloc can fail or fragment that pool) or on a
+ * latency-critical stream (where cudaMalloc/cudaFree's implicit device
+ * synchronisation is not acceptable).  No counterpart in the reference.
+ * Allocates nothing: its scratch is a static device array of 2^20 elements
+ * (4 MiB in libmatgb_f32, 8 MiB in libmatgb_f64) that every GPU loading the
+ * library holds until exit; m above 2^20 is rejected with MATGB_ERR_ARG.
+ * Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and
+ * does not touch the library stream.  The first call on a device looks up the
+ * array's device address, so make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller. */
+int matgb_gemv_noalloc_dev(size_t m, size_t n, mat_elem_t alpha,
+                           const mat_elem_t *A, size_t lda,
+                           const mat_elem_t *x, mat_elem_t beta,
+                           mat_elem_t *y, void *stream);
+
 /* ---- Host (Mat) superset ------------------------------------------------- */
 /* AX = B for every column of B (mat_solve reads only column 0, mat.h:4825). */
 void matgb_solve_multi(Mat *X, const Mat *A, const Mat *B);

@@ -149,6 +149,8 @@ class Lib:
                                        C.POINTER(MatIRReport)]),
             "mat_solve_ir": (_I, [MP, MP, MP, C.POINTER(MatIROpts),
                                   C.POINTER(MatIRReport)]),
+            "matgb_gemv_noalloc_dev": (_I, [_S, _S, E, _P, _S, _P, E, _P,
+                                            _P]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(c, name)

@@ -317,3 +317,83 @@ int matgb_gemv_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
 }
 
 }  // extern "C"
+
+// ---- GEMV without allocation -------------------------------------------------
+// For callers that must not allocate device memory: the column-split partial
+// sums live in this file-scope device array instead of the library's
+// workspace, and the caller supplies the stream.  Every GPU that loads the
+// library holds the array (kGemvStaticElems elements: 4 MiB in libmatgb_f32,
+// 8 MiB in libmatgb_f64) until the process exits.
+#include <mutex>
+
+namespace mgb {
+
+constexpr size_t kGemvStaticElems = (size_t)1 << 20;
+static __device__ __align__(256) elem_t g_gemv_static_scratch[kGemvStaticElems];
+
+// Device address of the array for the current device, looked up once per
+// device (host code may not use the symbol's host-side name as a pointer).
+static int gemv_static_scratch(elem_t **out, int *sms) {
+  static std::mutex mu;
+  static elem_t *addr[64] = {};
+  static int nsm[64] = {};
+  int dev = -1;
+  MGB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(MATGB_ERR_ARG, "device id %d", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    MGB_CUDA(cudaGetSymbolAddress(&p, g_gemv_static_scratch));
+    MGB_CUDA(cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev));
+    addr[dev] = (elem_t *)p;
+  }
+  *out = addr[dev];
+  *sms = nsm[dev];
+  return 0;
+}
+
+}  // namespace mgb
+
+extern "C" int matgb_gemv_noalloc_dev(size_t m, size_t n, mat_elem_t alpha,
+                                      const mat_elem_t *A, size_t lda,
+                                      const mat_elem_t *x, mat_elem_t beta,
+                                      mat_elem_t *y, void *stream) {
+  using namespace mgb;
+  if (lda < m) return set_error(MATGB_ERR_ARG, "gemv_noalloc: lda < m");
+  if (m > kGemvStaticElems)
+    return set_error(MATGB_ERR_ARG,
+                     "gemv_noalloc: m = %zu exceeds the static scratch of %zu "
+                     "elements",
+                     m, kGemvStaticElems);
+  if (m == 0) return 0;
+  elem_t *P = nullptr;
+  int sms = 0;
+  MGB_TRY(gemv_static_scratch(&P, &sms));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t M = (int64_t)m, N = (int64_t)n;
+  const int64_t rb = (M + kGemvRows - 1) / kGemvRows;
+  const int64_t target = (int64_t)(sms > 0 ? sms : 148) * 8;
+  int64_t chunks = (target + rb - 1) / rb;
+  const int64_t cap = (int64_t)(kGemvStaticElems / m);
+  if (chunks > cap) chunks = cap;
+  if (chunks > N) chunks = N;
+  if (chunks > 1024) chunks = 1024;
+  int64_t cols_per = 0;
+  if (N > 0) {
+    if (chunks < 1) chunks = 1;
+    cols_per = (N + chunks - 1) / chunks;
+    chunks = (N + cols_per - 1) / cols_per;
+    // every (chunk, row) slot read below is written here first, so the
+    // array needs no clearing between calls
+    gemv_partial_kernel<elem_t><<<dim3((unsigned)rb, (unsigned)chunks),
+                                  kGemvRows, 0, st>>>(M, N, cols_per, A,
+                                                      (int64_t)lda, x, P);
+    MGB_LAUNCHED("gemv_partial_noalloc");
+  } else {
+    chunks = 0;  // y = beta*y; nothing is read from the array
+  }
+  gemv_reduce_kernel<elem_t><<<(unsigned)((M + 255) / 256), 256, 0, st>>>(
+      M, (int)chunks, alpha, P, beta, y);
+  MGB_LAUNCHED("gemv_reduce_noalloc");
+  return 0;
+}
