@@ -139,19 +139,23 @@ int matgb_gemv_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
  * update and convergence test run on the GPU in the library's element type
  * (FP64 in libmatgb_f64). */
 typedef struct {
-  int lp_format; /* 1 = BF16 (default), 0 = FP16 (per-block power-of-2 scale) */
-  int max_iter;  /* refinement solves (default 30)                            */
-  double tol;    /* target backward error; <= 0: n * unit roundoff of the
-                    element type (n * 2^-53 in libmatgb_f64)                   */
+  int lp_format;     /* 1 = BF16 (default), 0 = FP16 (per-block power-of-2
+                        scale), -1 = FP32 trailing updates (SIMT)            */
+  int max_iter;      /* refinement solves over all attempts (default 30)     */
+  double tol;        /* target backward error; <= 0: n * unit roundoff of the
+                        element type (n * 2^-53 in libmatgb_f64)             */
+  int fp32_fallback; /* 1 (default): if refinement with the 16-bit factors
+                        stagnates (kappa(A) * u_16 >~ 1), refactor once with
+                        FP32 trailing updates and refine again               */
 } MatIROpts;
 
 typedef struct {
   int iterations;        /* LU solves done (1 = no refinement needed)        */
   int converged;         /* backward_error <= tol                             */
-  int lp_format;
+  int lp_format;         /* format of the factors that produced x           */
   double backward_error; /* |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf)      */
   double residual_inf, x_inf, a_inf, b_inf, tol;
-  double ms_factor;      /* GPU time of the conversion + factorisation        */
+  double ms_factor;      /* GPU time of conversion + factorisation(s)         */
   double ms_refine;      /* GPU time of solves, residuals and updates         */
 } MatIRReport;
 
@@ -163,6 +167,26 @@ int matgb_gesv_ir_dev(size_t n, const mat_elem_t *A, size_t lda,
 /* Host Mat form; returns 0 or a negative status. */
 int mat_solve_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,
                  MatIRReport *rep);
+/* Many right-hand sides (B, X: n x nrhs; the backward error reported is the
+ * largest over the columns). */
+int matgb_gesv_ir_multi_dev(size_t n, size_t nrhs, const mat_elem_t *A,
+                            size_t lda, const mat_elem_t *B, size_t ldb,
+                            mat_elem_t *X, size_t ldx, const MatIROpts *opts,
+                            MatIRReport *rep);
+/* SPD form (generalises mat_solve_spd, mat.h:4839-4871): Cholesky of the lower
+ * triangle with FP32 panels and tensor-core SYRK updates (BF16, or FP16 with a
+ * power-of-two scale), refinement as above.  Returns 0, -1 when the matrix is
+ * not positive definite (even in FP32), or a negative status. */
+int matgb_posv_ir_dev(size_t n, size_t nrhs, const mat_elem_t *A, size_t lda,
+                      const mat_elem_t *B, size_t ldb, mat_elem_t *X,
+                      size_t ldx, const MatIROpts *opts, MatIRReport *rep);
+/* Host Mat form of matgb_posv_ir_dev (b and x n x nrhs). */
+int mat_solve_spd_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,
+                     MatIRReport *rep);
+/* The FP32 Cholesky alone (device, in place, lower) with tensor-core (1 BF16,
+ * 0 FP16) or SIMT (-1) trailing updates; *info as matgb_potrf_dev. */
+int matgb_potrf_lp_dev(size_t n, float *A, size_t lda, int32_t *info,
+                       int lp_format);
 /* The FP32 LU alone (device, in place) with trailing updates on the tensor
  * cores (lp_format 1 BF16, 0 FP16) or, for lp_format -1, the FP32 SIMT GEMM.
  * ipiv/perm as matgb_getrf_dev.  Pivots are never skipped (threshold 0). */
@@ -196,6 +220,21 @@ int matgb_gemv_noalloc_dev(size_t m, size_t n, mat_elem_t alpha,
                            const mat_elem_t *A, size_t lda,
                            const mat_elem_t *x, mat_elem_t beta,
                            mat_elem_t *y, void *stream);
+
+/* ---- Batched small systems ------------------------------------------------- */
+/* Solve `count` independent systems in one pass (mat_solve / mat_solve_spd
+ * applied to each, mat.h:4807-4871).  Device pointers: system s has order
+ * n[s] (1..128; 1..64 in libmatgb_f64), its matrix at A + offA[s]
+ * (column-major, leading dimension n[s]) and its right-hand side / solution at
+ * b + offv[s] / x + offv[s].  kind[s] = 0: partial-pivot LU with the
+ * reference's pivot rule; 1: Cholesky of the lower triangle.  status[s]: 0, or
+ * -1 when Cholesky met a pivot <= 0 (x[s] then untouched, as mat_solve_spd
+ * returns -1).  Asynchronous on the library stream. */
+int matgb_solve_batched_dev(int64_t count, const int32_t *n,
+                            const int64_t *offA, const mat_elem_t *A,
+                            const int64_t *offv, const mat_elem_t *b,
+                            mat_elem_t *x, const uint8_t *kind,
+                            int32_t *status);
 
 /* ---- Host (Mat) superset ------------------------------------------------- */
 /* AX = B for every column of B (mat_solve reads only column 0, mat.h:4825). */

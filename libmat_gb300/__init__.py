@@ -29,7 +29,7 @@ class PermStruct(C.Structure):
 
 class MatIROpts(C.Structure):
     _fields_ = [("lp_format", C.c_int), ("max_iter", C.c_int),
-                ("tol", C.c_double)]
+                ("tol", C.c_double), ("fp32_fallback", C.c_int)]
 
 
 class MatIRReport(C.Structure):
@@ -151,6 +151,17 @@ class Lib:
                                   C.POINTER(MatIRReport)]),
             "matgb_gemv_noalloc_dev": (_I, [_S, _S, E, _P, _S, _P, E, _P,
                                             _P]),
+            "matgb_solve_batched_dev": (_I, [C.c_int64, _P, _P, _P, _P, _P,
+                                             _P, _P, _P]),
+            "matgb_gesv_ir_multi_dev": (_I, [_S, _S, _P, _S, _P, _S, _P, _S,
+                                             C.POINTER(MatIROpts),
+                                             C.POINTER(MatIRReport)]),
+            "matgb_posv_ir_dev": (_I, [_S, _S, _P, _S, _P, _S, _P, _S,
+                                       C.POINTER(MatIROpts),
+                                       C.POINTER(MatIRReport)]),
+            "mat_solve_spd_ir": (_I, [MP, MP, MP, C.POINTER(MatIROpts),
+                                      C.POINTER(MatIRReport)]),
+            "matgb_potrf_lp_dev": (_I, [_S, _P, _S, _P, _I]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(c, name)
@@ -290,16 +301,63 @@ class Lib:
         self.check(0, "solve_multi")
         return (X, int(r)) if spd else X
 
-    def mat_solve_ir(self, A, b, lp_format=1, max_iter=30, tol=0.0):
+    def mat_solve_ir(self, A, b, lp_format=1, max_iter=30, tol=0.0,
+                     fp32_fallback=1):
         """Mixed-precision LU + refinement; returns (x, report dict)."""
         A, b = self.arr(A), self.arr(b)
         x = np.zeros((A.shape[1], 1), self.dtype, order="F")
-        o = MatIROpts(lp_format, max_iter, tol)
+        o = MatIROpts(lp_format, max_iter, tol, fp32_fallback)
         rep = MatIRReport()
         rc = self.c.mat_solve_ir(C.byref(self.mat(x)), C.byref(self.mat(A)),
                                  C.byref(self.mat(b)), C.byref(o), C.byref(rep))
         self.check(rc, "mat_solve_ir")
         return x.reshape(-1), rep.as_dict()
+
+    def solve_batched(self, mats, rhs, kinds):
+        """Solve many small systems in one pass.  mats: list of square arrays,
+        rhs: list of vectors, kinds: 0 (LU) / 1 (Cholesky) per system.
+        Returns (list of solutions, status array)."""
+        count = len(mats)
+        ns = np.array([m.shape[0] for m in mats], np.int32)
+        offA = np.zeros(count, np.int64)
+        offv = np.zeros(count, np.int64)
+        offA[1:] = np.cumsum(ns.astype(np.int64) ** 2)[:-1]
+        offv[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+        Acat = np.concatenate([np.asarray(m, self.dtype).ravel(order="F")
+                               for m in mats])
+        bcat = np.concatenate([np.asarray(v, self.dtype).ravel() for v in rhs])
+        kd = np.asarray(kinds, np.uint8)
+        bufs = [self.dalloc(a.nbytes) for a in (ns, offA, offv, Acat, bcat, bcat, kd)]
+        st = self.dalloc(4 * count)
+        try:
+            for d, a in zip(bufs, (ns, offA, offv, Acat, bcat, bcat, kd)):
+                self.h2d(d, a)
+            rc = self.c.matgb_solve_batched_dev(count, bufs[0], bufs[1], bufs[3],
+                                                bufs[2], bufs[4], bufs[5],
+                                                bufs[6], st)
+            self.check(rc, "solve_batched")
+            x = np.empty_like(bcat)
+            self.d2h(x, bufs[5])
+            status = np.empty(count, np.int32)
+            self.d2h(status, st)
+        finally:
+            for d in bufs + [st]:
+                self.dfree(d)
+        return [x[o:o + k] for o, k in zip(offv, ns)], status
+
+    def mat_solve_spd_ir(self, A, B, lp_format=1, max_iter=30, tol=0.0,
+                         fp32_fallback=1):
+        """Mixed-precision Cholesky + refinement, many RHS; (X, ret, report)."""
+        A, B = self.arr(A), self.arr(B)
+        X = np.zeros((A.shape[1], B.shape[1]), self.dtype, order="F")
+        o = MatIROpts(lp_format, max_iter, tol, fp32_fallback)
+        rep = MatIRReport()
+        rc = self.c.mat_solve_spd_ir(C.byref(self.mat(X)), C.byref(self.mat(A)),
+                                     C.byref(self.mat(B)), C.byref(o),
+                                     C.byref(rep))
+        if rc not in (0, -1):
+            self.check(rc, "mat_solve_spd_ir")
+        return X, int(rc), rep.as_dict()
 
     # --------------------------------------------------- device helpers
     def dalloc(self, nbytes):

@@ -1,0 +1,120 @@
+// Batched solves of many small, uneven systems in one pass: the GB300 form of
+// calling mat_solve (mat.h:4807-4837) / mat_solve_spd (mat.h:4839-4871) in a
+// loop over independent systems.
+//
+// Layout: all matrices packed back to back in one buffer (system s at
+// A + offA[s], column-major, leading dimension n_s), right-hand sides and
+// solutions packed at offv[s].  kind[s] = 0 solves by partial-pivot LU with the
+// reference's pivot rule (first index of max |a|, tiny pivots swapped in but
+// not divided by), kind[s] = 1 by Cholesky (status -1 when a pivot is <= 0,
+// as mat_solve_spd returns -1; x is then left untouched).
+//
+// Kernel: one thread per matrix row, the row (and its right-hand-side entry)
+// held in registers, one system per NB-thread group, NB a compile-time size
+// bucket (16, 32, 64, 96, 128); the double build covers orders up to 64.  With the elimination loop fully unrolled
+// every register index is static.  LU step k: arg-max of column k across the
+// rows (warp shuffles, then shared memory across warps), exchange of rows k
+// and p through shared memory, rank-1 update of the owned row; the right-hand
+// side rides along as an extra column, so forward substitution is fused;
+// back substitution broadcasts one x_j per step.  Cholesky: right-looking with
+// the current column broadcast through shared memory, forward substitution
+// fused, back substitution with L^T read from shared memory.
+//
+// Scheduling: a device-side pre-pass sorts systems into (size bucket, kind)
+// queues; one persistent launch per queue pulls systems with an atomic
+// counter, largest sizes first.
+#include "batched_kernels.cuh"
+
+namespace mgb {
+
+// queue = 2*bucket + kind; counts per queue, then the list is grouped by queue
+__global__ void bucket_count_kernel(int64_t count, const int32_t *__restrict__ n,
+                                    const uint8_t *__restrict__ kind,
+                                    BatchQueues *q) {
+  __shared__ int h[kNumQueues];
+  if (threadIdx.x < kNumQueues) h[threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < count;
+       s += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&h[2 * bucket_of(n[s]) + (kind[s] == 1)], 1);
+  __syncthreads();
+  if (threadIdx.x < kNumQueues) atomicAdd(&q->count[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void bucket_scatter_kernel(int64_t count,
+                                      const int32_t *__restrict__ n,
+                                      const uint8_t *__restrict__ kind,
+                                      BatchQueues *q, int32_t *__restrict__ list) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < count;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const int qi = 2 * bucket_of(n[s]) + (kind[s] == 1);
+    int base = 0;
+    for (int i = 0; i < qi; i++) base += q->count[i];
+    const int pos = atomicAdd(&q->fill[qi], 1);
+    list[base + pos] = (int32_t)s;
+  }
+}
+
+// Orders outside what this build supports get status -2 and are not solved
+// (1..128 in float, 1..64 in double).
+__global__ void check_sizes_kernel(int64_t count, const int32_t *__restrict__ n,
+                                   int nmax, int32_t *__restrict__ status) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < count;
+       s += (int64_t)gridDim.x * blockDim.x)
+    if (n[s] < 1 || n[s] > nmax) status[s] = -2;
+}
+
+int solve_batched(int64_t count, const int32_t *n, const int64_t *offA,
+                  const elem_t *A, const int64_t *offv, const elem_t *b,
+                  elem_t *x, const uint8_t *kind, int32_t *status) {
+  Ctx *cx = ctx();
+  if (!cx) return MATGB_ERR_NO_DEVICE;
+  if (count <= 0) return 0;
+  if (count > INT32_MAX) return set_error(MATGB_ERR_ARG, "batch too large");
+  BatchQueues *q = (BatchQueues *)ws(WS_T2, sizeof(BatchQueues) + 256);
+  int32_t *list = (int32_t *)ws(WS_V1, (size_t)count * sizeof(int32_t));
+  if (!q || !list) return MATGB_ERR_NOMEM;
+  int *bad = (int *)((char *)q + sizeof(BatchQueues));
+  cudaStream_t st = cx->stream;
+  MGB_CUDA(cudaMemsetAsync(q, 0, sizeof(BatchQueues) + sizeof(int), st));
+  const unsigned g = (unsigned)((count + 255) / 256 < 1024 ? (count + 255) / 256 : 1024);
+#ifdef MAT_DOUBLE_PRECISION
+  constexpr int nmax = 64;
+#else
+  constexpr int nmax = 128;
+#endif
+  bucket_count_kernel<<<g, 256, 0, st>>>(count, n, kind, q);
+  MGB_LAUNCHED("bucket_count");
+  bucket_scatter_kernel<<<g, 256, 0, st>>>(count, n, kind, q, list);
+  MGB_LAUNCHED("bucket_scatter");
+  // the largest systems first, so the long ones start early
+  for (int bk = kNumBuckets - 1; bk >= 0; bk--)
+    for (int kd = 0; kd < 2; kd++) {
+      const int qi = 2 * bk + kd;
+      using Fn = int (*)(int, const int32_t *, BatchQueues *, const int32_t *,
+                         const int64_t *, const elem_t *, const int64_t *,
+                         const elem_t *, elem_t *, int32_t *);
+      static const Fn fns[kNumBuckets][2] = {
+          {batched_bucket_16_lu, batched_bucket_16_chol},
+          {batched_bucket_32_lu, batched_bucket_32_chol},
+          {batched_bucket_64_lu, batched_bucket_64_chol},
+          {batched_bucket_96_lu, batched_bucket_96_chol},
+          {batched_bucket_128_lu, batched_bucket_128_chol}};
+      MGB_TRY(fns[bk][kd](qi, list, q, n, offA, A, offv, b, x, status));
+    }
+  check_sizes_kernel<<<g, 256, 0, st>>>(count, n, nmax, status);
+  MGB_LAUNCHED("check_sizes");
+  return 0;
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+extern "C" int matgb_solve_batched_dev(int64_t count, const int32_t *n,
+                                       const int64_t *offA, const mat_elem_t *A,
+                                       const int64_t *offv, const mat_elem_t *b,
+                                       mat_elem_t *x, const uint8_t *kind,
+                                       int32_t *status) {
+  return solve_batched(count, n, offA, A, offv, b, x, kind, status);
+}

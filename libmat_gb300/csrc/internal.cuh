@@ -119,9 +119,25 @@ template <typename T>
 int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
             const int32_t *perm, const T *B, int64_t ldb, T *X, int64_t ldx);
 // Tensor-core rank-K update (tc_gemm.cu).
+// lower: only tiles on/below the diagonal, elements with col <= row;
+// skip: every CTA returns at once when *skip != 0 (may be null).
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
-            const float *alpha_scale, float beta, float *C, int64_t ldc);
+            const float *alpha_scale, float beta, float *C, int64_t ldc,
+            int lower, const int32_t *skip);
+// Cholesky trailing update C22 -= L21 L21^T on the tensor cores (mixed.cu).
+int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
+                   float *C22, int64_t ldc, int lp, const int32_t *info);
+template <typename T>
+int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp);
+// Single-launch triangular solve with one right-hand side (trsv.cu).
+template <typename T>
+int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
+           int64_t ldt, T *x);
+int trsv_status();
+template <typename T>
+int potrs_t(int64_t n, int64_t nrhs, const T *L, int64_t lda, T *B,
+            int64_t ldb, const int32_t *info);
 int tc_error_flag(int clear);
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm);
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,

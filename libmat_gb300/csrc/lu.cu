@@ -197,6 +197,151 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
   }
 }
 
+// Register-resident panel for the reference's 24-column width: thread tid of
+// CTA c owns panel rows c*rpc + tid + r*NT (r < R), all 24 columns of each in
+// registers; the column loop is unrolled so every register index is static.
+// Per column: arg-max over owned rows, warp shuffles, each warp's candidate
+// row staged in shared memory, CTA-level pick, DSMEM publication of the CTA
+// candidate (and of row kk) to every CTA, one cluster barrier, swap, scale,
+// rank-1 update in registers.
+constexpr int kW = kRefBlock;
+
+template <typename T, int NT>
+struct RegPanelSmem {
+  T wrow[NT / 32][kW];
+  T krow[kW];
+  T wkey[NT / 32];
+  int widx[NT / 32];
+  T xval[2][16][kW];
+  T xkey[2][16];
+  int xidx[2][16];
+  T kval[2][kW];
+};
+
+template <typename T, int R, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    lu_panel_reg_kernel(T *__restrict__ A, int64_t lda, int64_t n, int64_t k0,
+                        int rpc, int32_t *__restrict__ ipiv, T eps) {
+  constexpr int NW = NT / 32;
+  __shared__ RegPanelSmem<T, NT> sm;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CS = (int)cluster.num_blocks();
+  const int c = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m = (int)(n - k0);
+  const int rbase = c * rpc;
+  int prow[R];
+  T a[R][kW];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int lr = tid + r * NT;
+    prow[r] = (lr < rpc && rbase + lr < m) ? rbase + lr : -1;
+#pragma unroll
+    for (int j = 0; j < kW; j++)
+      a[r][j] = prow[r] >= 0 ? A[(k0 + prow[r]) + (k0 + j) * lda] : T(0);
+  }
+#pragma unroll
+  for (int kk = 0; kk < kW; kk++) {
+    const int buf = kk & 1;
+    T bk = (T)-2;
+    int bi = INT_MAX;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+      if (prow[r] >= kk) {
+        const T key = piv_key(a[r][kk], prow[r] == kk);
+        if (better(key, prow[r], bk, bi)) { bk = key; bi = prow[r]; }
+      }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ok = __shfl_xor_sync(0xffffffffu, bk, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (better(ok, oi, bk, bi)) { bk = ok; bi = oi; }
+    }
+    // every lane now holds the warp's best; its owner stages the row
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      if (prow[r] >= 0 && prow[r] == bi) {
+#pragma unroll
+        for (int j = 0; j < kW; j++) sm.wrow[warp][j] = a[r][j];
+      }
+      if (prow[r] == kk) {
+#pragma unroll
+        for (int j = 0; j < kW; j++) sm.krow[j] = a[r][j];
+      }
+    }
+    if (lane == 0) { sm.wkey[warp] = bk; sm.widx[warp] = bi; }
+    __syncthreads();
+    T ck = sm.wkey[0];
+    int ci = sm.widx[0], cw = 0;
+#pragma unroll
+    for (int q = 1; q < NW; q++)
+      if (better(sm.wkey[q], sm.widx[q], ck, ci)) { ck = sm.wkey[q]; ci = sm.widx[q]; cw = q; }
+    const bool own_k = (kk >= rbase && kk < rbase + rpc);
+    const int nval = CS * kW;
+    const int total = nval + CS + (own_k ? nval : 0);
+    for (int t = tid; t < total; t += NT) {
+      if (t < nval) {
+        const int q = t / kW, j = t % kW;
+        T *dst = cluster.map_shared_rank(&sm.xval[buf][c][0], q);
+        dst[j] = ci != INT_MAX ? sm.wrow[cw][j] : T(0);
+      } else if (t < nval + CS) {
+        const int q = t - nval;
+        *cluster.map_shared_rank(&sm.xkey[buf][c], q) = ck;
+        *cluster.map_shared_rank(&sm.xidx[buf][c], q) = ci;
+      } else {
+        const int u = t - nval - CS;
+        const int q = u / kW, j = u % kW;
+        *cluster.map_shared_rank(&sm.kval[buf][j], q) = sm.krow[j];
+      }
+    }
+    cluster.sync();
+    int wc = 0;
+    T gk = sm.xkey[buf][0];
+    int p = sm.xidx[buf][0];
+    for (int q = 1; q < CS; q++)
+      if (better(sm.xkey[buf][q], sm.xidx[buf][q], gk, p)) {
+        gk = sm.xkey[buf][q];
+        p = sm.xidx[buf][q];
+        wc = q;
+      }
+    if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
+    const T *u = &sm.xval[buf][wc][0];
+    const T *kv = &sm.kval[buf][0];
+    if (p != kk) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        if (prow[r] == p) {
+#pragma unroll
+          for (int j = 0; j < kW; j++) a[r][j] = kv[j];
+        } else if (prow[r] == kk) {
+#pragma unroll
+          for (int j = 0; j < kW; j++) a[r][j] = u[j];
+        }
+      }
+    }
+    const T piv = u[kk];
+    if (!(fabs(piv) < eps)) {
+      const T inv = T(1) / piv;
+      T uj[kW];
+#pragma unroll
+      for (int j = kk + 1; j < kW; j++) uj[j] = u[j];
+#pragma unroll
+      for (int r = 0; r < R; r++)
+        if (prow[r] > kk) {
+          const T l = a[r][kk] * inv;
+          a[r][kk] = l;
+#pragma unroll
+          for (int j = kk + 1; j < kW; j++) a[r][j] = fma(-uj[j], l, a[r][j]);
+        }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++)
+    if (prow[r] >= 0)
+#pragma unroll
+      for (int j = 0; j < kW; j++) A[(k0 + prow[r]) + (k0 + j) * lda] = a[r][j];
+}
+
 // ---- row swaps ----------------------------------------------------------------
 // Net effect of the swap sequence ipiv[k1..k2) (global row indices, each
 // ipiv[k] >= k) on rows: after it, row pos[t] holds the original row src[t]
@@ -311,55 +456,72 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
 }
 
 // ---- U12 = L11^{-1} A12 with L11 unit lower (TB x TB) ----------------------
-// One thread per right-hand-side column; the column lives in registers and
-// the substitution runs in the reference's axpy order (mat.h:4264-4271).
+// One warp per right-hand-side column: lane l holds rows l, l+32, ... of the
+// column in registers, L11 sits in shared memory; step k broadcasts x_k by a
+// shuffle and every lane updates its rows below k -- the reference's axpy
+// order (mat.h:4264-4271).  Loads and stores of a column are coalesced.
 template <typename T, int TB>
-__global__ void __launch_bounds__(64)
-    trsm_unit_reg_kernel(const T *__restrict__ L, int64_t ldl, T *__restrict__ B,
-                         int64_t ldb, int64_t ncols) {
-  __shared__ T Ls[TB][TB + 1];
-  for (int e = threadIdx.x; e < TB * TB; e += 64) {
-    const int i = e % TB, j = e / TB;
-    Ls[j][i] = L[i + (int64_t)j * ldl];
+__global__ void __launch_bounds__(256)
+    trsm_unit_warp_kernel(const T *__restrict__ L, int64_t ldl,
+                          T *__restrict__ B, int64_t ldb, int64_t ncols) {
+  constexpr int RPL = (TB + 31) / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *Ls = (T *)smem_raw;  // Ls[k*(TB+1) + i] = L(i, k)
+  for (int e = threadIdx.x; e < TB * TB; e += 256) {
+    const int i = e % TB, k = e / TB;
+    Ls[k * (TB + 1) + i] = L[i + (int64_t)k * ldl];
   }
   __syncthreads();
-  const int64_t col = (int64_t)blockIdx.x * 64 + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t col = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
   if (col >= ncols) return;
   T *b = B + col * ldb;
-  T x[TB];
+  T x[RPL];
 #pragma unroll
-  for (int i = 0; i < TB; i++) x[i] = b[i];
+  for (int r = 0; r < RPL; r++) {
+    const int i = lane + 32 * r;
+    x[r] = i < TB ? b[i] : T(0);
+  }
 #pragma unroll
-  for (int k = 0; k < TB; k++)
+  for (int k = 0; k < TB - 1; k++) {
+    const T xk = __shfl_sync(0xffffffffu, x[k / 32], k % 32);
 #pragma unroll
-    for (int i = k + 1; i < TB; i++) x[i] = fma(-Ls[k][i], x[k], x[i]);
+    for (int r = k / 32; r < RPL; r++) {
+      const int i = lane + 32 * r;
+      if (i > k && i < TB) x[r] = fma(-Ls[k * (TB + 1) + i], xk, x[r]);
+    }
+  }
 #pragma unroll
-  for (int i = 1; i < TB; i++) b[i] = x[i];
+  for (int r = 0; r < RPL; r++) {
+    const int i = lane + 32 * r;
+    if (i > 0 && i < TB) b[i] = x[r];
+  }
+}
+
+template <typename T, int TB>
+static int launch_trsm_warp(int64_t ncols, const T *L, int64_t ldl, T *B,
+                            int64_t ldb) {
+  auto k = trsm_unit_warp_kernel<T, TB>;
+  const size_t smem = (size_t)TB * (TB + 1) * sizeof(T);
+  static bool attr = false;
+  if (!attr) {
+    MGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    attr = true;
+  }
+  KtScope kt("trsm_lu", (double)TB * TB * ncols, (double)sizeof(T) * 2.0 * TB * ncols);
+  k<<<(unsigned)((ncols + 7) / 8), 256, smem, ctx()->stream>>>(L, ldl, B, ldb, ncols);
+  MGB_LAUNCHED("trsm_lu");
+  return 0;
 }
 
 template <typename T>
 static int trsm_unit_lower(int tb, int64_t ncols, const T *L, int64_t ldl, T *B,
                            int64_t ldb) {
   if (ncols <= 0 || tb <= 1) return 0;
-  const unsigned grid = (unsigned)((ncols + 63) / 64);
-  if (tb == kOuterBlock && sizeof(T) == 4) {
-    KtScope kt("trsm_lu", (double)tb * tb * ncols, (double)sizeof(T) * 2.0 * tb * ncols);
-    trsm_unit_reg_kernel<T, kOuterBlock><<<grid, 64, 0, ctx()->stream>>>(L, ldl, B, ldb, ncols);
-    MGB_LAUNCHED("trsm_lu");
-    return 0;
-  }
-  if (tb == kRefBlock) {
-    KtScope kt("trsm_lu", (double)tb * tb * ncols, (double)sizeof(T) * 2.0 * tb * ncols);
-    trsm_unit_reg_kernel<T, kRefBlock><<<grid, 64, 0, ctx()->stream>>>(L, ldl, B, ldb, ncols);
-    MGB_LAUNCHED("trsm_lu");
-    return 0;
-  }
-  if (tb == kOuterBlockLp && sizeof(T) == 4) {
-    KtScope kt("trsm_lu", (double)tb * tb * ncols, (double)sizeof(T) * 2.0 * tb * ncols);
-    trsm_unit_reg_kernel<T, kOuterBlockLp><<<grid, 64, 0, ctx()->stream>>>(L, ldl, B, ldb, ncols);
-    MGB_LAUNCHED("trsm_lu");
-    return 0;
-  }
+  if (tb == kRefBlock) return launch_trsm_warp<T, kRefBlock>(ncols, L, ldl, B, ldb);
+  if (tb == kOuterBlock) return launch_trsm_warp<T, kOuterBlock>(ncols, L, ldl, B, ldb);
+  if (tb == kOuterBlockLp) return launch_trsm_warp<T, kOuterBlockLp>(ncols, L, ldl, B, ldb);
   return trsm_left_t<T>(true, false, true, tb, ncols, L, ldl, B, ldb, nullptr);
 }
 
@@ -401,7 +563,7 @@ int PanelState<T>::maxcs = 8;
 template <typename T>
 static int panel_setup() {
   if (PanelState<T>::ready) return 0;
-  auto kern = lu_panel_kernel<T>;
+  auto kern = lu_panel_kernel<T>;  // attribute and launch use this pointer
   MGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kSmemMax));
   // 16-CTA clusters are non-portable: use them only if the device accepts one.
@@ -457,29 +619,134 @@ static int plan_panel(int64_t m, int wmax, PanelPlan *pl) {
                    (long long)m);
 }
 
-// Factor the panel rows [k0,n) x cols [k0, k0+w'), w' <= w chosen to fit.
+template <typename T, int R, int NT>
+static int launch_reg_panel(T *A, int64_t lda, int64_t n, int64_t k0, int cs,
+                            int rpc, int32_t *ipiv, T eps) {
+  auto kern = lu_panel_reg_kernel<T, R, NT>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaGetLastError();
+    attr = true;
+  }
+  const double m = (double)(n - k0);
+  KtScope kt("lu_panel", m * kW * kW, 2.0 * m * kW * sizeof(T));
+  if (cs == 1) {
+    kern<<<1, NT, 0, ctx()->stream>>>(A, lda, n, k0, rpc, ipiv, eps);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = ctx()->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, k0, rpc, ipiv, eps);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(MATGB_ERR_CUDA,
+                       "lu_panel_reg<R=%d,NT=%d> launch (cluster %d, rows %lld, "
+                       "rpc %d): %s", R, NT, cs, (long long)(n - k0), rpc,
+                       cudaGetErrorString(e));
+    }
+  }
+  MGB_LAUNCHED("lu_panel");
+  return 0;
+}
+
+// Register-panel candidates (rows per thread, threads per CTA), cheapest
+// first; the register budget per thread (24*R values + the hoisted pivot row)
+// decides which fit.
+template <typename T>
+static int try_reg_panel(T *A, int64_t lda, int64_t n, int64_t k0,
+                         int32_t *ipiv, T eps, bool *done) {
+  const int64_t m = n - k0;
+  const int maxcs = PanelState<T>::maxcs;
+  *done = false;
+  auto pick = [&](int cap) -> int {
+    for (int cs = 1; cs <= maxcs; cs *= 2)
+      if ((int64_t)cs * cap >= m) return cs;
+    return 0;
+  };
+  if constexpr (sizeof(T) == 4) {
+    int cs;
+    if ((cs = pick(512))) {
+      *done = true;
+      return launch_reg_panel<T, 1, 512>(A, lda, n, k0, cs, (int)((m + cs - 1) / cs), ipiv, eps);
+    }
+    if ((cs = pick(1024))) {
+      *done = true;
+      return launch_reg_panel<T, 2, 512>(A, lda, n, k0, cs, (int)((m + cs - 1) / cs), ipiv, eps);
+    }
+    if ((cs = pick(1024))) {
+      *done = true;
+      return launch_reg_panel<T, 4, 256>(A, lda, n, k0, cs, (int)((m + cs - 1) / cs), ipiv, eps);
+    }
+  } else {
+    int cs;
+    if ((cs = pick(256))) {
+      *done = true;
+      return launch_reg_panel<T, 1, 256>(A, lda, n, k0, cs, (int)((m + cs - 1) / cs), ipiv, eps);
+    }
+    if ((cs = pick(512))) {
+      *done = true;
+      return launch_reg_panel<T, 2, 256>(A, lda, n, k0, cs, (int)((m + cs - 1) / cs), ipiv, eps);
+    }
+  }
+  return 0;
+}
+
+// Factor the panel rows [k0,n) x cols [k0, k0+w'), w' <= w chosen to fit:
+// the register kernel for full 24-column panels that fit a cluster's
+// registers, otherwise the shared-memory kernel.
 template <typename T>
 int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
                T eps, int *w_used) {
   MGB_TRY(panel_setup<T>());
+  if (w >= kW) {
+    bool done = false;
+    MGB_TRY(try_reg_panel<T>(A, lda, n, k0, ipiv, eps, &done));
+    if (done) {
+      *w_used = kW;
+      return 0;
+    }
+  }
   PanelPlan pl;
   MGB_TRY(plan_panel<T>(n - k0, w, &pl));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(pl.cs);
-  cfg.blockDim = dim3(kPanelThreads);
-  cfg.dynamicSmemBytes = pl.smem;
-  cfg.stream = ctx()->stream;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = pl.cs;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
   const double m = (double)(n - k0);
   KtScope kt("lu_panel", m * pl.w * pl.w, 2.0 * m * pl.w * sizeof(T));
-  MGB_CUDA(cudaLaunchKernelEx(&cfg, lu_panel_kernel<T>, A, lda, n, k0, pl.w,
-                              pl.rpc, ipiv, eps));
+  auto kern = lu_panel_kernel<T>;
+  if (pl.cs == 1) {
+    kern<<<1, kPanelThreads, pl.smem, ctx()->stream>>>(A, lda, n, k0, pl.w,
+                                                        pl.rpc, ipiv, eps);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(pl.cs);
+    cfg.blockDim = dim3(kPanelThreads);
+    cfg.dynamicSmemBytes = pl.smem;
+    cfg.stream = ctx()->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = pl.cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, k0, pl.w, pl.rpc,
+                                       ipiv, eps);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(MATGB_ERR_CUDA,
+                       "lu_panel launch (cluster %d, rows %lld, w %d, smem %zu): %s",
+                       pl.cs, (long long)(n - k0), pl.w, pl.smem,
+                       cudaGetErrorString(e));
+    }
+  }
   MGB_LAUNCHED("lu_panel");
   *w_used = pl.w;
   return 0;

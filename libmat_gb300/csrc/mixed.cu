@@ -18,6 +18,8 @@
 
 #include <string.h>
 
+#include <vector>
+
 #include "internal.cuh"
 
 namespace mgb {
@@ -29,20 +31,37 @@ __device__ __forceinline__ uint16_t to16(float v) {
   return __half_as_ushort(__float2half_rn(v));
 }
 
+__device__ __forceinline__ float fp16_scale(unsigned amax_bits) {
+  const float a = __uint_as_float(amax_bits);
+  if (!(a > 0.f) || isinf(a)) return 1.f;
+  int e;
+  frexpf(a, &e);  // a = f * 2^e, f in [0.5, 1)
+  return ldexpf(1.f, 14 - e);
+}
+
 // out[i*Kp + k] = A[i + k*lda] for i < m, k < nb (zero for nb <= k < Kp):
 // L21 (column-major, M-contiguous) to a K-contiguous 16-bit operand.
 template <int BF16>
 __global__ void pack_l21_kernel(const float *__restrict__ A, int64_t lda,
                                 int64_t m, int nb, int Kp,
-                                uint16_t *__restrict__ out) {
+                                uint16_t *__restrict__ out,
+                                const unsigned *__restrict__ amax_bits,
+                                float *__restrict__ scale) {
   __shared__ float t[32][33];
+  // optional FP16 scale s (products of two scaled operands carry s^2)
+  const float s = amax_bits ? fp16_scale(*amax_bits) : 1.f;
+  if (scale && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+    scale[0] = s;
+    scale[1] = 1.f / s;
+    scale[2] = 1.f / (s * s);
+  }
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   const int64_t i0 = (int64_t)blockIdx.x * 32;
   const int k0 = blockIdx.y * 32;
   for (int r = ty; r < 32; r += 8) {
     const int64_t i = i0 + tx;
     const int k = k0 + r;
-    t[r][tx] = (i < m && k < nb) ? A[i + (int64_t)k * lda] : 0.f;
+    t[r][tx] = (i < m && k < nb) ? s * A[i + (int64_t)k * lda] : 0.f;
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
@@ -65,14 +84,6 @@ __global__ void u12_amax_kernel(const float *__restrict__ A, int64_t lda,
   }
   for (int off = 16; off; off >>= 1) m = fmaxf(m, __shfl_xor_sync(~0u, m, off));
   if ((threadIdx.x & 31) == 0) atomicMax(amax_bits, __float_as_uint(m));
-}
-
-__device__ __forceinline__ float fp16_scale(unsigned amax_bits) {
-  const float a = __uint_as_float(amax_bits);
-  if (!(a > 0.f) || isinf(a)) return 1.f;
-  int e;
-  frexpf(a, &e);  // a = f * 2^e, f in [0.5, 1)
-  return ldexpf(1.f, 14 - e);
 }
 
 // out[j*Kp + k] = s * A[k + j*lda] (k < nb), 0 for nb <= k < Kp.
@@ -117,9 +128,11 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
     KtScope kt("lp_pack", 0.0, 6.0 * (m + ncols) * nb);
     dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
     if (lp == 1)
-      pack_l21_kernel<1><<<g, 256, 0, st>>>(A + ke + kb * lda, lda, m, nb, Kp, A16);
+      pack_l21_kernel<1><<<g, 256, 0, st>>>(A + ke + kb * lda, lda, m, nb, Kp,
+                                            A16, nullptr, nullptr);
     else
-      pack_l21_kernel<0><<<g, 256, 0, st>>>(A + ke + kb * lda, lda, m, nb, Kp, A16);
+      pack_l21_kernel<0><<<g, 256, 0, st>>>(A + ke + kb * lda, lda, m, nb, Kp,
+                                            A16, nullptr, nullptr);
     MGB_LAUNCHED("pack_l21");
     const float *U12 = A + kb + ke * lda;
     if (lp == 0) {
@@ -136,7 +149,35 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
     MGB_LAUNCHED("pack_u12");
   }
   return tc_gemm(lp == 1, m, c1 - c0, Kp, A16, Kp, B16 + (c0 - ke) * Kp, Kp,
-                 -1.f, lp == 0 ? sc + 1 : nullptr, 1.f, A + ke + c0 * lda, lda);
+                 -1.f, lp == 0 ? sc + 1 : nullptr, 1.f, A + ke + c0 * lda, lda,
+                 0, nullptr);
+}
+
+// Cholesky: C22 (lower) -= L21 L21^T with L21 packed once to 16 bits and used
+// as both operands; FP16 scales L21 by a power of two s and the epilogue
+// multiplies by 1/s^2.
+int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
+                   float *C22, int64_t ldc, int lp, const int32_t *info) {
+  const int Kp = (nb + 63) / 64 * 64;
+  uint16_t *A16 = (uint16_t *)ws(WS_T0, (size_t)m * Kp * 2);
+  float *sc = (float *)ws(WS_T2, 64);
+  if (!A16 || !sc) return MATGB_ERR_NOMEM;
+  unsigned *amax = (unsigned *)(sc + 4);
+  cudaStream_t st = ctx()->stream;
+  KtScope kt("lp_pack", 0.0, 6.0 * m * nb);
+  dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
+  if (lp == 1) {
+    pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
+  } else {
+    MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
+    u12_amax_kernel<<<grid_cap((int64_t)nb * m), 256, 0, st>>>(L21, lda, (int)m,
+                                                                nb, amax);
+    MGB_LAUNCHED("l21_amax");
+    pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc);
+  }
+  MGB_LAUNCHED("pack_l21");
+  return tc_gemm(lp == 1, m, m, Kp, A16, Kp, A16, Kp, -1.f,
+                 lp == 0 ? sc + 2 : nullptr, 1.f, C22, ldc, 1, info);
 }
 
 // ---- refinement kernels ------------------------------------------------------------
@@ -165,58 +206,74 @@ __global__ void row_abs_sum_kernel(int64_t n, const S *__restrict__ A,
   atomicMax(out, (unsigned long long)__double_as_longlong(s));
 }
 
+// Per-column max |R(:,c)| and max |X(:,c)| (bit patterns of non-negative
+// doubles; NaN propagates).  grid.y = column.
 template <typename S>
-__global__ void amax2_kernel(int64_t n, const S *__restrict__ x,
-                             const S *__restrict__ y,
-                             unsigned long long *__restrict__ out) {
-  double mx = 0, my = 0;
+__global__ void col_amax2_kernel(int64_t n, const S *__restrict__ R,
+                                 int64_t ldr, const S *__restrict__ X,
+                                 int64_t ldx,
+                                 unsigned long long *__restrict__ out) {
+  const int64_t c = blockIdx.y;
+  double mr = 0, mx = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const double a = fabs((double)x[i]), b = fabs((double)y[i]);
-    mx = a > mx || a != a ? a : mx;
-    my = b > my || b != b ? b : my;
+    const double a = fabs((double)R[i + c * ldr]), b = fabs((double)X[i + c * ldx]);
+    mr = (a > mr || a != a) ? a : mr;
+    mx = (b > mx || b != b) ? b : mx;
   }
   for (int off = 16; off; off >>= 1) {
-    mx = fmax(mx, __shfl_xor_sync(~0u, mx, off));
-    my = fmax(my, __shfl_xor_sync(~0u, my, off));
+    const double o1 = __shfl_xor_sync(~0u, mr, off);
+    const double o2 = __shfl_xor_sync(~0u, mx, off);
+    mr = (o1 > mr || o1 != o1) ? o1 : mr;
+    mx = (o2 > mx || o2 != o2) ? o2 : mx;
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicMax(out, (unsigned long long)__double_as_longlong(mx));
-    atomicMax(out + 1, (unsigned long long)__double_as_longlong(my));
+    atomicMax(out + 2 * c, (unsigned long long)__double_as_longlong(mr));
+    atomicMax(out + 2 * c + 1, (unsigned long long)__double_as_longlong(mx));
   }
 }
 
-// rf = r / rn in FP32 (rn read from the device, 1 when zero)
+// RF(:,c) = R(:,c) / rn_c in FP32 (rn_c = out[2c], 1 when zero or not finite)
 template <typename S>
-__global__ void scale_to_float_kernel(int64_t n, const S *__restrict__ r,
+__global__ void scale_to_float_kernel(int64_t n, const S *__restrict__ R,
+                                      int64_t ldr,
                                       const unsigned long long *__restrict__ rn,
-                                      float *__restrict__ rf) {
-  double s = __longlong_as_double((long long)rn[0]);
+                                      float *__restrict__ RF) {
+  const int64_t c = blockIdx.y;
+  double s = __longlong_as_double((long long)rn[2 * c]);
   s = (s > 0 && s < INFINITY) ? 1.0 / s : 1.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    rf[i] = (float)((double)r[i] * s);
+    RF[i + c * n] = (float)((double)R[i + c * ldr] * s);
 }
 
-// x += rn * d
+// X(:,c) += rn_c * D(:,c)
 template <typename S>
-__global__ void update_x_kernel(int64_t n, S *__restrict__ x,
-                                const float *__restrict__ d,
+__global__ void update_x_kernel(int64_t n, S *__restrict__ X, int64_t ldx,
+                                const float *__restrict__ D,
                                 const unsigned long long *__restrict__ rn) {
-  double s = __longlong_as_double((long long)rn[0]);
+  const int64_t c = blockIdx.y;
+  double s = __longlong_as_double((long long)rn[2 * c]);
   if (!(s > 0 && s < INFINITY)) s = 1.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    x[i] = (S)((double)x[i] + s * (double)d[i]);
+    X[i + c * ldx] = (S)((double)X[i + c * ldx] + s * (double)D[i + c * n]);
 }
 
-// Two reduced doubles (stored as their bit patterns) to the host.
-static int fetch2(const unsigned long long *d, double v[2]) {
-  unsigned long long h[2] = {0, 0};
-  MGB_CUDA(cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost,
+template <typename S>
+__global__ void copy_cols_kernel(int64_t n, int64_t nrhs, const S *__restrict__ B,
+                                 int64_t ldb, S *__restrict__ R, int64_t ldr) {
+  const int64_t tot = n * nrhs;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
+       e += (int64_t)gridDim.x * blockDim.x)
+    R[(e % n) + (e / n) * ldr] = B[(e % n) + (e / n) * ldb];
+}
+
+// Reduced doubles (stored as bit patterns) to the host.
+static int fetch(const unsigned long long *d, double *v, int count) {
+  MGB_CUDA(cudaMemcpyAsync(v, d, count * sizeof(double), cudaMemcpyDeviceToHost,
                            ctx()->stream));
   MGB_CUDA(cudaStreamSynchronize(ctx()->stream));
-  memcpy(v, h, sizeof h);
   return 0;
 }
 
@@ -226,109 +283,171 @@ struct IrEvents {
 };
 static IrEvents g_ir;
 
-// Solve A x = b (A n x n in the library type, column-major) with the
-// mixed-precision factorisation and refinement.  x may start anywhere: it is
-// overwritten.
-int gesv_ir(int64_t n, const elem_t *A, int64_t lda, const elem_t *b,
-            elem_t *x, const MatIROpts &o, MatIRReport *rep) {
+// Solve A X = B (A n x n, B/X n x nrhs, column-major, library element type)
+// with a low-precision LU (spd = false) or Cholesky (spd = true) and
+// refinement in the element type.  Returns 0, or sets *not_spd when even the
+// FP32 Cholesky meets a non-positive pivot.
+int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
+             const elem_t *B, int64_t ldb, elem_t *X, int64_t ldx,
+             const MatIROpts &o, MatIRReport *rep, int *not_spd) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
-  if (n <= 0) return 0;
-  if (o.lp_format != 0 && o.lp_format != 1)
-    return set_error(MATGB_ERR_ARG, "lp_format must be 0 (FP16) or 1 (BF16)");
+  if (not_spd) *not_spd = 0;
+  if (n <= 0 || nrhs <= 0) return 0;
+  if (o.lp_format < -1 || o.lp_format > 1)
+    return set_error(MATGB_ERR_ARG,
+                     "lp_format must be 1 (BF16), 0 (FP16) or -1 (FP32)");
   if (!g_ir.ready) {
     for (auto &e : g_ir.e) MGB_CUDA(cudaEventCreate(&e));
     g_ir.ready = true;
   }
   cudaStream_t st = cx->stream;
   float *W = (float *)ws(WS_U, (size_t)n * n * sizeof(float));
-  int32_t *piv = (int32_t *)ws(WS_PIV, (size_t)2 * n * sizeof(int32_t));
-  elem_t *r = (elem_t *)ws(WS_V0, (size_t)n * sizeof(elem_t));
-  float *rf = (float *)ws(WS_V1, (size_t)2 * n * sizeof(float));
-  unsigned long long *red =
-      (unsigned long long *)ws(WS_INFO, 8 * sizeof(unsigned long long));
-  if (!W || !piv || !r || !rf || !red) return MATGB_ERR_NOMEM;
-  float *df = rf + n;
+  int32_t *piv = (int32_t *)ws(WS_PIV, (size_t)(2 * n + 8) * sizeof(int32_t));
+  elem_t *R = (elem_t *)ws(WS_V0, (size_t)n * nrhs * sizeof(elem_t));
+  float *RF = (float *)ws(WS_V1, (size_t)2 * n * nrhs * sizeof(float));
+  unsigned long long *red = (unsigned long long *)ws(
+      WS_INFO, (size_t)(2 * nrhs + 8) * sizeof(unsigned long long));
+  if (!W || !piv || !R || !RF || !red) return MATGB_ERR_NOMEM;
+  float *DF = RF + n * nrhs;
+  int32_t *info = piv + 2 * n;
+  unsigned long long *rs = red + 8;  // 2 per column
+  const dim3 cg(grid_cap(n) < 64 ? grid_cap(n) : 64, (unsigned)nrhs);
+  const unsigned gnn = grid_cap(n * nrhs);
 
-  MGB_CUDA(cudaEventRecord(g_ir.e[0], st));
-  to_float_kernel<elem_t><<<grid_cap(n * n), 256, 0, st>>>(n, n, A, lda, W, n);
-  MGB_LAUNCHED("to_float");
-  MGB_TRY(getrf_t<float>(n, W, n, piv, piv + n, 0.f, o.lp_format));
-  MGB_CUDA(cudaEventRecord(g_ir.e[1], st));
-
-  MGB_CUDA(cudaMemsetAsync(red, 0, 8 * sizeof(unsigned long long), st));
+  // |A|_inf and per-column |B|_inf
+  MGB_CUDA(cudaMemsetAsync(red, 0, (size_t)(2 * nrhs + 8) * sizeof(unsigned long long), st));
   row_abs_sum_kernel<elem_t><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(
-      n, A, lda, red + 4);
+      n, A, lda, red);
   MGB_LAUNCHED("row_abs_sum");
-  amax2_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, b, b, red + 2);
-  MGB_LAUNCHED("amax");
-  double nv[2], av[2];
-  MGB_TRY(fetch2(red + 2, nv));
-  MGB_TRY(fetch2(red + 4, av));
-  const double anorm = av[0], bnorm = nv[0];
+  col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, B, ldb, B, ldb, rs);
+  MGB_LAUNCHED("col_amax");
+  std::vector<double> hv(2 * nrhs + 8);
+  MGB_TRY(fetch(red, hv.data(), 2 * (int)nrhs + 8));
+  const double anorm = hv[0];
+  std::vector<double> bn(nrhs);
+  for (int64_t c = 0; c < nrhs; c++) bn[c] = hv[8 + 2 * c];
   const double eps = sizeof(elem_t) == 8 ? 1.1102230246251565e-16
                                          : 5.960464477539063e-08;
   const double tol = o.tol > 0 ? o.tol : (double)n * eps;
   const int maxit = o.max_iter > 0 ? o.max_iter : 30;
 
-  MGB_CUDA(cudaMemsetAsync(x, 0, (size_t)n * sizeof(elem_t), st));
-  MGB_CUDA(cudaMemcpyAsync(r, b, (size_t)n * sizeof(elem_t),
-                           cudaMemcpyDeviceToDevice, st));
-  double eta = INFINITY, rn = bnorm, xn = 0, prev = INFINITY;
+  int lp = o.lp_format;
+  double eta = INFINITY, rn = 0, xn = 0;
   int it = 0, converged = 0;
-  while (it < maxit) {
-    // correction d = (LU)^{-1} r in FP32 (the first pass is the plain solve)
-    MGB_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(unsigned long long), st));
-    amax2_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, r, r, red);
-    MGB_LAUNCHED("amax");
-    scale_to_float_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, r, red, rf);
-    MGB_LAUNCHED("scale_to_float");
-    MGB_TRY(getrs_t<float>(n, 1, W, n, piv + n, rf, n, df, n));
-    update_x_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, x, df, red);
-    MGB_LAUNCHED("update_x");
-    it++;
-    // residual of the updated x in the refinement precision
-    MGB_CUDA(cudaMemcpyAsync(r, b, (size_t)n * sizeof(elem_t),
-                             cudaMemcpyDeviceToDevice, st));
-    MGB_TRY(gemv_t<elem_t>(n, n, elem_t(-1), A, lda, x, elem_t(1), r));
-    MGB_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(unsigned long long), st));
-    amax2_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, r, x, red);
-    MGB_LAUNCHED("amax");
-    double v[2];
-    MGB_TRY(fetch2(red, v));
-    rn = v[0];
-    xn = v[1];
-    const double den = anorm * xn + bnorm;
-    eta = den > 0 ? rn / den : (rn > 0 ? INFINITY : 0.0);
-    if (eta <= tol) {
-      converged = 1;
-      break;
+  float ms_factor = 0.f;
+  for (int attempt = 0; attempt < 2; attempt++) {
+    MGB_CUDA(cudaEventRecord(g_ir.e[0], st));
+    to_float_kernel<elem_t><<<grid_cap(n * n), 256, 0, st>>>(n, n, A, lda, W, n);
+    MGB_LAUNCHED("to_float");
+    if (spd)
+      MGB_TRY(potrf_t<float>(n, W, n, info, lp));
+    else
+      MGB_TRY(getrf_t<float>(n, W, n, piv, piv + n, 0.f, lp));
+    MGB_CUDA(cudaEventRecord(g_ir.e[1], st));
+    MGB_CUDA(cudaEventSynchronize(g_ir.e[1]));
+    float f = 0.f;
+    cudaEventElapsedTime(&f, g_ir.e[0], g_ir.e[1]);
+    ms_factor += f;
+    if (spd) {
+      int32_t hinfo = 0;
+      MGB_CUDA(cudaMemcpy(&hinfo, info, sizeof hinfo, cudaMemcpyDeviceToHost));
+      if (hinfo != 0) {  // the rounded matrix is not positive definite
+        if (lp >= 0 && o.fp32_fallback) {
+          lp = -1;
+          continue;
+        }
+        if (not_spd) *not_spd = 1;
+        break;
+      }
     }
-    // stop when refinement stagnates or diverges
-    if (!(eta < 0.5 * prev)) break;
-    prev = eta;
+
+    MGB_CUDA(cudaMemsetAsync(red, 0, 8 * sizeof(unsigned long long), st));
+    copy_cols_kernel<elem_t><<<gnn, 256, 0, st>>>(n, nrhs, B, ldb, R, n);
+    MGB_LAUNCHED("copy_cols");
+    for (int64_t c = 0; c < nrhs; c++)
+      MGB_CUDA(cudaMemsetAsync(X + c * ldx, 0, (size_t)n * sizeof(elem_t), st));
+    double prev = INFINITY;
+    while (it < maxit) {
+      // correction D = (LU)^{-1} R in FP32, column-scaled (first pass: plain)
+      MGB_CUDA(cudaMemsetAsync(rs, 0, (size_t)2 * nrhs * sizeof(unsigned long long), st));
+      col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, R, n, R, n, rs);
+      MGB_LAUNCHED("col_amax");
+      scale_to_float_kernel<elem_t><<<cg, 256, 0, st>>>(n, R, n, rs, RF);
+      MGB_LAUNCHED("scale_to_float");
+      if (spd) {
+        MGB_CUDA(cudaMemcpyAsync(DF, RF, (size_t)n * nrhs * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, st));
+        MGB_TRY(potrs_t<float>(n, nrhs, W, n, DF, n, nullptr));
+      } else {
+        MGB_TRY(getrs_t<float>(n, nrhs, W, n, piv + n, RF, n, DF, n));
+      }
+      update_x_kernel<elem_t><<<cg, 256, 0, st>>>(n, X, ldx, DF, rs);
+      MGB_LAUNCHED("update_x");
+      it++;
+      // residual R = B - A X in the refinement precision
+      copy_cols_kernel<elem_t><<<gnn, 256, 0, st>>>(n, nrhs, B, ldb, R, n);
+      MGB_LAUNCHED("copy_cols");
+      if (nrhs == 1 && ldx >= n)
+        MGB_TRY(gemv_t<elem_t>(n, n, elem_t(-1), A, lda, X, elem_t(1), R));
+      else
+        MGB_TRY(gemm_skip_t<elem_t>(false, false, n, nrhs, n, elem_t(-1), A,
+                                    lda, X, ldx, elem_t(1), R, n, 0, nullptr));
+      MGB_CUDA(cudaMemsetAsync(rs, 0, (size_t)2 * nrhs * sizeof(unsigned long long), st));
+      col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, R, n, X, ldx, rs);
+      MGB_LAUNCHED("col_amax");
+      MGB_TRY(fetch(rs, hv.data(), 2 * (int)nrhs));
+      eta = 0;
+      rn = 0;
+      xn = 0;
+      for (int64_t c = 0; c < nrhs; c++) {
+        const double r = hv[2 * c], xv = hv[2 * c + 1];
+        const double den = anorm * xv + bn[c];
+        double e = (den > 0) ? r / den : (r == 0 ? 0.0 : INFINITY);
+        if (r != r || den != den) e = NAN;
+        if (!(e <= eta)) eta = e;  // NaN-propagating max
+        if (!(r <= rn)) rn = r;
+        if (!(xv <= xn)) xn = xv;
+      }
+      if (eta <= tol) {
+        converged = 1;
+        break;
+      }
+      if (!(eta < 0.5 * prev)) break;  // stagnation or divergence
+      prev = eta;
+    }
+    // low-precision factors too coarse for this matrix (kappa * u_low >~ 1):
+    // refactor once with FP32 trailing updates and refine again
+    if (converged || lp < 0 || !o.fp32_fallback || it >= maxit) break;
+    lp = -1;
   }
   MGB_CUDA(cudaEventRecord(g_ir.e[2], st));
   MGB_CUDA(cudaEventSynchronize(g_ir.e[2]));
   if (tc_error_flag(1))
     return set_error(MATGB_ERR_TIMEOUT, "tensor-core update gave up waiting");
   if (rep) {
-    float f = 0, t = 0;
-    cudaEventElapsedTime(&f, g_ir.e[0], g_ir.e[1]);
+    float t = 0;
     cudaEventElapsedTime(&t, g_ir.e[1], g_ir.e[2]);
+    double bmax = 0;
+    for (double v : bn) bmax = v > bmax ? v : bmax;
     rep->iterations = it;
     rep->converged = converged;
     rep->backward_error = eta;
     rep->residual_inf = rn;
     rep->x_inf = xn;
     rep->a_inf = anorm;
-    rep->b_inf = bnorm;
+    rep->b_inf = bmax;
     rep->tol = tol;
-    rep->ms_factor = f;
+    rep->ms_factor = ms_factor;
     rep->ms_refine = t;
-    rep->lp_format = o.lp_format;
+    rep->lp_format = lp;
   }
   return 0;
+}
+
+int gesv_ir(int64_t n, const elem_t *A, int64_t lda, const elem_t *b,
+            elem_t *x, const MatIROpts &o, MatIRReport *rep) {
+  return solve_ir(false, n, 1, A, lda, b, n, x, n, o, rep, nullptr);
 }
 
 }  // namespace mgb
@@ -341,6 +460,7 @@ void matgb_ir_default_opts(MatIROpts *o) {
   o->lp_format = 1;
   o->max_iter = 30;
   o->tol = 0.0;
+  o->fp32_fallback = 1;
 }
 
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
@@ -360,6 +480,64 @@ int matgb_gesv_ir_dev(size_t n, const mat_elem_t *A, size_t lda,
   matgb_ir_default_opts(&o);
   if (opts) o = *opts;
   return gesv_ir((int64_t)n, A, (int64_t)lda, b, x, o, rep);
+}
+
+int matgb_gesv_ir_multi_dev(size_t n, size_t nrhs, const mat_elem_t *A,
+                            size_t lda, const mat_elem_t *B, size_t ldb,
+                            mat_elem_t *X, size_t ldx, const MatIROpts *opts,
+                            MatIRReport *rep) {
+  if (lda < n || ldb < n || ldx < n)
+    return set_error(MATGB_ERR_ARG, "gesv_ir: leading dimension too small");
+  MatIROpts o;
+  matgb_ir_default_opts(&o);
+  if (opts) o = *opts;
+  return solve_ir(false, (int64_t)n, (int64_t)nrhs, A, (int64_t)lda, B,
+                  (int64_t)ldb, X, (int64_t)ldx, o, rep, nullptr);
+}
+
+int matgb_posv_ir_dev(size_t n, size_t nrhs, const mat_elem_t *A, size_t lda,
+                      const mat_elem_t *B, size_t ldb, mat_elem_t *X,
+                      size_t ldx, const MatIROpts *opts, MatIRReport *rep) {
+  if (lda < n || ldb < n || ldx < n)
+    return set_error(MATGB_ERR_ARG, "posv_ir: leading dimension too small");
+  MatIROpts o;
+  matgb_ir_default_opts(&o);
+  if (opts) o = *opts;
+  int not_spd = 0;
+  MGB_TRY(solve_ir(true, (int64_t)n, (int64_t)nrhs, A, (int64_t)lda, B,
+                   (int64_t)ldb, X, (int64_t)ldx, o, rep, &not_spd));
+  return not_spd ? -1 : 0;
+}
+
+int mat_solve_spd_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,
+                     MatIRReport *rep) {
+  MAT_ASSERT_MAT(A);
+  MAT_ASSERT_MAT(x);
+  MAT_ASSERT_MAT(b);
+  MAT_ASSERT_SQUARE(A);
+  MAT_ASSERT(b->rows == A->rows && x->rows == A->cols);
+  MAT_ASSERT(x->cols == b->cols);
+  if (!ctx()) return MATGB_ERR_NO_DEVICE;
+  const int64_t n = A->rows, nr = b->cols;
+  cudaStream_t st = ctx()->stream;
+  elem_t *dA = (elem_t *)ws(WS_A, (size_t)n * n * sizeof(elem_t));
+  elem_t *db = (elem_t *)ws(WS_B, (size_t)n * nr * sizeof(elem_t));
+  elem_t *dx = (elem_t *)ws(WS_X, (size_t)n * nr * sizeof(elem_t));
+  if (!dA || !db || !dx) return MATGB_ERR_NOMEM;
+  MGB_CUDA(cudaMemcpyAsync(dA, A->data, (size_t)n * n * sizeof(elem_t),
+                           cudaMemcpyHostToDevice, st));
+  MGB_CUDA(cudaMemcpyAsync(db, b->data, (size_t)n * nr * sizeof(elem_t),
+                           cudaMemcpyHostToDevice, st));
+  MatIROpts o;
+  matgb_ir_default_opts(&o);
+  if (opts) o = *opts;
+  int not_spd = 0;
+  MGB_TRY(solve_ir(true, n, nr, dA, n, db, n, dx, n, o, rep, &not_spd));
+  if (not_spd) return -1;
+  MGB_CUDA(cudaMemcpyAsync(x->data, dx, (size_t)n * nr * sizeof(elem_t),
+                           cudaMemcpyDeviceToHost, st));
+  MGB_CUDA(cudaStreamSynchronize(st));
+  return 0;
 }
 
 int mat_solve_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,

@@ -59,6 +59,7 @@ int set_error(int code, const char *fmt, ...) {
 }
 
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+  cudaGetLastError();  // do not let a returned error resurface at a later check
   return set_error(MATGB_ERR_CUDA, "%s failed: %s (%s:%d)", what,
                    cudaGetErrorString(e), file, line);
 }

@@ -42,12 +42,13 @@ struct TcSmem {
   int timeout;
 };
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 2)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                    const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
                    float alpha, const float *__restrict__ alpha_scale,
                    float beta, float *__restrict__ C, int64_t ldc,
-                   uint32_t idesc, int *__restrict__ err) {
+                   uint32_t idesc, int lower, const int32_t *__restrict__ skip,
+                   int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // align the carve-out to 1024 B (the swizzle atom)
   TcSmem &s = *reinterpret_cast<TcSmem *>(
@@ -55,6 +56,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
   const int nkb = K / kTcBK;
+  // whole-CTA exits before any barrier or TMEM allocation: a failed earlier
+  // step (skip flag) or, for a lower-triangular update, a tile strictly above
+  // the diagonal
+  if (skip && *skip != 0) return;
+  if (lower && n0 >= m0 + kTcBM) return;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < kTcKB; i++) tc::mbar_init(&s.full[i], 1);
@@ -106,33 +112,49 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                    : "memory");
     }
   } else if (warp < 8) {
+    // Epilogue: warp w reads TMEM lane quarter w%4 (rows q*32..q*32+31) and
+    // column half w/4, in 16-column chunks; the C values of the next chunk are
+    // loaded before the current one is finished (the first before the
+    // accumulator is even ready), so HBM latency overlaps the MMAs.
+    constexpr int CH = 16, NCH = kTcBN / 2 / CH;
+    const int q = warp & 3, half = warp >> 2;
+    const int row = m0 + q * 32 + lane;
+    const int cbase = n0 + half * (kTcBN / 2);
+    const bool rok = row < M;
+    const bool rd = beta != 0.f;
+    float *cp = C + (int64_t)cbase * ldc + row;
+    auto load = [&](float (&d)[CH], int ch) {
+#pragma unroll
+      for (int j = 0; j < CH; j++) {
+        const int col = ch * CH + j;
+        d[j] = (rok && rd && cbase + col < N) ? cp[(int64_t)col * ldc] : 0.f;
+      }
+    };
+    float cur[CH];
+    load(cur, 0);
     const bool ready = tc::mbar_wait(&s.done, 0, kTcWaitLimit);
     tc::tc_fence_after();
     if (ready && !s.timeout) {
-      const int q = warp & 3, half = warp >> 2;
-      const int row = m0 + q * 32 + lane;
       const float al = alpha_scale ? alpha * (*alpha_scale) : alpha;
 #pragma unroll 1
-      for (int cc = 0; cc < kTcBN / 2; cc += 32) {
-        const int col0 = half * (kTcBN / 2) + cc;
-        float v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col0, v);
-        if (row < M) {
-          float *cp = C + (int64_t)(n0 + col0) * ldc + row;
-          const int ncol = min(32, N - (n0 + col0));
-          if (beta != 0.f) {
-            float old[32];
+      for (int ch = 0; ch < NCH; ch++) {
+        float nxt[CH];
+        if (ch + 1 < NCH) load(nxt, ch + 1);
+        float v[CH];
+        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) +
+                          (uint32_t)(half * (kTcBN / 2) + ch * CH),
+                      v);
+        if (rok) {
 #pragma unroll
-            for (int j = 0; j < 32; j++)
-              if (j < ncol) old[j] = cp[(int64_t)j * ldc];
-#pragma unroll
-            for (int j = 0; j < 32; j++)
-              if (j < ncol) cp[(int64_t)j * ldc] = fmaf(al, v[j], beta * old[j]);
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; j++)
-              if (j < ncol) cp[(int64_t)j * ldc] = al * v[j];
+          for (int j = 0; j < CH; j++) {
+            const int col = ch * CH + j;
+            if (cbase + col < N && (!lower || cbase + col <= row))
+              cp[(int64_t)col * ldc] = fmaf(al, v[j], beta * cur[j]);
           }
+        }
+        if (ch + 1 < NCH) {
+#pragma unroll
+          for (int j = 0; j < CH; j++) cur[j] = nxt[j];
         }
       }
     } else if (!ready) {
@@ -192,7 +214,8 @@ static int make_map(CUtensorMap *m, const void *ptr, int bf16, int64_t rows,
 // <= 128; lda, ldb multiples of 8 elements; 16-byte aligned bases.
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
-            const float *alpha_scale, float beta, float *C, int64_t ldc) {
+            const float *alpha_scale, float beta, float *C, int64_t ldc,
+            int lower, const int32_t *skip) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (M <= 0 || N <= 0) return 0;
@@ -206,11 +229,12 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
   MGB_TRY(make_map(&mb, B, bf16, N, K, ldb, kTcBN));
   dim3 grid((unsigned)((M + kTcBM - 1) / kTcBM), (unsigned)((N + kTcBN - 1) / kTcBN));
   const uint32_t idesc = tc::idesc_f16(bf16 ? 1 : 0, kTcBM, kTcBN);
-  KtScope kt("tc_gemm", 2.0 * M * N * K,
-             4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N + 2.0 * (M + N) * K);
+  const double frac = lower ? 0.5 : 1.0;
+  KtScope kt("tc_gemm", 2.0 * M * N * K * frac,
+             4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N * frac + 2.0 * (M + N) * K);
   tc_gemm_kernel<<<grid, kTcThreads, sizeof(TcSmem) + 1024, cx->stream>>>(
       ma, mb, (int)M, (int)N, (int)K, alpha, alpha_scale, beta, C, ldc, idesc,
-      g_tc_err);
+      lower, skip, g_tc_err);
   MGB_LAUNCHED("tc_gemm");
   return 0;
 }
@@ -234,7 +258,8 @@ int matgb_tc_gemm_dev(int bf16, size_t M, size_t N, size_t K, const void *A,
                       float beta, float *C, size_t ldc) {
   if (ldc < M) return set_error(MATGB_ERR_ARG, "tc_gemm: ldc < M");
   return tc_gemm(bf16, (int64_t)M, (int64_t)N, (int64_t)K, A, (int64_t)lda, B,
-                 (int64_t)ldb, alpha, nullptr, beta, C, (int64_t)ldc);
+                 (int64_t)ldb, alpha, nullptr, beta, C, (int64_t)ldc, 0,
+                 nullptr);
 }
 
 int matgb_tc_status(void) {

@@ -125,6 +125,8 @@ int trsm_left_t(bool lower, bool trans, bool unit, int64_t n, int64_t nrhs,
                 const int32_t *info) {
   if (!ctx()) return MATGB_ERR_NO_DEVICE;
   if (n <= 0 || nrhs <= 0) return 0;
+  // one right-hand side: the single-launch solver (no failure flag to honour)
+  if (nrhs == 1 && !info) return trsv_t<T>(lower, trans, unit, n, Tm, ldt, B);
   const bool el = (lower != trans);
   // Pointer to op(T)(r0, c0) for use as a GEMM operand with transpose 'trans'.
   auto sub = [&](int64_t r0, int64_t c0) {

@@ -154,14 +154,18 @@ def conditioned(n, kappa, seed):
     return np.asfortranarray((U * s) @ V.T)
 
 
-@pytest.mark.parametrize("lp", [1, 0])
-@pytest.mark.parametrize("n,kappa", [(512, 1e2), (1024, 1e2), (1000, 1e3)])
-def test_ir_f64_reaches_fp64_backward_error(gpu, lp, n, kappa):
+# kappa * u_16 < 1 (BF16 u = 2^-8, FP16 u = 2^-11): the 16-bit factors refine
+# to FP64 accuracy on their own; beyond it the FP32 refactorisation takes over.
+@pytest.mark.parametrize("lp,n,kappa,final_lp", [
+    (1, 512, 1e2, 1), (0, 512, 1e2, 0), (1, 1024, 1e2, 1), (0, 1024, 1e2, 0),
+    (0, 1000, 1e3, 0), (1, 1000, 1e4, -1), (0, 1000, 1e6, -1),
+    (-1, 700, 1e6, -1)])
+def test_ir_f64_reaches_fp64_backward_error(gpu, lp, n, kappa, final_lp):
     L = gpu["f64"]
     A = conditioned(n, kappa, 7 + n)
     b = np.random.default_rng(n).standard_normal(n)
     x, rep = L.mat_solve_ir(A, b, lp_format=lp)
-    assert rep["converged"] == 1, rep
+    assert rep["converged"] == 1 and rep["lp_format"] == final_lp, rep
     eta = np.abs(b - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
                                      + np.abs(b).max())
     assert eta <= n * 2.0 ** -53, (eta, rep)
@@ -185,3 +189,62 @@ def test_ir_reports_nonconvergence_for_singular(gpu):
     b = np.arange(n, dtype=np.float64)
     x, rep = L.mat_solve_ir(A, b, lp_format=1, max_iter=5)
     assert rep["converged"] == 0 and rep["iterations"] <= 5
+    assert not np.isfinite(rep["backward_error"]) or rep["backward_error"] > 1e-6
+
+
+def spd_conditioned(n, lam_max, seed):
+    """Q diag(lambda) Q^T, lambda log-uniform in [1, lam_max]."""
+    rs = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rs.standard_normal((n, n)))
+    lam = np.exp(rs.uniform(0, np.log(lam_max), n))
+    A = (Q * lam) @ Q.T
+    return np.asfortranarray((A + A.T) / 2)
+
+
+@pytest.mark.parametrize("lp,n,lam,final_lp", [
+    (1, 600, 1e2, 1), (0, 700, 1e3, 0), (1, 500, 1e6, -1), (-1, 400, 1e6, -1)])
+def test_spd_ir_reaches_fp64_backward_error(gpu, lp, n, lam, final_lp):
+    L = gpu["f64"]
+    A = spd_conditioned(n, lam, 31 + n)
+    B = np.random.default_rng(n).standard_normal((n, 8))
+    X, ret, rep = L.mat_solve_spd_ir(A, B, lp_format=lp)
+    assert ret == 0 and rep["converged"] == 1 and rep["lp_format"] == final_lp, rep
+    for c in range(B.shape[1]):
+        x, b = X[:, c], B[:, c]
+        eta = np.abs(b - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
+                                         + np.abs(b).max())
+        assert eta <= n * 2.0 ** -53, (c, eta)
+
+
+def test_spd_ir_not_spd_returns_minus_one(gpu):
+    L = gpu["f64"]
+    A = np.eye(300)
+    A[150, 150] = -1.0
+    X, ret, rep = L.mat_solve_spd_ir(A, np.ones((300, 2)), lp_format=1)
+    assert ret == -1
+
+
+def test_lp_cholesky_reconstructs(gpu):
+    """FP32 Cholesky with BF16/FP16 tensor-core SYRK updates: L L^T = A up to
+    the 16-bit rounding of the update operands."""
+    L = gpu["f32"]
+    n = 900
+    A = spd_conditioned(n, 1e2, 5).astype(np.float32)
+    for lp, tol in ((1, 3e-2), (0, 4e-3), (-1, 1e-5)):
+        dA = L.dalloc(A.nbytes)
+        di = L.dalloc(4)
+        try:
+            L.h2d(dA, A)
+            L.check(L.c.matgb_potrf_lp_dev(n, dA, n, di, lp), "potrf_lp")
+            F = np.empty((n, n), np.float32, order="F")
+            L.d2h(F, dA)
+            info = np.zeros(1, np.int32)
+            L.d2h(info, di)
+            L.check(L.c.matgb_tc_status(), "tc_status")
+        finally:
+            L.dfree(dA)
+            L.dfree(di)
+        assert info[0] == 0
+        Lf = np.tril(F.astype(np.float64))
+        err = np.abs(Lf @ Lf.T - A).max() / np.abs(A).max()
+        assert err <= tol, (lp, err)

@@ -202,7 +202,7 @@ def test_not_spd_returns_minus_one_at_any_block(gpu, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("n", [1, 3, 64, 95, 96, 97, 200, 500])
+@pytest.mark.parametrize("n", [1, 3, 64, 65, 95, 96, 97, 200, 500, 1000, 2049])
 def test_tri_solves_vs_oracle(gpu, prec, n):
     L_ = gpu[prec]
     O = Oracle(prec)
