@@ -141,22 +141,29 @@ int matgb_gemv_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
 typedef struct {
   int lp_format;     /* 1 = BF16 (default), 0 = FP16 (per-block power-of-2
                         scale), -1 = FP32 trailing updates (SIMT)            */
-  int max_iter;      /* refinement solves over all attempts (default 30)     */
+  int max_iter;      /* factor solves over all attempts (default 100)        */
   double tol;        /* target backward error; <= 0: n * unit roundoff of the
                         element type (n * 2^-53 in libmatgb_f64)             */
   int fp32_fallback; /* 1 (default): if refinement with the 16-bit factors
-                        stagnates (kappa(A) * u_16 >~ 1), refactor once with
-                        FP32 trailing updates and refine again               */
+                        stagnates, refactor once with FP32 trailing updates
+                        and refine again                                     */
+  int krylov;        /* 1 (default): a single right-hand side is refined by
+                        flexible GMRES preconditioned with the low-precision
+                        factors (converges for kappa(A) * u_16 well above 1);
+                        0: classic refinement, one factor solve per step    */
+  int krylov_dim;    /* Krylov vectors per cycle (default 40, at most 64)   */
 } MatIROpts;
 
 typedef struct {
-  int iterations;        /* LU solves done (1 = no refinement needed)        */
+  int iterations;        /* factor solves done (1 = no refinement needed)    */
   int converged;         /* backward_error <= tol                             */
   int lp_format;         /* format of the factors that produced x           */
   double backward_error; /* |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf)      */
   double residual_inf, x_inf, a_inf, b_inf, tol;
   double ms_factor;      /* GPU time of conversion + factorisation(s)         */
   double ms_refine;      /* GPU time of solves, residuals and updates         */
+  int refinements;       /* residuals computed in the element type            */
+  int krylov_steps;      /* FGMRES steps over all cycles (0: classic)         */
 } MatIRReport;
 
 void matgb_ir_default_opts(MatIROpts *o);

@@ -29,7 +29,8 @@ class PermStruct(C.Structure):
 
 class MatIROpts(C.Structure):
     _fields_ = [("lp_format", C.c_int), ("max_iter", C.c_int),
-                ("tol", C.c_double), ("fp32_fallback", C.c_int)]
+                ("tol", C.c_double), ("fp32_fallback", C.c_int),
+                ("krylov", C.c_int), ("krylov_dim", C.c_int)]
 
 
 class MatIRReport(C.Structure):
@@ -38,7 +39,8 @@ class MatIRReport(C.Structure):
                 ("residual_inf", C.c_double), ("x_inf", C.c_double),
                 ("a_inf", C.c_double), ("b_inf", C.c_double),
                 ("tol", C.c_double), ("ms_factor", C.c_double),
-                ("ms_refine", C.c_double)]
+                ("ms_refine", C.c_double), ("refinements", C.c_int),
+                ("krylov_steps", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -301,12 +303,23 @@ class Lib:
         self.check(0, "solve_multi")
         return (X, int(r)) if spd else X
 
-    def mat_solve_ir(self, A, b, lp_format=1, max_iter=30, tol=0.0,
-                     fp32_fallback=1):
+    def ir_opts(self, **kw):
+        """MatIROpts with the library defaults, fields overridden by kw."""
+        o = MatIROpts()
+        self.c.matgb_ir_default_opts(C.byref(o))
+        for k, v in kw.items():
+            if v is not None:
+                setattr(o, k, v)
+        return o
+
+    def mat_solve_ir(self, A, b, lp_format=1, max_iter=None, tol=0.0,
+                     fp32_fallback=1, krylov=None, krylov_dim=None):
         """Mixed-precision LU + refinement; returns (x, report dict)."""
         A, b = self.arr(A), self.arr(b)
         x = np.zeros((A.shape[1], 1), self.dtype, order="F")
-        o = MatIROpts(lp_format, max_iter, tol, fp32_fallback)
+        o = self.ir_opts(lp_format=lp_format, max_iter=max_iter, tol=tol,
+                         fp32_fallback=fp32_fallback, krylov=krylov,
+                         krylov_dim=krylov_dim)
         rep = MatIRReport()
         rc = self.c.mat_solve_ir(C.byref(self.mat(x)), C.byref(self.mat(A)),
                                  C.byref(self.mat(b)), C.byref(o), C.byref(rep))
@@ -345,12 +358,14 @@ class Lib:
                 self.dfree(d)
         return [x[o:o + k] for o, k in zip(offv, ns)], status
 
-    def mat_solve_spd_ir(self, A, B, lp_format=1, max_iter=30, tol=0.0,
-                         fp32_fallback=1):
+    def mat_solve_spd_ir(self, A, B, lp_format=1, max_iter=None, tol=0.0,
+                         fp32_fallback=1, krylov=None, krylov_dim=None):
         """Mixed-precision Cholesky + refinement, many RHS; (X, ret, report)."""
         A, B = self.arr(A), self.arr(B)
         X = np.zeros((A.shape[1], B.shape[1]), self.dtype, order="F")
-        o = MatIROpts(lp_format, max_iter, tol, fp32_fallback)
+        o = self.ir_opts(lp_format=lp_format, max_iter=max_iter, tol=tol,
+                         fp32_fallback=fp32_fallback, krylov=krylov,
+                         krylov_dim=krylov_dim)
         rep = MatIRReport()
         rc = self.c.mat_solve_spd_ir(C.byref(self.mat(X)), C.byref(self.mat(A)),
                                      C.byref(self.mat(B)), C.byref(o),

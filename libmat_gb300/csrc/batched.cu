@@ -4,21 +4,25 @@
 //
 // Layout: all matrices packed back to back in one buffer (system s at
 // A + offA[s], column-major, leading dimension n_s), right-hand sides and
-// solutions packed at offv[s].  kind[s] = 0 solves by partial-pivot LU with the
-// reference's pivot rule (first index of max |a|, tiny pivots swapped in but
-// not divided by), kind[s] = 1 by Cholesky (status -1 when a pivot is <= 0,
-// as mat_solve_spd returns -1; x is then left untouched).
+// solutions packed at offv[s].  kind[s] = 0 solves a general system with the
+// reference's partial-pivoting rule (first index of max |a|, tiny pivots
+// swapped in but not eliminated with), kind[s] = 1 an SPD system (status -1
+// when a pivot is <= 0, as mat_solve_spd returns -1; x is then left
+// untouched).
 //
 // Kernel: one thread per matrix row, the row (and its right-hand-side entry)
-// held in registers, one system per NB-thread group, NB a compile-time size
-// bucket (16, 32, 64, 96, 128); the double build covers orders up to 64.  With the elimination loop fully unrolled
-// every register index is static.  LU step k: arg-max of column k across the
-// rows (warp shuffles, then shared memory across warps), exchange of rows k
-// and p through shared memory, rank-1 update of the owned row; the right-hand
-// side rides along as an extra column, so forward substitution is fused;
-// back substitution broadcasts one x_j per step.  Cholesky: right-looking with
-// the current column broadcast through shared memory, forward substitution
-// fused, back substitution with L^T read from shared memory.
+// held in registers, one system per group of NB threads, NB a compile-time
+// size bucket (16, 32, 64, 96, 128; two 16-row systems share a warp); the
+// double build covers orders up to 64.  Gauss-Jordan elimination in a
+// shifted register frame (the pivot column is always register 0, so the step
+// loop is an ordinary loop over statically indexed registers): one barrier
+// per step, the pivot chosen by warp shuffles then across warps through
+// shared memory, the winning row read by every row from its warp's slot,
+// rows above the pivot eliminated too so no back substitution is needed.
+// General systems use partial pivoting with mat_plu's pivot rule (rows trade
+// roles, not data); SPD systems rebuild the symmetric matrix from the lower
+// triangle (what mat_chol reads), do no exchanges and report -1 when a
+// pivot -- the Schur-complement diagonal mat_chol tests -- is <= 0.
 //
 // Scheduling: a device-side pre-pass sorts systems into (size bucket, kind)
 // queues; one persistent launch per queue pulls systems with an atomic

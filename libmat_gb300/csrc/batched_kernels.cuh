@@ -1,7 +1,7 @@
 // Device side of the batched small-system solver (see batched.cu): size
-// buckets, per-row register kernels for LU and Cholesky.  Included by one
-// translation unit per bucket so the heavily unrolled kernels compile in
-// parallel.
+// buckets and the per-row register kernel shared by the general (partial
+// pivoting) and SPD systems.  Included by one translation unit per bucket so
+// the kernels compile in parallel.
 #pragma once
 
 #include "internal.cuh"
@@ -25,6 +25,9 @@ struct BatchQueues {
   int fill[kNumQueues];   // scatter cursors
 };
 
+// |v| as a pivot key; NaN loses to every number except in the first row of
+// the search, where it wins (mat__iamax keeps its starting element when
+// nothing compares greater).
 template <typename T>
 __device__ __forceinline__ T bkey(T v, bool first) {
   T a = fabs(v);
@@ -32,220 +35,238 @@ __device__ __forceinline__ T bkey(T v, bool first) {
   return a;
 }
 
-// Threads per system: one per row, at least a full warp (rows >= NB idle).
+// Threads per system: one per row.  NB = 16 packs two systems in a warp.
 template <int NB>
 struct Tpg {
-  static constexpr int v = NB < 32 ? 32 : NB;
+  static constexpr int v = NB < 16 ? 16 : NB;
+};
+// Columns per statically unrolled chunk of the row.
+template <int NB>
+struct Chunk {
+  static constexpr int v = NB < 32 ? NB : 32;
+};
+// Warps (or half warps) per system.
+template <int NB>
+struct Warps {
+  static constexpr int v = NB <= 32 ? 1 : NB / 32;
 };
 
-// Group-wide barrier: the group is one warp for NB <= 32 (several groups per
-// CTA), otherwise the whole CTA (one group per CTA).
+// Lanes of the warp that belong to this thread's system.
+template <int NB>
+__device__ __forceinline__ unsigned group_mask() {
+  if constexpr (NB <= 16)
+    return 0xffffu << (threadIdx.x & 16);
+  else
+    return 0xffffffffu;
+}
+
+// Group-wide barrier: a half warp (NB = 16), a warp (NB = 32) or the whole
+// CTA (one system per CTA).
 template <int NB>
 __device__ __forceinline__ void gsync() {
-  if (NB <= 32) __syncwarp();
-  else __syncthreads();
+  if constexpr (NB <= 32)
+    __syncwarp(group_mask<NB>());
+  else
+    __syncthreads();
 }
+
+// Row slot: slot[3 + k] = a[k] (k < NB) and slot[NB + 3] = right-hand side,
+// so the update's u[j + 1] = slot[j + 4] starts on a 16-byte boundary for
+// every 4th (float) or 2nd (double) j and is read with vector loads.
+template <int NB>
+struct SlotLen {
+  static constexpr int v = NB + 4;
+};
 
 template <typename T, int NB>
 struct BatchSmem {
-  T rowU[2][NB + 1];   // pivot row (incoming row k)
-  T rowK[2][NB + 1];   // old row k (goes to row p)
-  T wkey[(NB + 31) / 32];
-  int widx[(NB + 31) / 32];
-  T bc;                // broadcast scalar
-  T bc2[2];            // double-buffered broadcast (LU back substitution)
-  int flag;
-  T Lc[NB * (NB + 1) / 2];  // Cholesky: column k at [k*NB - k(k-1)/2, ...)
+  __align__(16) T slot[2][Warps<NB>::v][SlotLen<NB>::v];  // by step parity
+  T wkey[2][Warps<NB>::v];
+  int widx[2][Warps<NB>::v];
 };
 
-// The elimination steps are generated by template recursion so that every
-// register index is a compile-time constant (a plain loop of 64-128 steps is
-// not fully unrolled by the compiler and the row would spill to local memory).
-template <typename T, int NB, int K>
-struct LuStep {
-  // Thread i keeps its physical row; lr is the logical row it currently plays
-  // (row exchanges swap roles, not data).  The pivot is the first logical
-  // index with max |a| among logical rows >= K (mat__iamax's rule).
-  static __device__ __forceinline__ void run(T (&a)[NB], T &rb, int &lr, int n,
-                                             int i, bool act,
-                                             BatchSmem<T, NB> &sm, T eps) {
-    if constexpr (K < NB - 1) {
-      if (K >= n - 1) return;  // the reference never searches the last column
-      constexpr int buf = K & 1;
-      const int lane = i & 31, w = i >> 5;
+template <typename T>
+struct VecOf;
+template <>
+struct VecOf<float> {
+  using type = float4;
+  static constexpr int w = 4;
+  static __device__ __forceinline__ void get(const float *p, float (&o)[4]) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+};
+template <>
+struct VecOf<double> {
+  using type = double2;
+  static constexpr int w = 2;
+  static __device__ __forceinline__ void get(const double *p, double (&o)[2]) {
+    const double2 v = *reinterpret_cast<const double2 *>(p);
+    o[0] = v.x; o[1] = v.y;
+  }
+};
+
+// Write the owned row (its live leading entries, chunk by chunk) and its
+// right-hand side into a slot.
+template <typename T, int NB>
+__device__ __forceinline__ void put_row(T *slot, const T (&a)[NB], T rb,
+                                        int n_live) {
+  constexpr int C = Chunk<NB>::v;
+#pragma unroll
+  for (int c = 0; c < NB / C; c++) {
+    if (c * C < n_live) {
+#pragma unroll
+      for (int k = 0; k < C; k++) slot[3 + c * C + k] = a[c * C + k];
+    }
+  }
+  slot[NB + 3] = rb;
+}
+
+// One elimination step in the shifted frame: a[j] <- a[j+1] - u[j+1] * l over
+// the chunks that still hold live output columns (j < n_out); entries past
+// the live ones are never read into live ones, so partial chunks need no
+// masking.  rb <- rb - u_rhs * l.
+template <typename T, int NB>
+__device__ __forceinline__ void shift_update(T (&a)[NB], T &rb, const T *slot,
+                                             T l, int n_out) {
+  constexpr int C = Chunk<NB>::v;
+  constexpr int W = VecOf<T>::w;
+#pragma unroll
+  for (int c = 0; c < NB / C; c++) {
+    if (c * C < n_out) {
+#pragma unroll
+      for (int j0 = c * C; j0 < c * C + C; j0 += W) {
+        T u[W];
+        VecOf<T>::get(slot + j0 + 4, u);
+#pragma unroll
+        for (int q = 0; q < W; q++) {
+          const int j = j0 + q;
+          if (j + 1 < NB) a[j] = fma(-u[q], l, a[j + 1]);
+        }
+      }
+    }
+  }
+  rb = fma(-slot[NB + 3], l, rb);
+}
+
+// Solve one system of order n <= NB with the group's NB threads (thread i
+// owns row i).  Gauss-Jordan in a shifted register frame: before step K every
+// row holds its entries of columns K..n-1 in a[0..n-K-1], so the pivot column
+// is always a[0] and every register index is static while the step loop is
+// an ordinary loop (compact code).  Step K picks the pivot row, every other
+// row eliminates column K (rows above the pivot included, so no back
+// substitution is needed), and all rows shift left by one.  At the end the
+// row playing logical row r holds x_r * d_r in its right-hand side, d_r its
+// pivot.
+//
+// KIND 0 (general): partial pivoting with mat_plu's rule -- the first
+// logical row of max |a| among rows K..n-1, the last column not searched --
+// rows trading roles (a logical row index per thread) instead of data.
+// Each warp's best candidate stages its row in shared memory before the one
+// barrier of the step, so the winner's row is read from its warp's slot.  A
+// pivot below eps is not eliminated with (mat_plu skips such columns).
+// KIND 1 (SPD): the symmetric matrix is rebuilt from the lower triangle
+// (all that mat_chol reads), no row exchanges, and a pivot d_K <= 0 -- the
+// Schur-complement diagonal mat_chol tests -- makes the status -1 and leaves
+// x untouched.  Returns the status.
+template <typename T, int NB, int KIND>
+__device__ int solve_one(const T *__restrict__ A, int n,
+                         const T *__restrict__ b, T *__restrict__ x,
+                         BatchSmem<T, NB> &sm, int i, T eps) {
+  const bool act = i < n;
+  const int w = NB <= 32 ? 0 : (i >> 5);
+  const unsigned gm = group_mask<NB>();
+  T a[NB];
+  T rb = act ? b[i] : T(0);
+#pragma unroll
+  for (int j = 0; j < NB; j++) {
+    T v = T(0);
+    if (act && j < n) {
+      if (KIND == 1 && j > i)
+        v = A[j + (int64_t)i * n];  // upper entry mirrored from the lower
+      else
+        v = A[i + (int64_t)j * n];
+    }
+    a[j] = v;
+  }
+  int lr = i;  // logical row played by this thread
+  T dg = T(1);
+  for (int K = 0; K < n; K++) {
+    const int par = K & 1;
+    const int live = n - K;  // live entries per row before the step
+    int p = K;
+    int pw = 0;
+    if (KIND == 0 && K < n - 1) {
       const bool cand = act && lr >= K;
-      T key = cand ? bkey(a[K], lr == K) : (T)-2;
+      T key = cand ? bkey(a[0], lr == K) : (T)-2;
       int idx = cand ? lr : 0x7fffffff;
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const T ok = __shfl_xor_sync(0xffffffffu, key, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, idx, off);
-        if (ok > key || (ok == key && oi < idx)) { key = ok; idx = oi; }
-      }
-      int p = idx;
-      if constexpr (NB > 32) {
-        if (lane == 0) { sm.wkey[w] = key; sm.widx[w] = idx; }
-        gsync<NB>();
-        T bk = sm.wkey[0];
-        p = sm.widx[0];
-#pragma unroll
-        for (int q = 1; q < NB / 32; q++) {
-          const T kq = sm.wkey[q];
-          const int iq = sm.widx[q];
-          if (kq > bk || (kq == bk && iq < p)) { bk = kq; p = iq; }
+      for (int off = (NB <= 16 ? 8 : 16); off > 0; off >>= 1) {
+        const T ok = __shfl_xor_sync(gm, key, off);
+        const int oi = __shfl_xor_sync(gm, idx, off);
+        if (ok > key || (ok == key && oi < idx)) {
+          key = ok;
+          idx = oi;
         }
       }
-      // the pivot row's trailing part is broadcast; roles K and p swap
-      const int old = lr;
-      if (act && old == p) {
-#pragma unroll
-        for (int j = K; j < NB; j++) sm.rowU[buf][j] = a[j];
-        sm.rowU[buf][NB] = rb;
-        lr = K;
-      } else if (act && old == K) {
-        lr = p;
+      // every warp publishes its best key (-2: no candidate left in it)
+      if ((i & 31) == 0) {
+        sm.wkey[par][w] = key;
+        sm.widx[par][w] = idx;
       }
+      if (cand && lr == idx) put_row<T, NB>(sm.slot[par][w], a, rb, live);
       gsync<NB>();
-      const T piv = sm.rowU[buf][K];
-      if (!(fabs(piv) < eps) && act && lr > K) {
-        const T l = a[K] * (T(1) / piv);
-        a[K] = l;
+      p = sm.widx[par][0];
+      if constexpr (Warps<NB>::v > 1) {
+        T bk = sm.wkey[par][0];
 #pragma unroll
-        for (int j = K + 1; j < NB; j++) a[j] = fma(-sm.rowU[buf][j], l, a[j]);
-        rb = fma(-sm.rowU[buf][NB], l, rb);
-      }
-      LuStep<T, NB, K + 1>::run(a, rb, lr, n, i, act, sm, eps);
-    }
-  }
-};
-
-// Back substitution U x = z by logical row, one x_J broadcast per step (J
-// descending), the broadcast slot double-buffered so one barrier suffices.
-template <typename T, int NB, int J>
-struct BackStep {
-  static __device__ __forceinline__ void run(const T (&a)[NB], T &rb, T &xi,
-                                             int lr, int n, BatchSmem<T, NB> &sm) {
-    if constexpr (J >= 0) {
-      if (J < n) {
-        if (lr == J) {
-          xi = rb / a[J];
-          sm.bc2[J & 1] = xi;
+        for (int q = 1; q < Warps<NB>::v; q++) {
+          const T kq = sm.wkey[par][q];
+          const int iq = sm.widx[par][q];
+          if (kq > bk || (kq == bk && iq < p)) {
+            bk = kq;
+            p = iq;
+            pw = q;
+          }
         }
-        gsync<NB>();
-        if (lr < J) rb = fma(-a[J], sm.bc2[J & 1], rb);
       }
-      BackStep<T, NB, J - 1>::run(a, rb, xi, lr, n, sm);
+    } else {
+      // the pivot is logical row K itself
+      if (act && lr == K) put_row<T, NB>(sm.slot[par][0], a, rb, live);
+      gsync<NB>();
     }
+    const T *u = sm.slot[par][pw];
+    const T piv = u[3];
+    if (KIND == 1 && piv <= T(0)) return -1;  // NaN passes, as in mat_chol
+    const int old = lr;
+    const bool is_piv = act && old == p;
+    if (is_piv) {
+      lr = K;
+      dg = a[0];
+    } else if (act && old == K) {
+      lr = p;
+    }
+    // one code path for every row: the pivot row (and every row when the
+    // pivot is too small to eliminate with) shifts with multiplier 0, which
+    // leaves its entries unchanged (live entries are finite)
+    const bool elim = KIND == 1 || !(fabs(piv) < eps);
+    const T l = (act && elim && !is_piv) ? a[0] * (T(1) / piv) : T(0);
+    shift_update<T, NB>(a, rb, u, l, live - 1);
   }
-};
-
-template <typename T, int NB>
-__device__ void solve_lu(const T *__restrict__ A, int n, const T *__restrict__ b,
-                         T *__restrict__ x, BatchSmem<T, NB> &sm, int i, T eps) {
-  const bool act = i < n;
-  T a[NB];
-  T rb = act ? b[i] : T(0);
-#pragma unroll
-  for (int j = 0; j < NB; j++) a[j] = (act && j < n) ? A[i + (int64_t)j * n] : T(0);
-  int lr = i;
-  LuStep<T, NB, 0>::run(a, rb, lr, n, i, act, sm, eps);
-  T xi = T(0);
-  BackStep<T, NB, NB - 1>::run(a, rb, xi, act ? lr : NB, n, sm);
-  if (act) x[lr] = xi;
+  if (act && lr >= 0 && lr < n) x[lr] = rb / dg;  // lr < n by construction
+  return 0;
 }
 
-// Cholesky, column K: l_KK = sqrt(a_KK) (status -1 when a_KK <= 0, NaN
-// passes as in the reference), column K scaled by 1/l_KK, forward
-// substitution fused (y_K = b_K / l_KK), rank-1 update of the lower triangle
-// of the owned row with column K broadcast through shared memory.
+// Resident CTAs per SM asked of the register allocator for the two largest
+// buckets (the row itself takes NB registers): 3 x 128 and 4 x 96 threads.
 template <int NB>
-__host__ __device__ constexpr int col_off(int k) { return k * NB - k * (k - 1) / 2; }
-
-template <typename T, int NB, int K>
-struct CholStep {
-  static __device__ __forceinline__ void run(T (&a)[NB], T &rb, int n, int i,
-                                             bool act, BatchSmem<T, NB> &sm) {
-    if constexpr (K < NB) {
-      if (K >= n) return;
-      if (i == K) {
-        const T d = a[K];
-        if (d <= 0) sm.flag = 1;
-        const T lkk = sqrt(d);
-        a[K] = lkk;
-        rb = rb / lkk;
-        sm.bc = rb;
-        sm.Lc[col_off<NB>(K)] = lkk;
-      }
-      gsync<NB>();
-      if (sm.flag) return;
-      const T lkk = sm.Lc[col_off<NB>(K)];
-      const T yk = sm.bc;
-      if (i > K && act) {
-        const T l = a[K] * (T(1) / lkk);
-        a[K] = l;
-        sm.Lc[col_off<NB>(K) + (i - K)] = l;
-        rb = fma(-l, yk, rb);
-      }
-      gsync<NB>();
-      if (i > K && act) {
-        const T l = a[K];
-#pragma unroll
-        for (int j = K + 1; j < NB; j++)
-          if (j <= i) a[j] = fma(-l, sm.Lc[col_off<NB>(K) + (j - K)], a[j]);
-      }
-      CholStep<T, NB, K + 1>::run(a, rb, n, i, act, sm);
-    }
-  }
+struct MinCtas {
+  static constexpr int v = NB == 128 ? 3 : NB == 96 ? 4 : 1;
 };
 
-template <typename T, int NB, int J>
-struct CholBackStep {
-  static __device__ __forceinline__ void run(T &rb, T &xi, int n, int i,
-                                             BatchSmem<T, NB> &sm) {
-    if constexpr (J >= 0) {
-      if (J < n) {
-        if (i == J) {
-          xi = rb / sm.Lc[col_off<NB>(J)];
-          sm.bc = xi;
-        }
-        gsync<NB>();
-        const T xj = sm.bc;
-        // L^T(i, J) = L(J, i) = Lc[col_off(i) + J - i] for i < J
-        if (i < J) rb = fma(-sm.Lc[col_off<NB>(i) + (J - i)], xj, rb);
-        gsync<NB>();
-      }
-      CholBackStep<T, NB, J - 1>::run(rb, xi, n, i, sm);
-    }
-  }
-};
-
-template <typename T, int NB>
-__device__ void solve_chol(const T *__restrict__ A, int n, const T *__restrict__ b,
-                           T *__restrict__ x, BatchSmem<T, NB> &sm, int i,
-                           int32_t *status) {
-  const bool act = i < n;
-  T a[NB];
-  T rb = act ? b[i] : T(0);
-  // lower triangle of row i (mat_chol reads only the lower triangle)
-#pragma unroll
-  for (int j = 0; j < NB; j++)
-    a[j] = (act && j <= i) ? A[i + (int64_t)j * n] : T(0);
-  if (i == 0) sm.flag = 0;
-  gsync<NB>();
-  CholStep<T, NB, 0>::run(a, rb, n, i, act, sm);
-  if (sm.flag) {
-    if (i == 0) *status = -1;
-    return;
-  }
-  T xi = T(0);
-  CholBackStep<T, NB, NB - 1>::run(rb, xi, n, i, sm);
-  if (act) x[i] = xi;
-}
-
-// Persistent: every NB-thread group pulls systems of its bucket until the
-// queue is empty.  NB <= 32: several independent warp groups per CTA.
+// Persistent: every group pulls systems of its queue until it is empty.
 template <typename T, int NB, int GROUPS, int KIND>
-__global__ void __launch_bounds__(Tpg<NB>::v *GROUPS)
+__global__ void __launch_bounds__(Tpg<NB>::v *GROUPS, MinCtas<NB>::v)
     batched_kernel(int queue, const int32_t *__restrict__ list,
                    BatchQueues *q, const int32_t *__restrict__ nvec,
                    const int64_t *__restrict__ offA, const T *__restrict__ A,
@@ -268,16 +289,12 @@ __global__ void __launch_bounds__(Tpg<NB>::v *GROUPS)
     const int s = list[base + t];
     const int n = nvec[s];
     if (n < 1 || n > NB) continue;  // unsupported order: reported by the driver
-    if (i == 0) status[s] = 0;
-    if constexpr (KIND == 1)
-      solve_chol<T, NB>(A + offA[s], n, b + offv[s], x + offv[s], smem[g], i,
-                        status + s);
-    else
-      solve_lu<T, NB>(A + offA[s], n, b + offv[s], x + offv[s], smem[g], i, eps);
+    const int st = solve_one<T, NB, KIND>(A + offA[s], n, b + offv[s],
+                                          x + offv[s], smem[g], i, eps);
+    if (i == 0) status[s] = st;
     gsync<NB>();
   }
 }
-
 
 template <typename T, int NB, int GROUPS, int KIND>
 int launch_batched_queue(int queue, const int32_t *list, BatchQueues *q,
@@ -299,7 +316,7 @@ int launch_batched_queue(int queue, const int32_t *list, BatchQueues *q,
   const int grid = ctx()->sms * per_sm;
   static const char *names[2][5] = {
       {"batched_lu_16", "batched_lu_32", "batched_lu_64", "batched_lu_96", "batched_lu_128"},
-      {"batched_chol_16", "batched_chol_32", "batched_chol_64", "batched_chol_96", "batched_chol_128"}};
+      {"batched_spd_16", "batched_spd_32", "batched_spd_64", "batched_spd_96", "batched_spd_128"}};
   KtScope kt(names[KIND][NB <= 16 ? 0 : NB <= 32 ? 1 : NB <= 64 ? 2 : NB <= 96 ? 3 : 4], 0.0, 0.0);
   k<<<grid, threads, smem, ctx()->stream>>>(queue, list, q, n, offA, A, offv, b,
                                             x, status, eps);
@@ -308,7 +325,7 @@ int launch_batched_queue(int queue, const int32_t *list, BatchQueues *q,
 }
 
 // One entry point per (bucket, kind), each in its own translation unit
-// batched_nb<NB>_<lu|chol>.cu so the unrolled kernels compile in parallel.
+// batched_nb<NB>_<lu|chol>.cu so the kernels compile in parallel.
 #define MGB_BATCH_DECL(NB, KIND)                                               \
   int batched_bucket_##NB##_##KIND(int queue, const int32_t *list,             \
                                    BatchQueues *q, const int32_t *n,           \

@@ -109,13 +109,6 @@ __global__ void __launch_bounds__(256)
 }
 
 template <typename T>
-struct CholState {
-  static bool ready;
-};
-template <typename T>
-bool CholState<T>::ready = false;
-
-template <typename T>
 int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
@@ -123,19 +116,15 @@ int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
   if (n <= 0) return 0;
   if (lp >= 0 && sizeof(T) != 4)
     return set_error(MATGB_ERR_ARG, "tensor-core Cholesky is float");
-  // attribute and launch go through the same function pointer
+  const int NB = lp >= 0 ? kCholBlockLp : kCholBlock;
+  // the shared-memory opt-in is set on every call (a host-side attribute
+  // write), through the same function pointers the launches use
   auto kdiag = potrf_diag_kernel<T>;
   auto ktrsm = chol_trsm_kernel<T>;
-  if (!CholState<T>::ready) {
-    MGB_CUDA(cudaFuncSetAttribute(kdiag,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)diag_smem<T>(kCholBlockLp)));
-    MGB_CUDA(cudaFuncSetAttribute(ktrsm,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)ctrsm_smem<T>(kCholBlockLp)));
-    CholState<T>::ready = true;
-  }
-  const int NB = lp >= 0 ? kCholBlockLp : kCholBlock;
+  MGB_CUDA(cudaFuncSetAttribute(kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)diag_smem<T>(NB)));
+  MGB_CUDA(cudaFuncSetAttribute(ktrsm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ctrsm_smem<T>(NB)));
   for (int64_t kb = 0; kb < n; kb += NB) {
     const int nb = (int)((n - kb) < NB ? (n - kb) : NB);
     T *A11 = A + kb + kb * lda;
@@ -143,7 +132,7 @@ int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
       KtScope kt("potrf_diag", nb * (double)nb * nb / 3.0,
                  (double)nb * nb * sizeof(T));
       kdiag<<<1, 256, diag_smem<T>(nb), cx->stream>>>(nb, A11, lda, info, kb);
-      MGB_LAUNCHED("potrf_diag");
+      MGB_TRY(launch_check((const void *)kdiag, "potrf_diag", diag_smem<T>(nb)));
     }
     const int64_t m = n - kb - nb;
     if (m > 0) {
@@ -153,7 +142,7 @@ int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
                     2.0 * m * nb * sizeof(T));
         ktrsm<<<(unsigned)((m + 31) / 32), 256, ctrsm_smem<T>(nb), cx->stream>>>(
             nb, A11, A21, lda, m, info);
-        MGB_LAUNCHED("chol_trsm");
+        MGB_TRY(launch_check((const void *)ktrsm, "chol_trsm", ctrsm_smem<T>(nb)));
       }
       T *A22 = A + (kb + nb) + (kb + nb) * lda;
       if (lp < 0)

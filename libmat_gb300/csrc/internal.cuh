@@ -30,6 +30,7 @@ Ctx *ctx();
 int set_error(int code, const char *fmt, ...);
 // Record a CUDA failure with its call site.
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+int launch_check(const void *func, const char *name, size_t smem);
 // For the void mat_* entry points: report and abort unless disabled.
 void fail_void(const char *where);
 
@@ -49,7 +50,7 @@ struct KtScope {
 // counterpart of the reference's scratch arena, mat.h:865-895).
 enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
-  WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_NSLOTS
+  WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_NSLOTS
 };
 void *ws(int slot, size_t bytes);
 
@@ -139,6 +140,15 @@ template <typename T>
 int potrs_t(int64_t n, int64_t nrhs, const T *L, int64_t lda, T *B,
             int64_t ldb, const int32_t *info);
 int tc_error_flag(int clear);
+// Flexible GMRES for the refinement correction (krylov.cu): solves A d = r0
+// with r0 in V(:, 0) on entry; V holds m + 1 and Z m vectors of length n, F
+// 2n floats; stops when the residual estimate is <= max(rtol*|r0|, atol).
+constexpr int kKrylovMaxDim = 64;
+constexpr int kKrylovMaxParts = 64;
+int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
+                 const float *W, const int32_t *perm, elem_t *V, elem_t *Z,
+                 float *F, int m, double rtol, double atol, elem_t *d,
+                 int *inner, double *res_est);
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm);
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,
           const int32_t *perm, const elem_t *B, int64_t ldb, elem_t *X,

@@ -22,6 +22,8 @@
 
 #include "internal.cuh"
 
+#include <algorithm>
+
 namespace mgb {
 
 // ---- packing the trailing-update operands -------------------------------------
@@ -269,6 +271,15 @@ __global__ void copy_cols_kernel(int64_t n, int64_t nrhs, const S *__restrict__ 
     R[(e % n) + (e / n) * ldr] = B[(e % n) + (e / n) * ldb];
 }
 
+// X += D (element type)
+template <typename S>
+__global__ void add_vec_kernel(int64_t n, S *__restrict__ X,
+                               const S *__restrict__ D) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    X[i] = X[i] + D[i];
+}
+
 // Reduced doubles (stored as bit patterns) to the host.
 static int fetch(const unsigned long long *d, double *v, int count) {
   MGB_CUDA(cudaMemcpyAsync(v, d, count * sizeof(double), cudaMemcpyDeviceToHost,
@@ -330,11 +341,15 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   const double eps = sizeof(elem_t) == 8 ? 1.1102230246251565e-16
                                          : 5.960464477539063e-08;
   const double tol = o.tol > 0 ? o.tol : (double)n * eps;
-  const int maxit = o.max_iter > 0 ? o.max_iter : 30;
+  const int maxit = o.max_iter > 0 ? o.max_iter : 100;
 
   int lp = o.lp_format;
   double eta = INFINITY, rn = 0, xn = 0;
-  int it = 0, converged = 0;
+  int it = 0, converged = 0, refinements = 0, ksteps = 0;
+  const bool use_krylov = o.krylov != 0 && nrhs == 1;
+  const int kdim = o.krylov_dim > 0 ? (o.krylov_dim < kKrylovMaxDim ? o.krylov_dim
+                                                                    : kKrylovMaxDim)
+                                    : 40;
   float ms_factor = 0.f;
   for (int attempt = 0; attempt < 2; attempt++) {
     MGB_CUDA(cudaEventRecord(g_ir.e[0], st));
@@ -368,7 +383,53 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
     for (int64_t c = 0; c < nrhs; c++)
       MGB_CUDA(cudaMemsetAsync(X + c * ldx, 0, (size_t)n * sizeof(elem_t), st));
     double prev = INFINITY;
-    while (it < maxit) {
+    if (use_krylov) {
+      // FGMRES cycles on the correction equation, residual in V(:, 0)
+      elem_t *V = (elem_t *)ws(WS_KV, (size_t)(2 * kdim + 2) * n * sizeof(elem_t));
+      if (!V) return MATGB_ERR_NOMEM;
+      elem_t *Z = V + (size_t)(kdim + 1) * n;
+      elem_t *D = Z + (size_t)kdim * n;
+      MGB_CUDA(cudaMemcpyAsync(V, R, (size_t)n * sizeof(elem_t),
+                               cudaMemcpyDeviceToDevice, st));
+      double xn_known = 0;
+      while (it < maxit) {
+        int inner = 0;
+        double est = 0;
+        const int mcap = (int)std::min<int64_t>(kdim, maxit - it);
+        // first cycle: ten orders of reduction; later ones: the absolute
+        // residual that meets the backward-error target with room to spare
+        const double atol =
+            refinements == 0 ? 0.0 : 0.25 * tol * (anorm * xn_known + bn[0]);
+        MGB_TRY(fgmres_cycle(spd, n, A, lda, W, piv + n, V, Z, RF, mcap, 1e-10,
+                             atol, D, &inner, &est));
+        it += inner;
+        ksteps += inner;
+        add_vec_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, X, D);
+        MGB_LAUNCHED("add_vec");
+        refinements++;
+        // true residual in the element type
+        MGB_CUDA(cudaMemcpyAsync(V, B, (size_t)n * sizeof(elem_t),
+                                 cudaMemcpyDeviceToDevice, st));
+        MGB_TRY(gemv_t<elem_t>(n, n, elem_t(-1), A, lda, X, elem_t(1), V));
+        MGB_CUDA(cudaMemsetAsync(rs, 0, 2 * sizeof(unsigned long long), st));
+        col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, V, n, X, ldx, rs);
+        MGB_LAUNCHED("col_amax");
+        MGB_TRY(fetch(rs, hv.data(), 2));
+        rn = hv[0];
+        xn = hv[1];
+        xn_known = xn;
+        const double den = anorm * xn + bn[0];
+        eta = (den > 0) ? rn / den : (rn == 0 ? 0.0 : INFINITY);
+        if (rn != rn || den != den) eta = NAN;
+        if (eta <= tol) {
+          converged = 1;
+          break;
+        }
+        if (!(eta < 0.5 * prev)) break;  // stagnation or divergence
+        prev = eta;
+      }
+    }
+    while (!use_krylov && it < maxit) {
       // correction D = (LU)^{-1} R in FP32, column-scaled (first pass: plain)
       MGB_CUDA(cudaMemsetAsync(rs, 0, (size_t)2 * nrhs * sizeof(unsigned long long), st));
       col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, R, n, R, n, rs);
@@ -385,6 +446,7 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
       update_x_kernel<elem_t><<<cg, 256, 0, st>>>(n, X, ldx, DF, rs);
       MGB_LAUNCHED("update_x");
       it++;
+      refinements++;
       // residual R = B - A X in the refinement precision
       copy_cols_kernel<elem_t><<<gnn, 256, 0, st>>>(n, nrhs, B, ldb, R, n);
       MGB_LAUNCHED("copy_cols");
@@ -441,6 +503,8 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
     rep->ms_factor = ms_factor;
     rep->ms_refine = t;
     rep->lp_format = lp;
+    rep->refinements = refinements;
+    rep->krylov_steps = ksteps;
   }
   return 0;
 }
@@ -458,9 +522,11 @@ extern "C" {
 
 void matgb_ir_default_opts(MatIROpts *o) {
   o->lp_format = 1;
-  o->max_iter = 30;
+  o->max_iter = 100;
   o->tol = 0.0;
   o->fp32_fallback = 1;
+  o->krylov = 1;
+  o->krylov_dim = 40;
 }
 
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,

@@ -69,6 +69,22 @@ void fail_void(const char *where) {
   if (g_abort_on_error) abort();
 }
 
+// As launched(), and on failure the message carries the kernel's registered
+// limits next to the dynamic shared memory the launch asked for.
+int launch_check(const void *func, const char *name, size_t smem) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return 0;
+  cudaFuncAttributes fa{};
+  cudaError_t e2 = cudaFuncGetAttributes(&fa, func);
+  cudaGetLastError();
+  return set_error(MATGB_ERR_CUDA,
+                   "launch of %s failed: %s (dynamic smem asked %zu, kernel max "
+                   "dynamic %d, static %zu, regs %d, attr query %s)",
+                   name, cudaGetErrorString(e), smem, fa.maxDynamicSharedSizeBytes,
+                   fa.sharedSizeBytes, fa.numRegs, cudaGetErrorString(e2));
+}
+
 int launched(const char *name) {
   g_launches.fetch_add(1, std::memory_order_relaxed);
   cudaError_t e = cudaGetLastError();

@@ -154,18 +154,24 @@ def conditioned(n, kappa, seed):
     return np.asfortranarray((U * s) @ V.T)
 
 
-# kappa * u_16 < 1 (BF16 u = 2^-8, FP16 u = 2^-11): the 16-bit factors refine
-# to FP64 accuracy on their own; beyond it the FP32 refactorisation takes over.
-@pytest.mark.parametrize("lp,n,kappa,final_lp", [
-    (1, 512, 1e2, 1), (0, 512, 1e2, 0), (1, 1024, 1e2, 1), (0, 1024, 1e2, 0),
-    (0, 1000, 1e3, 0), (1, 1000, 1e4, -1), (0, 1000, 1e6, -1),
-    (-1, 700, 1e6, -1)])
-def test_ir_f64_reaches_fp64_backward_error(gpu, lp, n, kappa, final_lp):
+# Classic refinement (krylov=0): kappa * u_16 < 1 (BF16 u = 2^-8, FP16
+# u = 2^-11) refines the 16-bit factors to FP64 accuracy on their own, beyond
+# it the FP32 refactorisation takes over.  FGMRES refinement (krylov=1) keeps
+# the 16-bit factors up to kappa = 1e6.
+@pytest.mark.parametrize("krylov,lp,n,kappa,final_lp", [
+    (0, 1, 512, 1e2, 1), (0, 0, 512, 1e2, 0), (0, 1, 1024, 1e2, 1),
+    (0, 0, 1024, 1e2, 0), (0, 0, 1000, 1e3, 0), (0, 1, 1000, 1e4, -1),
+    (0, 0, 1000, 1e6, -1), (0, -1, 700, 1e6, -1),
+    (1, 1, 512, 1e2, 1), (1, 0, 1024, 1e2, 0), (1, 1, 1000, 1e4, 1),
+    (1, 0, 1000, 1e4, 0), (1, 1, 1000, 1e6, 1), (1, 0, 1200, 1e6, 0),
+    (1, -1, 700, 1e6, -1)])
+def test_ir_f64_reaches_fp64_backward_error(gpu, krylov, lp, n, kappa, final_lp):
     L = gpu["f64"]
     A = conditioned(n, kappa, 7 + n)
     b = np.random.default_rng(n).standard_normal(n)
-    x, rep = L.mat_solve_ir(A, b, lp_format=lp)
+    x, rep = L.mat_solve_ir(A, b, lp_format=lp, krylov=krylov)
     assert rep["converged"] == 1 and rep["lp_format"] == final_lp, rep
+    assert (rep["krylov_steps"] > 0) == (krylov == 1), rep
     eta = np.abs(b - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
                                      + np.abs(b).max())
     assert eta <= n * 2.0 ** -53, (eta, rep)
@@ -214,6 +220,23 @@ def test_spd_ir_reaches_fp64_backward_error(gpu, lp, n, lam, final_lp):
         eta = np.abs(b - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
                                          + np.abs(b).max())
         assert eta <= n * 2.0 ** -53, (c, eta)
+
+
+@pytest.mark.parametrize("lp,lam", [(1, 1e3), (1, 1e6), (0, 1e6)])
+def test_spd_ir_single_rhs_fgmres(gpu, lp, lam):
+    """One right-hand side: FGMRES on the Cholesky-preconditioned correction
+    keeps the 16-bit factors where classic refinement would fall back."""
+    L = gpu["f64"]
+    n = 800
+    A = spd_conditioned(n, lam, 91)
+    b = np.random.default_rng(3).standard_normal((n, 1))
+    X, ret, rep = L.mat_solve_spd_ir(A, b, lp_format=lp)
+    assert ret == 0 and rep["converged"] == 1 and rep["lp_format"] == lp, rep
+    assert rep["krylov_steps"] > 0
+    x = X[:, 0]
+    eta = np.abs(b[:, 0] - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
+                                           + np.abs(b).max())
+    assert eta <= n * 2.0 ** -53, eta
 
 
 def test_spd_ir_not_spd_returns_minus_one(gpu):
