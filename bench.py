@@ -1,18 +1,41 @@
 """Benchmark of libmatgb's dense-solve hot path on one GB300.
 
-Default workload (plain_lu_solve_8192_f32): PLU of an 8192x8192 float32
-matrix with i.i.d. N(0,1) entries plus the 16-right-hand-side solve (the
-large plain config).  One step = factor a fresh copy of A (pre-staged in
-HBM, 256 MiB, larger than the 129 MB L2, so no flush is needed) and solve
-16 columns.  Work per step (HPL convention, the reference's PLU formula
-tests/bench/compare/bench_plu.cpp:74-75 plus 2n^2 per right-hand side):
-2n^3/3 + 16*2n^2 FLOP.
+Headline workload (mixed_lu_ir_16384_f64): mat_solve's LU solve of an
+n = 16384 double-precision system A x = b, 1 right-hand side N(0,1), with
+A = U diag(sigma) V^T, U and V the Q factors of Householder QR of seeded
+Gaussian matrices and sigma geometrically spaced to condition numbers 1e2,
+1e4 and 1e6 (one matrix per condition number, all resident in HBM: 2 GiB
+each, larger than the 129 MB L2).  The solver factors in FP32 with the
+trailing updates on the tensor cores (FP16 operands with power-of-two
+block scales, each split into hi + remainder and multiplied as three
+products, FP32 accumulation) and
+refines in FP64 on the GPU (FGMRES preconditioned by the factors) until the
+backward error |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf) <= n * 2^-53.
+One step = one complete solve of one of the three systems (the steps cycle
+through the condition numbers); work per step is the HPL count of the
+reference's PLU formula (tests/bench/compare/bench_plu.cpp:74-75) plus the
+solve, 2n^3/3 + 2n^2 FLOP.  Every step's backward error is checked.
+
+Reported beside it: the plain FP64 GPU LU solve of the same system (the
+baseline the mixed solver must beat by 3x), the tensor-core rank-K update's
+roofline (achieved TFLOP/s over the measured BF16 peak), an end-to-end figure
+through mat_solve_ir with pinned host buffers, the reference's algorithm on
+one host core (oracle port, f64, at reduced n), and secondary workloads: the
+plain float32 GEMM and PLU solve at 8192, the SPD solve at 16384 with 64
+right-hand sides, and 100,000 batched uneven solves.
+
+Data: the matrices are generated on the GPU with PyTorch (QR in float32,
+product in float64 -- the orthogonal factors are exact to ~1e-6, so the
+condition numbers hold to that relative accuracy); PyTorch is only the
+harness here, the solves run in libmatgb.  Torch tensors are row-major, so
+the library (column-major) sees A^T, which has the same singular values.
 
 Prints ONE JSON line.  --impl reference times the reference's algorithm on
 the host cores instead (the oracle port: the reference's own source is not
 present where this runs), on a bounded sample of the same workload.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import shutil
@@ -27,16 +50,21 @@ sys.path.insert(0, ROOT)
 
 METRIC = ("LU/Chol solve TFLOP/s at bwd err <= n*eps64 (mixed+IR vs plain); "
           "batched solves/s")
+KAPPAS = (1e2, 1e4, 1e6)
 
 
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
-            d = json.load(f)
-        return d, "measured"
+            return json.load(f), "measured"
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0,
             "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def out_path(name):
+    d = os.path.join(ROOT, "gpurun_out")
+    return os.path.join(d, name) if os.path.isdir(d) else os.path.join("/tmp", name)
 
 
 class Clocks:
@@ -56,6 +84,7 @@ class Clocks:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
         return self
 
     def __exit__(self, *a):
@@ -87,72 +116,264 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def cpu_plain_sample(n=2048, nrhs=16, budget_s=12.0):
-    """The reference's PLU + per-column triangular solves (oracle port, one
-    core) on an n x n sample of the same distribution.  Returns TFLOP/s."""
-    from oracle.loader import Oracle
-    from libmat_gb300 import rng
-    O = Oracle("f32", "port")
-    A = rng.normal(1001, (n, n), np.float32)
-    B = rng.normal(2001, (n, nrhs), np.float32)
-    flops = 2 * n ** 3 / 3 + nrhs * 2 * n * n
-    reps, t0 = 0, time.perf_counter()
+def ktable(L):
+    """Per-kernel event timing collected by the library (name, launches, ms,
+    algorithmic flop, algorithmic bytes)."""
+    res, i = [], 0
+    names = (C.c_char * 64)()
     while True:
-        L, U, p, _ = O.plu(A)
-        for c in range(nrhs):
-            z = O.solve_tril_unit(L, B[p, c])
-            O.solve_triu(U, z)
-        reps += 1
-        el = time.perf_counter() - t0
-        if el > budget_s or reps >= 50:
+        cnt, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+        if L.c.matgb_ktime_get(i, names, 64, C.byref(cnt), C.byref(ms),
+                               C.byref(fl), C.byref(by)) != 0:
             break
-    return flops * reps / el / 1e12, el / reps, n
+        res.append((names.value.decode(), cnt.value, ms.value, fl.value, by.value))
+        i += 1
+    return sorted(res, key=lambda r: -r[2])
 
 
-def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    n = 2048
-    tf, per, _ = 0.0, 0.0, n
-    for _ in range(args.warmup):
-        cpu_plain_sample(n, budget_s=0.0)
-    vals = []
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        v, per, _ = cpu_plain_sample(n, budget_s=0.0)
-        vals.append(v)
-    el = time.perf_counter() - t0
-    tf = float(np.median(vals))
-    line = {
-        "impl": "reference", "metric": METRIC, "value": tf, "unit": "TFLOP/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": "plain_lu_solve_8192_f32",
-                   "sample": f"PLU + 16-RHS solve at n={n} (bounded sample)"},
-        "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": 1,
-                         "kind": "port",
-                         "sample": f"n={n} f32 N(0,1), 16 RHS, 1 thread"},
-        "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
+# ----------------------------------------------------------------- data
+def conditioned_set(n, kappas, seed):
+    """A_kappa = U diag(sigma_kappa) V^T on the GPU (torch, float64)."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    U, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float32,
+                                       generator=g))
+    V, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float32,
+                                       generator=g))
+    U = U.double()
+    V = V.double()
+    mats = {}
+    for k in kappas:
+        sig = k ** (-torch.arange(n, device="cuda", dtype=torch.float64) / (n - 1))
+        mats[k] = (U * sig) @ V.T
+    b = torch.randn(n, device="cuda", dtype=torch.float64, generator=g)
+    del U, V
+    torch.cuda.synchronize()
+    return mats, b
+
+
+def spd_set(n, lam_maxes, nrhs, seed):
+    """A = Q diag(lambda) Q^T, lambda log-uniform in [1, lam_max]."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    Q, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float32,
+                                       generator=g))
+    Q = Q.double()
+    mats = {}
+    for lm in lam_maxes:
+        u = torch.rand(n, device="cuda", dtype=torch.float64, generator=g)
+        lam = torch.exp(u * np.log(lm))
+        A = (Q * lam) @ Q.T
+        mats[lm] = (A + A.T) * 0.5
+    B = torch.randn(nrhs, n, device="cuda", dtype=torch.float64, generator=g)
+    del Q
+    torch.cuda.synchronize()
+    return mats, B  # B row-major nrhs x n == column-major n x nrhs
+
+
+def bwd_err_T(A, x, b):
+    """Backward error of the system the library solved (A^T x = b)."""
+    r = (b - A.T @ x).abs().max().item()
+    return r / (A.abs().sum(0).max().item() * x.abs().max().item()
+                + b.abs().max().item())
+
+
+# ----------------------------------------------------------------- headline
+def run_headline(args, mg):
+    import torch
+    L = mg.load("f64")
+    n = args.n
+    flops = 2 * n ** 3 / 3 + 2 * n * n
+    tol = n * 2.0 ** -53
+    t0 = time.time()
+    mats, b = conditioned_set(n, KAPPAS, 1234)
+    gen_s = time.time() - t0
+    x = torch.zeros(n, device="cuda", dtype=torch.float64)
+    opts = L.ir_opts(lp_format=args.lp)
+    rep = mg.MatIRReport()
+    seq = [KAPPAS[i % len(KAPPAS)] for i in range(args.steps)]
+
+    def solve(k):
+        rc = L.c.matgb_gesv_ir_dev(n, mats[k].data_ptr(), n, b.data_ptr(),
+                                   x.data_ptr(), C.byref(opts), C.byref(rep))
+        L.check(rc, "gesv_ir")
+        return rep.as_dict()
+
+    for i in range(args.warmup):
+        solve(KAPPAS[i % len(KAPPAS)])
+    L.sync()
+    l0 = L.c.matgb_launch_count()
+    reps = []
+    with Clocks(out_path("bench_clocks.csv")) as clk:
+        t_wall = time.perf_counter()
+        L.check(L.c.matgb_event_record(0), "ev")
+        for k in seq:
+            reps.append(solve(k))
+        L.check(L.c.matgb_event_record(1), "ev")
+        L.sync()
+        t_wall = time.perf_counter() - t_wall
+        ms = L.c.matgb_event_elapsed_ms(0, 1)
+    launches = int(L.c.matgb_launch_count() - l0)
+    ms_step = ms / len(seq)
+    value = flops / (ms_step * 1e-3) / 1e12
+    per_kappa = {}
+    for k, r in zip(seq, reps):
+        d = per_kappa.setdefault("%g" % k, {"steps": 0, "ms": [], "converged": 1,
+                                            "bwd_err_max": 0.0})
+        d["steps"] += 1
+        d["ms"].append(r["ms_factor"] + r["ms_refine"])
+        d["converged"] &= r["converged"]
+        d["bwd_err_max"] = max(d["bwd_err_max"], r["backward_error"])
+        d["lp_format"] = r["lp_format"]
+        d["krylov_steps"] = r["krylov_steps"]
+        d["refinements"] = r["refinements"]
+        d["ms_factor"] = r["ms_factor"]
+        d["ms_refine"] = r["ms_refine"]
+    for d in per_kappa.values():
+        d["ms"] = float(np.mean(d["ms"]))
+    # independent check of the last solve of each condition number
+    for k in KAPPAS:
+        solve(k)
+        L.sync()
+        per_kappa["%g" % k]["bwd_err_check"] = bwd_err_T(mats[k], x, b)
+    all_ok = all(d["converged"] == 1 and d["bwd_err_max"] <= tol
+                 for d in per_kappa.values())
+
+    # per-kernel timing over one solve per condition number
+    L.c.matgb_ktime_enable(1)
+    for k in KAPPAS:
+        solve(k)
+    L.sync()
+    kt = ktable(L)
+    L.c.matgb_ktime_enable(0)
+    rl = tc_roofline(kt)
+
+    # plain FP64 GPU LU + solve of the kappa = 1e4 system (same API family)
+    A = mats[1e4]
+    Aw = torch.empty_like(A)
+    piv = torch.empty(2 * n, device="cuda", dtype=torch.int32)
+    xp = torch.empty_like(b)
+    small = torch.randn(512, 512, device="cuda", dtype=torch.float64)
+    L.check(L.c.matgb_getrf_dev(512, small.data_ptr(), 512, piv.data_ptr(),
+                                piv.data_ptr() + 4 * n), "getrf warm")
+    Aw.copy_(A)
+    torch.cuda.synchronize()
+    L.sync()
+    L.check(L.c.matgb_event_record(2), "ev")
+    L.check(L.c.matgb_getrf_dev(n, Aw.data_ptr(), n, piv.data_ptr(),
+                                piv.data_ptr() + 4 * n), "getrf")
+    L.check(L.c.matgb_getrs_dev(n, 1, Aw.data_ptr(), n, piv.data_ptr() + 4 * n,
+                                b.data_ptr(), n, xp.data_ptr(), n), "getrs")
+    L.check(L.c.matgb_event_record(3), "ev")
+    L.sync()
+    ms_plain = L.c.matgb_event_elapsed_ms(2, 3)
+    plain = {"ms": ms_plain, "tflops": flops / (ms_plain * 1e-3) / 1e12,
+             "bwd_err": bwd_err_T(A, xp, b), "kappa": 1e4,
+             "api": "matgb_getrf_dev + matgb_getrs_dev (f64)",
+             "speedup_of_mixed": {kk: ms_plain / d["ms"]
+                                  for kk, d in per_kappa.items()}}
+    del Aw, xp
+
+    # end to end through mat_solve_ir with pinned host buffers (kappa = 1e4)
+    e2e = e2e_mixed(L, mg, A, b, flops, opts, max(1, min(args.steps, 3)))
+    for k in list(mats):
+        del mats[k]
+    torch.cuda.empty_cache()
+    return {
+        "value": value, "unit": "TFLOP/s", "ms_per_step": ms_step,
+        "wall_ms_per_step": t_wall * 1e3 / len(seq),
+        "dtype": "f64 (FP32 factors, FP16 tensor-core updates, FP32 accumulate)",
+        "gpu_launches": launches,
+        "config": {"workload": "mixed_lu_ir_16384_f64", "n": n, "nrhs": 1,
+                   "kappas": list(KAPPAS), "factor_format": {2: "fp16 split (hi+lo, 3 products)", 1: "bf16",
+                                     0: "fp16", -1: "fp32 simt"}[args.lp],
+                   "refinement": "FGMRES (FP64) preconditioned by the factors",
+                   "A": "U diag(sigma) V^T, U,V from QR of seeded N(0,1)",
+                   "target_bwd_err": tol, "gen_s": round(gen_s, 1),
+                   "l2": "inputs larger than L2 (2 GiB per A, 3 resident)"},
+        "all_converged_to_target": all_ok, "per_kappa": per_kappa,
+        "plain_fp64": plain, "roofline": rl, "e2e": e2e,
+        "clocks": clk.summary(), "kernels": [
+            {"name": r[0], "launches": r[1], "ms": round(r[2], 3)} for r in kt[:12]],
     }
-    print(json.dumps(line), flush=True)
 
 
-def run_plain(args, mg):
+def tc_roofline(kt):
+    """Roofline of the tensor-core trailing update: a rank-128 update reads and
+    writes its FP32 C tile once for 2*128 (x3 split) flops per element, so it
+    is bound by HBM unless the tensor fraction is the larger one; both are
+    given, the binding one is the headline."""
+    pk, src = peaks()
+    tot = sum(r[2] for r in kt) or 1.0
+    tc = [r for r in kt if r[0].startswith("tc_gemm")]
+    if not tc:
+        return None
+    name, cnt, ms, fl, by = tc[0]
+    tflops = fl / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
+    gbs = by / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    tpk = pk.get("bf16_tflops_sustained") or pk.get("bf16_tflops")
+    hpk = pk["hbm_gbs"]
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "tc_gemm_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+    hbm = {"achieved": gbs, "peak": hpk, "unit": "GB/s", "frac": gbs / hpk}
+    ten = {"achieved": tflops, "peak": tpk, "unit": "TFLOP/s",
+           "frac": tflops / tpk if tpk else None}
+    bound = "hbm" if hbm["frac"] >= (ten["frac"] or 0) else "tensor"
+    head = hbm if bound == "hbm" else ten
+    return {"kernel": name, "bound": bound, "launches": cnt, "share": ms / tot,
+            "achieved": head["achieved"], "peak": head["peak"],
+            "unit": head["unit"], "frac": head["frac"], "traffic": traffic,
+            "algorithmic_bytes_per_launch": by / cnt if cnt else None,
+            "hbm": hbm, "tensor": ten,
+            "peak_source": f"{src} peaks: hbm_gbs, bf16_tflops_sustained "
+                           "(kernel timed inside a long step)"}
+
+
+def e2e_mixed(L, mg, A, b, flops, opts, ke):
+    import torch
+    n = A.shape[0]
+    es = 8
+    hA = L.c.matgb_host_alloc(n * n * es)
+    hb = L.c.matgb_host_alloc(n * es)
+    hx = L.c.matgb_host_alloc(n * es)
+    torch.cuda.synchronize()
+    L.check(L.c.matgb_memcpy_d2h(hA, A.data_ptr(), n * n * es), "d2h")
+    L.check(L.c.matgb_memcpy_d2h(hb, b.data_ptr(), n * es), "d2h")
+    L.sync()
+    MA = mg.MatStruct(n, n, hA)
+    MB = mg.MatStruct(n, 1, hb)
+    MX = mg.MatStruct(n, 1, hx)
+    rep = mg.MatIRReport()
+    L.check(L.c.mat_solve_ir(C.byref(MX), C.byref(MA), C.byref(MB),
+                             C.byref(opts), C.byref(rep)), "mat_solve_ir")
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        L.check(L.c.mat_solve_ir(C.byref(MX), C.byref(MA), C.byref(MB),
+                                 C.byref(opts), C.byref(rep)), "mat_solve_ir")
+    ms = (time.perf_counter() - t0) / ke * 1e3
+    ok = rep.converged
+    for p in (hA, hb, hx):
+        L.c.matgb_host_free(p)
+    return {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+            "h2d_bytes_per_step": n * n * es + n * es, "d2h_bytes_per_step": n * es,
+            "ms_per_step": ms, "converged": int(ok),
+            "api": "mat_solve_ir (host Mat/Vec, pinned), kappa = 1e4"}
+
+
+# ----------------------------------------------------------------- secondary
+def run_plain_f32(mg, steps=3, warmup=3):
+    """Plain float32 PLU + 16-RHS solve at 8192 and the 8192^3 GEMM."""
     L = mg.load("f32")
     c = L.c
-    n, nrhs = args.n, 16
-    es = 4
-    K, W = args.steps, args.warmup
-    flops = 2 * n ** 3 / 3 + nrhs * 2 * n * n
+    n, nrhs, es = 8192, 16, 4
     nA = n * n * es
-    # device buffers: a pristine A, one working copy per timed step, B, X, piv
-    copies = K + 1
     dA0 = L.dalloc(nA)
-    dAs = [L.dalloc(nA) for _ in range(copies)]
+    dAs = [L.dalloc(nA) for _ in range(steps)]
     dB = L.dalloc(n * nrhs * es)
     dX = L.dalloc(n * nrhs * es)
     dpiv = L.dalloc(2 * n * 4)
@@ -164,172 +385,316 @@ def run_plain(args, mg):
         L.check(c.matgb_getrs_dev(n, nrhs, dA, n, dpiv + n * 4, dB, n, dX, n),
                 "getrs")
 
-    for i in range(W):
+    for _ in range(warmup):
         L.check(c.matgb_memcpy_d2d(dAs[0], dA0, nA), "d2d")
         step(dAs[0])
-    for d in dAs[:K]:
+    for d in dAs:
         L.check(c.matgb_memcpy_d2d(d, dA0, nA), "d2d")
     L.sync()
-    l0 = L.launches()
-    clk = Clocks(os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
-                 if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else
-                 "/tmp/bench_clocks.csv")
-    with clk:
-        time.sleep(0.3)
-        L.check(c.matgb_event_record(0), "ev")
-        for k in range(K):
-            step(dAs[k])
-        L.check(c.matgb_event_record(1), "ev")
-        ms = c.matgb_event_elapsed_ms(0, 1)
-    launches = L.launches() - l0
-    ms_step = ms / K
-    value = flops / (ms_step * 1e-3) / 1e12
-
-    # parity spot check at full size: backward error of the 16 solves
+    L.check(c.matgb_event_record(0), "ev")
+    for d in dAs:
+        step(d)
+    L.check(c.matgb_event_record(1), "ev")
+    L.sync()
+    ms = c.matgb_event_elapsed_ms(0, 1) / steps
+    flops = 2 * n ** 3 / 3 + nrhs * 2 * n * n
     A = np.empty((n, n), np.float32, order="F")
-    L.d2h(A, dA0)
     B = np.empty((n, nrhs), np.float32, order="F")
     X = np.empty((n, nrhs), np.float32, order="F")
+    L.d2h(A, dA0)
     L.d2h(B, dB)
     L.d2h(X, dX)
     A64 = A.astype(np.float64)
-    R = B.astype(np.float64) - A64 @ X.astype(np.float64)
-    eta = float((np.abs(R).max(0) / (np.abs(A64).sum(1).max() *
-                                     np.abs(X).max(0) + np.abs(B).max(0))).max())
-
-    # roofline of the dominant kernel (the trailing-update GEMM) from the
-    # library's per-kernel event timing over one more step
-    rl = kernel_roofline(L, lambda: step(dAs[K]), dA0, nA, dAs[K])
-
-    # end to end through the public API with host (pinned) buffers
-    hA = c.matgb_host_alloc(nA)
-    hB = c.matgb_host_alloc(n * nrhs * es)
-    hX = c.matgb_host_alloc(n * nrhs * es)
-    c.matgb_memcpy_d2h(hA, dA0, nA)
-    c.matgb_memcpy_d2h(hB, dB, n * nrhs * es)
+    R = B - A64 @ X
+    eta = float((np.abs(R).max(0) / (np.abs(A64).sum(1).max() * np.abs(X).max(0)
+                                     + np.abs(B).max(0))).max())
+    # GEMM 8192^3 (C = A A, fresh output each time; inputs larger than L2)
+    dC = dAs[0]
+    for _ in range(warmup):
+        L.check(c.matgb_gemm_dev(b"N", b"N", n, n, n, 1.0, dA0, n, dA0, n, 0.0,
+                                 dC, n), "gemm")
     L.sync()
-    import ctypes as C
-    MA = mg.MatStruct(n, n, hA)
-    MB = mg.MatStruct(n, nrhs, hB)
-    MX = mg.MatStruct(n, nrhs, hX)
-    c.matgb_solve_multi(C.byref(MX), C.byref(MA), C.byref(MB))
-    L.check(0, "e2e warmup")
-    ke = max(1, min(K, 5))
-    L.check(c.matgb_event_record(2), "ev")
-    t0 = time.perf_counter()
-    for _ in range(ke):
-        c.matgb_solve_multi(C.byref(MX), C.byref(MA), C.byref(MB))
-    L.check(c.matgb_event_record(3), "ev")
-    ms_e2e = c.matgb_event_elapsed_ms(2, 3) / ke
-    wall_e2e = (time.perf_counter() - t0) / ke * 1e3
-    L.check(0, "e2e")
-    e2e = {"value": flops / (max(ms_e2e, wall_e2e) * 1e-3) / 1e12,
-           "unit": "TFLOP/s", "h2d_bytes_per_step": nA + n * nrhs * es,
-           "d2h_bytes_per_step": n * nrhs * es, "ms_per_step": max(ms_e2e, wall_e2e),
-           "api": "matgb_solve_multi (mat_solve over 16 columns), pinned host"}
-    for p in (hA, hB, hX):
-        c.matgb_host_free(p)
+    L.check(c.matgb_event_record(0), "ev")
+    for _ in range(steps):
+        L.check(c.matgb_gemm_dev(b"N", b"N", n, n, n, 1.0, dA0, n, dA0, n, 0.0,
+                                 dC, n), "gemm")
+    L.check(c.matgb_event_record(1), "ev")
+    L.sync()
+    ms_g = c.matgb_event_elapsed_ms(0, 1) / steps
     for d in [dA0, dB, dX, dpiv] + dAs:
         L.dfree(d)
-    return {
-        "value": value, "unit": "TFLOP/s", "ms_per_step": ms_step,
-        "dtype": "f32", "gpu_launches": launches,
-        "config": {"workload": "plain_lu_solve_8192_f32", "n": n, "nrhs": nrhs,
-                   "A": "i.i.d. N(0,1) (seeded)", "pivoting": "partial",
-                   "l2": "inputs larger than L2 (256 MiB per A); fresh copy per step"},
-        "backward_error_max": eta, "roofline": rl, "e2e": e2e,
-        "clocks": clk.summary(),
-    }
+    return {"plu_solve_8192_f32": {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12,
+                                   "nrhs": nrhs, "bwd_err_max": eta},
+            "gemm_8192_f32": {"ms": ms_g, "tflops": 2 * n ** 3 / (ms_g * 1e-3) / 1e12}}
 
 
-def kernel_roofline(L, one_step, dA0, nA, dwork):
-    c = L.c
-    L.check(c.matgb_memcpy_d2d(dwork, dA0, nA), "d2d")
+def run_spd(mg, n=16384, nrhs=64):
+    """SPD solve with 64 right-hand sides: mixed Cholesky + refinement for
+    lambda in [1,1e3] (BF16) and [1,1e6] (FP16), and the plain FP64 Cholesky."""
+    import torch
+    L = mg.load("f64")
+    mats, B = spd_set(n, (1e3, 1e6), nrhs, 77)
+    X = torch.empty_like(B)
+    flops = n ** 3 / 3 + 2 * nrhs * 2 * n * n
+    out = {}
+    for lm, lp in ((1e3, 1), (1e6, 0)):
+        opts = L.ir_opts(lp_format=lp)
+        rep = mg.MatIRReport()
+        for rnd in range(2):
+            L.sync()
+            t0 = time.perf_counter()
+            rc = L.c.matgb_posv_ir_dev(n, nrhs, mats[lm].data_ptr(), n,
+                                       B.data_ptr(), n, X.data_ptr(), n,
+                                       C.byref(opts), C.byref(rep))
+            L.sync()
+            ms = (time.perf_counter() - t0) * 1e3
+        L.check(rc if rc != -1 else 0, "posv_ir")
+        r = rep.as_dict()
+        out["lam_1e%d" % int(round(np.log10(lm)))] = {
+            "ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "ret": rc,
+            "converged": r["converged"], "bwd_err": r["backward_error"],
+            "lp_format": r["lp_format"], "refinements": r["refinements"],
+            "ms_factor": r["ms_factor"], "ms_refine": r["ms_refine"]}
+    # plain FP64 Cholesky + 64-RHS solve
+    A = mats[1e3]
+    Aw = A.clone()
+    info = torch.zeros(4, device="cuda", dtype=torch.int32)
+    Xp = B.clone()
+    torch.cuda.synchronize()
     L.sync()
-    c.matgb_ktime_enable(1)
-    one_step()
+    t0 = time.perf_counter()
+    L.check(L.c.matgb_potrf_dev(n, Aw.data_ptr(), n, info.data_ptr()), "potrf")
+    L.check(L.c.matgb_potrs_dev(n, nrhs, Aw.data_ptr(), n, Xp.data_ptr(), n,
+                                info.data_ptr()), "potrs")
     L.sync()
-    import ctypes as C
-    names = (C.c_char * 64)()
-    res = []
-    i = 0
-    while True:
-        cnt = C.c_longlong()
-        ms = C.c_double()
-        fl = C.c_double()
-        by = C.c_double()
-        if c.matgb_ktime_get(i, names, 64, C.byref(cnt), C.byref(ms),
-                             C.byref(fl), C.byref(by)) != 0:
-            break
-        res.append((names.value.decode(), cnt.value, ms.value, fl.value, by.value))
-        i += 1
-    c.matgb_ktime_enable(0)
-    tot = sum(r[2] for r in res) or 1.0
-    top = max(res, key=lambda r: r[2]) if res else ("none", 0, 0, 0, 0)
+    ms_p = (time.perf_counter() - t0) * 1e3
+    out["plain_fp64"] = {"ms": ms_p, "tflops": flops / (ms_p * 1e-3) / 1e12}
+    for k in out:
+        if k.startswith("lam"):
+            out[k]["speedup_vs_plain"] = ms_p / out[k]["ms"]
+    del mats, Aw, Xp, X, B
+    torch.cuda.empty_cache()
+    return {"workload": "spd_ir_16384_64rhs_f64", **out}
+
+
+def run_batched(mg, count=100000, steps=5, warmup=3):
+    L = mg.load("f32")
+    rs = np.random.default_rng(1005)
+    ns = rs.integers(4, 129, count).astype(np.int32)
+    kinds = (np.arange(count) % 2).astype(np.uint8)
+    offA = np.zeros(count, np.int64)
+    offA[1:] = np.cumsum(ns.astype(np.int64) ** 2)[:-1]
+    offv = np.zeros(count, np.int64)
+    offv[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+    totA = int(offA[-1] + ns[-1] ** 2)
+    totv = int(offv[-1] + ns[-1])
+    A = np.empty(totA, np.float32)
+    for n in range(4, 129):
+        idx = np.nonzero(ns == n)[0]
+        lu = idx[kinds[idx] == 0]
+        sp = idx[kinds[idx] == 1]
+        if len(lu):
+            M = rs.uniform(-1, 1, (len(lu), n, n)).astype(np.float32) + \
+                n * np.eye(n, dtype=np.float32)
+            A[(offA[lu][:, None] + np.arange(n * n)).ravel()] = \
+                M.transpose(0, 2, 1).reshape(len(lu), -1).ravel()
+        if len(sp):
+            Bm = rs.standard_normal((len(sp), n, n)).astype(np.float32)
+            M = np.matmul(Bm.transpose(0, 2, 1), Bm) + n * np.eye(n, dtype=np.float32)
+            A[(offA[sp][:, None] + np.arange(n * n)).ravel()] = \
+                M.transpose(0, 2, 1).reshape(len(sp), -1).ravel()
+    b = rs.standard_normal(totv).astype(np.float32)
+    arrs = {"n": ns, "oA": offA, "ov": offv, "A": A, "b": b, "k": kinds}
+    d = {k: L.dalloc(v.nbytes) for k, v in arrs.items()}
+    dx = L.dalloc(b.nbytes)
+    st = L.dalloc(4 * count)
+    for k, v in arrs.items():
+        L.h2d(d[k], v)
+    L.sync()
+
+    def run():
+        L.check(L.c.matgb_solve_batched_dev(count, d["n"], d["oA"], d["A"],
+                                            d["ov"], d["b"], dx, d["k"], st),
+                "batched")
+
+    for _ in range(warmup):
+        run()
+    L.sync()
+    L.check(L.c.matgb_event_record(0), "ev")
+    for _ in range(steps):
+        run()
+    L.check(L.c.matgb_event_record(1), "ev")
+    L.sync()
+    ms = L.c.matgb_event_elapsed_ms(0, 1) / steps
+    byt = 4 * (totA + 2 * totv)
+    status = np.empty(count, np.int32)
+    L.d2h(status, st)
+    x = np.empty(totv, np.float32)
+    L.d2h(x, dx)
+    worst = 0.0
+    for s in rs.integers(0, count, 100):
+        n = ns[s]
+        M = A[offA[s]:offA[s] + n * n].reshape(n, n, order="F").astype(np.float64)
+        xs = x[offv[s]:offv[s] + n].astype(np.float64)
+        bs = b[offv[s]:offv[s] + n]
+        worst = max(worst, np.abs(M @ xs - bs).max() /
+                    (np.abs(M).sum(1).max() * np.abs(xs).max() + np.abs(bs).max()))
+    for v in list(d.values()) + [dx, st]:
+        L.dfree(v)
     pk, src = peaks()
-    achieved = top[3] / (top[2] * 1e-3) / 1e12 if top[2] > 0 else 0.0
-    fp32_peak = pk.get("fp32_tflops") or L.c.matgb_measure_fma_peak(0)
-    if not fp32_peak or fp32_peak <= 0:
-        fp32_peak = None
-    return {
-        "kernel": top[0], "launches": top[1], "share": top[2] / tot,
-        "bound": "fp32_simt", "achieved": achieved, "unit": "TFLOP/s",
-        "peak": fp32_peak, "frac": (achieved / fp32_peak) if fp32_peak else None,
-        "traffic": None,
-        "note": "FP32 has no tensor-core kind on sm_103a; peak = FFMA issue "
-                "rate measured by matgb_peak_fp32 when available",
-        "per_kernel": [{"name": r[0], "launches": r[1], "ms": r[2],
-                        "tflops": (r[3] / (r[2] * 1e-3) / 1e12) if r[2] else 0}
-                       for r in sorted(res, key=lambda r: -r[2])],
+    gbs = byt / (ms * 1e-3) / 1e9
+    return {"workload": "batched_100k_uneven_f32", "ms": ms,
+            "solves_per_s": count / (ms * 1e-3), "bytes": byt,
+            "hbm_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"],
+            "hbm_peak_source": src, "status_nonzero": int((status != 0).sum()),
+            "bwd_err_sample_max": worst}
+
+
+# ----------------------------------------------------------------- CPU legs
+def cpu_sample(n=1024, budget_s=12.0):
+    """The reference's mat_solve (plain PLU + triangular solves) in double,
+    oracle port on one core, on an n x n N(0,1) sample.  TFLOP/s."""
+    from oracle.loader import Oracle
+    from libmat_gb300 import rng
+    O = Oracle("f64", "port")
+    A = rng.normal(1001, (n, n), np.float64)
+    b = rng.normal(2001, (n,), np.float64)
+    flops = 2 * n ** 3 / 3 + 2 * n * n
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        O.solve(A, b)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or reps >= 50:
+            break
+    return flops * reps / el / 1e12, el / reps
+
+
+def _ref_worker(args):
+    n, seed = args
+    from oracle.loader import Oracle
+    from libmat_gb300 import rng
+    O = Oracle("f64", "port")
+    A = rng.normal(seed, (n, n), np.float64)
+    b = rng.normal(seed + 1, (n,), np.float64)
+    O.solve(A, b)
+    return 1
+
+
+def run_reference(args):
+    """Reference arm: the reference's algorithm (oracle port of mat_solve in
+    double) on all host cores, one independent n x n solve per core per
+    step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    n = 1024
+    flops = 2 * n ** 3 / 3 + 2 * n * n
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for i in range(args.warmup):
+            pool.map(_ref_worker, [(n, 100 + i * cores + j) for j in range(cores)])
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            pool.map(_ref_worker, [(n, 5000 + i * cores + j) for j in range(cores)])
+        el = time.perf_counter() - t0
+    tf = flops * cores * args.steps / el / 1e12
+    line = {
+        "impl": "reference", "metric": METRIC, "value": tf, "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "mixed_lu_ir_16384_f64",
+                   "sample": f"{cores} independent f64 solves of n={n} per step "
+                             "(reference's plain LU solve, bounded sample)"},
+        "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"n={n} f64 N(0,1), 1 RHS, {cores} processes"},
+        "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
     }
+    print(json.dumps(line), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--lp", type=int, default=2,
+                    help="2 FP16 split (3 products), 0 FP16, 1 BF16, -1 FP32")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--only", choices=["plain_f32", "spd", "batched"],
+                    help="run one secondary workload alone and print its JSON "
+                         "(small cases for profiling)")
+    ap.add_argument("--count", type=int, default=100000,
+                    help="systems in the batched workload")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        import libmat_gb300 as mg
+        for p in ("f32", "f64"):
+            if mg.load(p).c.matgb_init(0) != 0:
+                raise SystemExit("matgb_init failed")
+        if args.only == "plain_f32":
+            out = run_plain_f32(mg, steps=args.steps, warmup=args.warmup)
+        elif args.only == "spd":
+            out = run_spd(mg, n=args.n)
+        else:
+            out = run_batched(mg, count=args.count, steps=args.steps,
+                              warmup=args.warmup)
+        print(json.dumps(out), flush=True)
+        return
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    import torch
+    torch.cuda.set_device(local)
     import libmat_gb300 as mg
     for p in ("f32", "f64"):
-        rc = mg.load(p).c.matgb_init(local)
-        if rc != 0:
+        if mg.load(p).c.matgb_init(local) != 0:
             raise SystemExit("matgb_init failed: %s" % mg.load(p).c.matgb_last_error())
-    res = run_plain(args, mg)
+    res = run_headline(args, mg)
     if world > 1:
-        # replicas only: every rank runs the same independent workload; the
-        # whole-job value is the sum, timed by the slowest rank.
+        # replicas only: every rank solves the same independent systems; the
+        # whole-job value is the sum over ranks timed by the slowest rank
         import torch.distributed as dist
         dist.init_process_group("gloo")
         t = [None] * world
         dist.all_gather_object(t, res["ms_per_step"])
-        res["ms_per_step"] = max(t)
         dist.destroy_process_group()
-        res["value"] = res["value"] * world * min(t) / max(t) if False else \
-            (2 * args.n ** 3 / 3 + 32 * args.n ** 2) * world / (res["ms_per_step"] * 1e-3) / 1e12
+        res["ms_per_step"] = max(t)
+        res["value"] = (2 * args.n ** 3 / 3 + 2 * args.n ** 2) * world / \
+            (res["ms_per_step"] * 1e-3) / 1e12
     if rank != 0:
         return
+    secondary = None
+    if not args.no_secondary:
+        secondary = {"plain_f32": run_plain_f32(mg), "spd": run_spd(mg),
+                     "batched": run_batched(mg)}
     cpu = None
     if not args.no_cpu:
-        v, per, n = cpu_plain_sample()
+        v, per = cpu_sample()
         cpu = {"value": v, "unit": "TFLOP/s", "cores": 1, "kind": "port",
-               "sample": f"PLU + 16 RHS at n={n}, f32 N(0,1), {per:.2f} s per solve"}
+               "sample": f"reference mat_solve algorithm in f64 at n=1024, "
+                         f"{per:.2f} s per solve"}
     line = {"metric": METRIC, "value": res["value"], "unit": res["unit"],
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": res["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": res["dtype"],
             "data": "synthetic", "config": res["config"],
-            "backward_error_max": res["backward_error_max"],
+            "all_converged_to_target": res["all_converged_to_target"],
+            "per_kappa": res["per_kappa"], "plain_fp64": res["plain_fp64"],
             "roofline": res["roofline"], "cpu_baseline": cpu, "e2e": res["e2e"],
-            "gpu_launches": res["gpu_launches"], "clocks": res["clocks"]}
+            "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
+            "kernels": res["kernels"], "secondary": secondary,
+            "wall_ms_per_step": res["wall_ms_per_step"]}
     print(json.dumps(line), flush=True)
 
 

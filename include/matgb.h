@@ -139,8 +139,13 @@ int matgb_gemv_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
  * update and convergence test run on the GPU in the library's element type
  * (FP64 in libmatgb_f64). */
 typedef struct {
-  int lp_format;     /* 1 = BF16 (default), 0 = FP16 (per-block power-of-2
-                        scale), -1 = FP32 trailing updates (SIMT)            */
+  int lp_format;     /* 2 (default) = FP16 split: both operands scaled by
+                        powers of two and split into FP16 hi + remainder,
+                        three tensor-core products per update (FP32-level
+                        factors; refinement converges to kappa ~ 1e6 and
+                        beyond); 0 = FP16 (one product, U12 scaled);
+                        1 = BF16 (one product; at n ~ 1e4 too coarse to
+                        refine past kappa ~ 1e2); -1 = FP32 SIMT updates    */
   int max_iter;      /* factor solves over all attempts (default 100)        */
   double tol;        /* target backward error; <= 0: n * unit roundoff of the
                         element type (n * 2^-53 in libmatgb_f64)             */
@@ -151,7 +156,7 @@ typedef struct {
                         flexible GMRES preconditioned with the low-precision
                         factors (converges for kappa(A) * u_16 well above 1);
                         0: classic refinement, one factor solve per step    */
-  int krylov_dim;    /* Krylov vectors per cycle (default 40, at most 64)   */
+  int krylov_dim;    /* Krylov vectors per cycle (default 50, at most 64)   */
 } MatIROpts;
 
 typedef struct {
@@ -190,12 +195,14 @@ int matgb_posv_ir_dev(size_t n, size_t nrhs, const mat_elem_t *A, size_t lda,
 /* Host Mat form of matgb_posv_ir_dev (b and x n x nrhs). */
 int mat_solve_spd_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,
                      MatIRReport *rep);
-/* The FP32 Cholesky alone (device, in place, lower) with tensor-core (1 BF16,
- * 0 FP16) or SIMT (-1) trailing updates; *info as matgb_potrf_dev. */
+/* The FP32 Cholesky alone (device, in place, lower) with tensor-core (2 FP16
+ * split, 1 BF16, 0 FP16) or SIMT (-1) trailing updates; *info as
+ * matgb_potrf_dev. */
 int matgb_potrf_lp_dev(size_t n, float *A, size_t lda, int32_t *info,
                        int lp_format);
 /* The FP32 LU alone (device, in place) with trailing updates on the tensor
- * cores (lp_format 1 BF16, 0 FP16) or, for lp_format -1, the FP32 SIMT GEMM.
+ * cores (lp_format 2 FP16 split, 1 BF16, 0 FP16) or, for lp_format -1, the
+ * FP32 SIMT GEMM.
  * ipiv/perm as matgb_getrf_dev.  Pivots are never skipped (threshold 0). */
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
                        int32_t *perm, int lp_format);
@@ -206,6 +213,13 @@ int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
 int matgb_tc_gemm_dev(int bf16, size_t M, size_t N, size_t K, const void *A,
                       size_t lda, const void *B, size_t ldb, float alpha,
                       float beta, float *C, size_t ldc);
+/* Split form: FP16 hi parts (Ah, Bh) and remainders (Al, Bl), same layouts;
+ * computes C = beta*C + alpha*(Ah Bh^T + Ah Bl^T + Al Bh^T) in one pass over
+ * C (three tensor-core products, FP32 accumulation).  K a multiple of 64. */
+int matgb_tc_gemm_split_dev(size_t M, size_t N, size_t K, const void *Ah,
+                            const void *Al, size_t lda, const void *Bh,
+                            const void *Bl, size_t ldb, float alpha, float beta,
+                            float *C, size_t ldc);
 /* 0, or MATGB_ERR_TIMEOUT if a tensor-core kernel gave up a bounded wait
  * since the last call (clears the flag; synchronises). */
 int matgb_tc_status(void);

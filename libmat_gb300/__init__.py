@@ -144,6 +144,8 @@ class Lib:
             "matgb_tc_gemm_dev": (_I, [_I, _S, _S, _S, _P, _S, _P, _S,
                                        C.c_float, C.c_float, _P, _S]),
             "matgb_tc_status": (_I, []),
+            "matgb_tc_gemm_split_dev": (_I, [_S, _S, _S, _P, _P, _S, _P, _P, _S,
+                                             C.c_float, C.c_float, _P, _S]),
             "matgb_getrf_lp_dev": (_I, [_S, _P, _S, _P, _P, _I]),
             "matgb_ir_default_opts": (None, [C.POINTER(MatIROpts)]),
             "matgb_gesv_ir_dev": (_I, [_S, _P, _S, _P, _P,
@@ -312,7 +314,7 @@ class Lib:
                 setattr(o, k, v)
         return o
 
-    def mat_solve_ir(self, A, b, lp_format=1, max_iter=None, tol=0.0,
+    def mat_solve_ir(self, A, b, lp_format=None, max_iter=None, tol=0.0,
                      fp32_fallback=1, krylov=None, krylov_dim=None):
         """Mixed-precision LU + refinement; returns (x, report dict)."""
         A, b = self.arr(A), self.arr(b)
@@ -358,7 +360,7 @@ class Lib:
                 self.dfree(d)
         return [x[o:o + k] for o, k in zip(offv, ns)], status
 
-    def mat_solve_spd_ir(self, A, B, lp_format=1, max_iter=None, tol=0.0,
+    def mat_solve_spd_ir(self, A, B, lp_format=None, max_iter=None, tol=0.0,
                          fp32_fallback=1, krylov=None, krylov_dim=None):
         """Mixed-precision Cholesky + refinement, many RHS; (X, ret, report)."""
         A, B = self.arr(A), self.arr(B)

@@ -95,6 +95,9 @@ struct VecOf<float> {
     const float4 v = *reinterpret_cast<const float4 *>(p);
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
   }
+  static __device__ __forceinline__ void put(float *p, const float (&o)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+  }
 };
 template <>
 struct VecOf<double> {
@@ -104,22 +107,31 @@ struct VecOf<double> {
     const double2 v = *reinterpret_cast<const double2 *>(p);
     o[0] = v.x; o[1] = v.y;
   }
+  static __device__ __forceinline__ void put(double *p, const double (&o)[2]) {
+    *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
+  }
 };
 
-// Write the owned row (its live leading entries, chunk by chunk) and its
-// right-hand side into a slot.
+// Write the owned row (its live entries) and its right-hand side into a slot
+// with 16-byte stores: slot[3] = a[0], then (a[Wg+1..Wg+W]) at slot[4+Wg], the
+// last group ending with the right-hand side at slot[NB+3].
 template <typename T, int NB>
 __device__ __forceinline__ void put_row(T *slot, const T (&a)[NB], T rb,
                                         int n_live) {
-  constexpr int C = Chunk<NB>::v;
+  constexpr int W = VecOf<T>::w;
+  slot[3] = a[0];
 #pragma unroll
-  for (int c = 0; c < NB / C; c++) {
-    if (c * C < n_live) {
+  for (int g = 0; g < NB / W; g++) {
+    if (W * g + 1 < n_live || g == NB / W - 1) {
+      T v[W];
 #pragma unroll
-      for (int k = 0; k < C; k++) slot[3 + c * C + k] = a[c * C + k];
+      for (int q = 0; q < W; q++) {
+        const int k = W * g + 1 + q;
+        v[q] = k < NB ? a[k] : rb;
+      }
+      VecOf<T>::put(slot + 4 + W * g, v);
     }
   }
-  slot[NB + 3] = rb;
 }
 
 // One elimination step in the shifted frame: a[j] <- a[j+1] - u[j+1] * l over

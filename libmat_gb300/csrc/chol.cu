@@ -204,7 +204,7 @@ int matgb_potrf_lp_dev(size_t n, float *A, size_t lda, int32_t *info,
                        int lp_format) {
   if (lda < n) return set_error(MATGB_ERR_ARG, "potrf_lp: lda < n");
   if (!info) return set_error(MATGB_ERR_ARG, "potrf_lp: info is NULL");
-  if (lp_format < -1 || lp_format > 1)
+  if (lp_format < -1 || lp_format > 2)
     return set_error(MATGB_ERR_ARG, "potrf_lp: lp_format");
   return potrf_t<float>((int64_t)n, A, (int64_t)lda, info, lp_format);
 }

@@ -121,11 +121,13 @@ int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
             const int32_t *perm, const T *B, int64_t ldb, T *X, int64_t ldx);
 // Tensor-core rank-K update (tc_gemm.cu).
 // lower: only tiles on/below the diagonal, elements with col <= row;
-// skip: every CTA returns at once when *skip != 0 (may be null).
+// skip: every CTA returns at once when *skip != 0 (may be null);
+// Alo/Blo (may be null): remainders of A and B for the three-product split.
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
-            int lower, const int32_t *skip);
+            int lower, const int32_t *skip, const void *Alo = nullptr,
+            const void *Blo = nullptr);
 // Cholesky trailing update C22 -= L21 L21^T on the tensor cores (mixed.cu).
 int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
                    float *C22, int64_t ldc, int lp, const int32_t *info);
@@ -145,10 +147,13 @@ int tc_error_flag(int clear);
 // 2n floats; stops when the residual estimate is <= max(rtol*|r0|, atol).
 constexpr int kKrylovMaxDim = 64;
 constexpr int kKrylovMaxParts = 64;
+// A cycle that has not reduced the residual estimate below abort_ratio * |r0|
+// after abort_after steps stops early with *stalled = 1.
 int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
                  const float *W, const int32_t *perm, elem_t *V, elem_t *Z,
-                 float *F, int m, double rtol, double atol, elem_t *d,
-                 int *inner, double *res_est);
+                 float *F, int m, double rtol, double atol, int abort_after,
+                 double abort_ratio, elem_t *d, int *inner, double *res_est,
+                 int *stalled);
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm);
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,
           const int32_t *perm, const elem_t *B, int64_t ldb, elem_t *X,

@@ -146,8 +146,9 @@ static unsigned grid_for(int64_t n) {
 
 int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
                  const float *W, const int32_t *perm, elem_t *V, elem_t *Z,
-                 float *F, int m, double rtol, double atol, elem_t *d,
-                 int *inner, double *res_est) {
+                 float *F, int m, double rtol, double atol, int abort_after,
+                 double abort_ratio, elem_t *d, int *inner, double *res_est,
+                 int *stalled) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   cudaStream_t st = cx->stream;
@@ -176,6 +177,7 @@ int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
   beta = std::sqrt(beta);
   *inner = 0;
   *res_est = beta;
+  *stalled = 0;
   if (!(beta > 0) || !std::isfinite(beta)) {
     MGB_CUDA(cudaMemsetAsync(d, 0, (size_t)n * sizeof(elem_t), st));
     return 0;
@@ -240,6 +242,12 @@ int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
     gv[k] = cs[k] * gv[k];
     *res_est = std::fabs(gv[k + 1]);
     const bool done = *res_est <= target || !(hn > 0);
+    // too slow for these factors: leave the cycle (the caller refactors)
+    if (!done && k + 1 >= abort_after && *res_est > abort_ratio * beta) {
+      *stalled = 1;
+      k++;
+      break;
+    }
     if (!done && k + 1 < m) {
       krylov_scale_kernel<elem_t><<<g, 256, 0, st>>>(n, w, 1.0 / hn, Fin);
       MGB_LAUNCHED("krylov_scale");

@@ -197,6 +197,32 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
   }
 }
 
+// Best (key, index) of cnt <= 32 candidates in shared memory, reduced across
+// the warp by shuffles (every lane gets the result and the winner's slot).
+// Ties between real candidates cannot happen (their indices are distinct).
+template <typename T>
+__device__ __forceinline__ void pick_best(const T *keys, const int *idxs,
+                                          int cnt, T &bk, int &bi, int &bw) {
+  const int lane = threadIdx.x & 31;
+  T k = lane < cnt ? keys[lane] : (T)-3;
+  int i = lane < cnt ? idxs[lane] : INT_MAX;
+  int w = lane;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const T ok = __shfl_xor_sync(0xffffffffu, k, off);
+    const int oi = __shfl_xor_sync(0xffffffffu, i, off);
+    const int ow = __shfl_xor_sync(0xffffffffu, w, off);
+    if (better(ok, oi, k, i)) {
+      k = ok;
+      i = oi;
+      w = ow;
+    }
+  }
+  bk = k;
+  bi = i;
+  bw = w;
+}
+
 // Register-resident panel for the reference's 24-column width: thread tid of
 // CTA c owns panel rows c*rpc + tid + r*NT (r < R), all 24 columns of each in
 // registers; the column loop is unrolled so every register index is static.
@@ -271,11 +297,9 @@ __global__ void __launch_bounds__(NT, 1)
     }
     if (lane == 0) { sm.wkey[warp] = bk; sm.widx[warp] = bi; }
     __syncthreads();
-    T ck = sm.wkey[0];
-    int ci = sm.widx[0], cw = 0;
-#pragma unroll
-    for (int q = 1; q < NW; q++)
-      if (better(sm.wkey[q], sm.widx[q], ck, ci)) { ck = sm.wkey[q]; ci = sm.widx[q]; cw = q; }
+    T ck;
+    int ci, cw;
+    pick_best<T>(sm.wkey, sm.widx, NW, ck, ci, cw);
     const bool own_k = (kk >= rbase && kk < rbase + rpc);
     const int nval = CS * kW;
     const int total = nval + CS + (own_k ? nval : 0);
@@ -295,15 +319,9 @@ __global__ void __launch_bounds__(NT, 1)
       }
     }
     cluster.sync();
-    int wc = 0;
-    T gk = sm.xkey[buf][0];
-    int p = sm.xidx[buf][0];
-    for (int q = 1; q < CS; q++)
-      if (better(sm.xkey[buf][q], sm.xidx[buf][q], gk, p)) {
-        gk = sm.xkey[buf][q];
-        p = sm.xidx[buf][q];
-        wc = q;
-      }
+    T gk;
+    int p, wc;
+    pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
     if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
     const T *u = &sm.xval[buf][wc][0];
     const T *kv = &sm.kval[buf][0];
@@ -403,41 +421,94 @@ __device__ void build_swap_map(SwapMap &sm, const int32_t *__restrict__ ipiv,
   if (lane == 0) sm.cnt = nk + nx;
 }
 
-// Apply the row mapping to columns [c0,c1) and [c2,c3) (LC per CTA) and, on
-// CTA 0, to the permutation vector.
-template <typename T>
-struct SwapCols {
-  static constexpr int LC = sizeof(T) == 4 ? 16 : 8;
-};
+// The map is built once per swap block by one warp (swap_map_kernel) into a
+// small device ring; the swap kernel's CTAs read it.
+__global__ void swap_map_kernel(const int32_t *__restrict__ ipiv, int64_t k1,
+                                int64_t k2, SwapMap *__restrict__ out) {
+  __shared__ SwapMap sm;
+  build_swap_map(sm, ipiv, k1, k2);
+  __syncwarp();
+  const int cnt = sm.cnt;
+  for (int i = threadIdx.x; i < cnt; i += 32) {
+    out->pos[i] = sm.pos[i];
+    out->src[i] = sm.src[i];
+  }
+  if (threadIdx.x == 0) out->cnt = cnt;
+}
 
-template <typename T>
+// Apply the row mapping to columns [c0,c1) and [c2,c3) and, on CTA 0, to the
+// permutation vector.  One warp per column at a time (8 warps, 32 columns per
+// CTA), lanes across the map entries: the rows of the block [k1,k2) are
+// contiguous in a column, so that half of every gather/scatter coalesces; a
+// column is read whole into registers before it is written.
+constexpr int kSwapCols = 32;
+
+// BUILD: few CTAs (a swap inside a block column) -- warp 0 of every CTA
+// builds the map itself, saving the extra launch; otherwise it comes from
+// swap_map_kernel.
+template <typename T, bool BUILD>
 __global__ void __launch_bounds__(256)
     laswp_kernel(T *__restrict__ A, int64_t lda, int64_t c0, int64_t c1,
-                 int64_t c2, int64_t c3, const int32_t *__restrict__ ipiv,
-                 int64_t k1, int64_t k2, int32_t *__restrict__ perm) {
-  constexpr int LC = SwapCols<T>::LC;
-  constexpr int RG = 256 / LC;
+                 int64_t c2, int64_t c3, const SwapMap *__restrict__ map,
+                 const int32_t *__restrict__ ipiv, int64_t k1, int64_t k2,
+                 int32_t *__restrict__ perm) {
+  constexpr int RPL = 2 * kSwapMax / 32;  // map entries per lane
   __shared__ SwapMap sm;
-  __shared__ T vals[2 * kSwapMax][LC + 1];
-  __shared__ int32_t pv[2 * kSwapMax];
-  if (threadIdx.x < 32) build_swap_map(sm, ipiv, k1, k2);
+  if (BUILD) {
+    if (threadIdx.x < 32) build_swap_map(sm, ipiv, k1, k2);
+  } else {
+    const int c = __ldg(&map->cnt);
+    for (int r = threadIdx.x; r < c; r += 256) {
+      sm.pos[r] = __ldg(&map->pos[r]);
+      sm.src[r] = __ldg(&map->src[r]);
+    }
+    if (threadIdx.x == 0) sm.cnt = c;
+  }
   __syncthreads();
   const int cnt = sm.cnt;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t src[RPL], pos[RPL];
+#pragma unroll
+  for (int q = 0; q < RPL; q++) {
+    const int r = lane + 32 * q;
+    src[q] = r < cnt ? sm.src[r] : 0;
+    pos[q] = r < cnt ? sm.pos[r] : 0;
+  }
   const int64_t na = c1 - c0, nb = c3 - c2;
-  const int tid = threadIdx.x, lc = tid % LC, rg = tid / LC;
-  const int64_t t = (int64_t)blockIdx.x * LC + lc;
-  const bool ok = t < na + nb;
-  T *colp = ok ? A + (t < na ? c0 + t : c2 + (t - na)) * lda : nullptr;
-  for (int r = rg; r < cnt; r += RG)
-    if (ok) vals[r][lc] = colp[sm.src[r]];
-  if (blockIdx.x == 0 && perm)
-    for (int r = tid; r < cnt; r += 256) pv[r] = perm[sm.src[r]];
-  __syncthreads();
-  for (int r = rg; r < cnt; r += RG)
-    if (ok) colp[sm.pos[r]] = vals[r][lc];
-  if (blockIdx.x == 0 && perm)
-    for (int r = tid; r < cnt; r += 256) perm[sm.pos[r]] = pv[r];
+  for (int cc = warp; cc < kSwapCols; cc += 8) {
+    const int64_t t = (int64_t)blockIdx.x * kSwapCols + cc;
+    if (t >= na + nb) break;
+    T *colp = A + (t < na ? c0 + t : c2 + (t - na)) * lda;
+    T v[RPL];
+#pragma unroll
+    for (int q = 0; q < RPL; q++)
+      if (lane + 32 * q < cnt) v[q] = colp[src[q]];
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < RPL; q++)
+      if (lane + 32 * q < cnt) colp[pos[q]] = v[q];
+  }
+  if (blockIdx.x == 0 && perm) {
+    // the permutation vector: one warp, same scheme
+    if (warp == 0) {
+      int32_t pv[RPL];
+#pragma unroll
+      for (int q = 0; q < RPL; q++)
+        if (lane + 32 * q < cnt) pv[q] = perm[src[q]];
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < RPL; q++)
+        if (lane + 32 * q < cnt) perm[pos[q]] = pv[q];
+    }
+  }
 }
+
+// Ring of device swap maps: the panel stream and the main stream each use
+// one slot at a time, and a slot is rewritten only several blocks later,
+// after stream order has retired its readers.
+constexpr int kSwapRing = 16;
+static SwapMap *g_swap_ring = nullptr;
+static int g_swap_next = 0;
 
 template <typename T>
 int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
@@ -445,12 +516,21 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
   const int64_t ncol = (c1 - c0) + (c3 - c2);
   if (k2 <= k1 || (ncol <= 0 && !perm)) return 0;
   if (k2 - k1 > kSwapMax) return set_error(MATGB_ERR_ARG, "laswp: block > 128");
-  constexpr int LC = SwapCols<T>::LC;
-  int64_t blocks = (ncol + LC - 1) / LC;
+  if (!g_swap_ring) MGB_CUDA(cudaMalloc(&g_swap_ring, kSwapRing * sizeof(SwapMap)));
+  SwapMap *map = g_swap_ring + g_swap_next;
+  g_swap_next = (g_swap_next + 1) % kSwapRing;
+  int64_t blocks = (ncol + kSwapCols - 1) / kSwapCols;
   if (blocks < 1) blocks = 1;
   KtScope kt("laswp", 0.0, 4.0 * (k2 - k1) * ncol * sizeof(T));
-  laswp_kernel<T><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
-      A, lda, c0, c1, c2, c3, ipiv, k1, k2, perm);
+  if (blocks <= 8) {
+    laswp_kernel<T, true><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
+        A, lda, c0, c1, c2, c3, nullptr, ipiv, k1, k2, perm);
+  } else {
+    swap_map_kernel<<<1, 32, 0, ctx()->stream>>>(ipiv, k1, k2, map);
+    MGB_LAUNCHED("swap_map");
+    laswp_kernel<T, false><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
+        A, lda, c0, c1, c2, c3, map, ipiv, k1, k2, perm);
+  }
   MGB_LAUNCHED("laswp");
   return 0;
 }

@@ -44,11 +44,19 @@ __device__ __forceinline__ float fp16_scale(unsigned amax_bits) {
 // out[i*Kp + k] = A[i + k*lda] for i < m, k < nb (zero for nb <= k < Kp):
 // L21 (column-major, M-contiguous) to a K-contiguous 16-bit operand.
 template <int BF16>
+__device__ __forceinline__ float from16(uint16_t h) {
+  if (BF16) return __bfloat162float(__ushort_as_bfloat16(h));
+  return __half2float(__ushort_as_half(h));
+}
+
+// out_lo (optional): the remainder v - hi(v), also 16-bit (the split form).
+template <int BF16>
 __global__ void pack_l21_kernel(const float *__restrict__ A, int64_t lda,
                                 int64_t m, int nb, int Kp,
                                 uint16_t *__restrict__ out,
                                 const unsigned *__restrict__ amax_bits,
-                                float *__restrict__ scale) {
+                                float *__restrict__ scale,
+                                uint16_t *__restrict__ out_lo = nullptr) {
   __shared__ float t[32][33];
   // optional FP16 scale s (products of two scaled operands carry s^2)
   const float s = amax_bits ? fp16_scale(*amax_bits) : 1.f;
@@ -68,7 +76,12 @@ __global__ void pack_l21_kernel(const float *__restrict__ A, int64_t lda,
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
     const int64_t i = i0 + r;
-    if (i < m) out[i * Kp + k0 + tx] = to16<BF16>(t[tx][r]);
+    if (i < m) {
+      const float v = t[tx][r];
+      const uint16_t h = to16<BF16>(v);
+      out[i * Kp + k0 + tx] = h;
+      if (out_lo) out_lo[i * Kp + k0 + tx] = to16<BF16>(v - from16<BF16>(h));
+    }
   }
 }
 
@@ -89,23 +102,31 @@ __global__ void u12_amax_kernel(const float *__restrict__ A, int64_t lda,
 }
 
 // out[j*Kp + k] = s * A[k + j*lda] (k < nb), 0 for nb <= k < Kp.
+// scale[1] = 1/s, or 1/(s * sL) when the L21 operand was scaled by
+// sL = fp16_scale(*amax_l); out_lo (optional) gets the remainders.
 template <int BF16>
 __global__ void pack_u12_kernel(const float *__restrict__ A, int64_t lda,
                                 int nb, int Kp, int64_t ncols,
                                 const unsigned *__restrict__ amax_bits,
                                 float *__restrict__ scale,
-                                uint16_t *__restrict__ out) {
+                                uint16_t *__restrict__ out,
+                                uint16_t *__restrict__ out_lo = nullptr,
+                                const unsigned *__restrict__ amax_l = nullptr) {
   const float s = (!BF16 && amax_bits) ? fp16_scale(*amax_bits) : 1.f;
   if (blockIdx.x == 0 && threadIdx.x == 0 && scale) {
+    const float sl = amax_l ? fp16_scale(*amax_l) : 1.f;
     scale[0] = s;
-    scale[1] = 1.f / s;
+    scale[1] = 1.f / (s * sl);  // powers of two: exact
   }
   const int64_t tot = (int64_t)Kp * ncols;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(e % Kp);
     const int64_t j = e / Kp;
-    out[e] = to16<BF16>(k < nb ? s * A[k + j * lda] : 0.f);
+    const float v = k < nb ? s * A[k + j * lda] : 0.f;
+    const uint16_t h = to16<BF16>(v);
+    out[e] = h;
+    if (out_lo) out_lo[e] = to16<BF16>(v - from16<BF16>(h));
   }
 }
 
@@ -115,58 +136,78 @@ static unsigned grid_cap(int64_t tot, int per = 256) {
   return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
+// lp: 1 BF16, 0 FP16 (U12 scaled by a power of two), 2 FP16 split (both
+// operands scaled and split into hi + remainder; three tensor-core products).
 int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
                        int64_t ke, int64_t c0, int64_t c1, int lp, bool pack) {
   const int nb = (int)(ke - kb);
   const int Kp = (nb + 63) / 64 * 64;
   const int64_t m = n - ke, ncols = n - ke;
-  uint16_t *A16 = (uint16_t *)ws(WS_T0, (size_t)m * Kp * 2);
-  uint16_t *B16 = (uint16_t *)ws(WS_T1, (size_t)ncols * Kp * 2);
+  const bool split = lp == 2;
+  const size_t an = (size_t)m * Kp, bn_ = (size_t)ncols * Kp;
+  uint16_t *A16 = (uint16_t *)ws(WS_T0, an * 2 * (split ? 2 : 1));
+  uint16_t *B16 = (uint16_t *)ws(WS_T1, bn_ * 2 * (split ? 2 : 1));
   float *sc = (float *)ws(WS_T2, 64);
   if (!A16 || !B16 || !sc) return MATGB_ERR_NOMEM;
-  unsigned *amax = (unsigned *)(sc + 4);
+  uint16_t *A16lo = split ? A16 + an : nullptr;
+  uint16_t *B16lo = split ? B16 + bn_ : nullptr;
+  unsigned *amax = (unsigned *)(sc + 4);  // [0] U12, [1] L21
   cudaStream_t st = ctx()->stream;
   if (pack) {
-    KtScope kt("lp_pack", 0.0, 6.0 * (m + ncols) * nb);
+    KtScope kt("lp_pack", 0.0, (split ? 10.0 : 6.0) * (m + ncols) * nb);
     dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
-    if (lp == 1)
-      pack_l21_kernel<1><<<g, 256, 0, st>>>(A + ke + kb * lda, lda, m, nb, Kp,
-                                            A16, nullptr, nullptr);
-    else
-      pack_l21_kernel<0><<<g, 256, 0, st>>>(A + ke + kb * lda, lda, m, nb, Kp,
-                                            A16, nullptr, nullptr);
-    MGB_LAUNCHED("pack_l21");
+    const float *L21 = A + ke + kb * lda;
     const float *U12 = A + kb + ke * lda;
-    if (lp == 0) {
-      MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
+    if (lp != 1) {
+      MGB_CUDA(cudaMemsetAsync(amax, 0, 2 * sizeof(unsigned), st));
       u12_amax_kernel<<<grid_cap((int64_t)nb * ncols), 256, 0, st>>>(
           U12, lda, nb, ncols, amax);
       MGB_LAUNCHED("u12_amax");
-      pack_u12_kernel<0><<<grid_cap((int64_t)Kp * ncols), 256, 0, st>>>(
-          U12, lda, nb, Kp, ncols, amax, sc, B16);
+    }
+    if (split) {
+      u12_amax_kernel<<<grid_cap((int64_t)nb * m), 256, 0, st>>>(
+          L21, lda, (int)m, nb, amax + 1);
+      MGB_LAUNCHED("l21_amax");
+      pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax + 1,
+                                            nullptr, A16lo);
+    } else if (lp == 1) {
+      pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr,
+                                            nullptr);
     } else {
+      pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr,
+                                            nullptr);
+    }
+    MGB_LAUNCHED("pack_l21");
+    if (lp == 1)
       pack_u12_kernel<1><<<grid_cap((int64_t)Kp * ncols), 256, 0, st>>>(
           U12, lda, nb, Kp, ncols, nullptr, sc, B16);
-    }
+    else
+      pack_u12_kernel<0><<<grid_cap((int64_t)Kp * ncols), 256, 0, st>>>(
+          U12, lda, nb, Kp, ncols, amax, sc, B16, B16lo,
+          split ? amax + 1 : nullptr);
     MGB_LAUNCHED("pack_u12");
   }
-  return tc_gemm(lp == 1, m, c1 - c0, Kp, A16, Kp, B16 + (c0 - ke) * Kp, Kp,
-                 -1.f, lp == 0 ? sc + 1 : nullptr, 1.f, A + ke + c0 * lda, lda,
-                 0, nullptr);
+  const int64_t off = (c0 - ke) * Kp;
+  return tc_gemm(lp == 1, m, c1 - c0, Kp, A16, Kp, B16 + off, Kp, -1.f,
+                 lp != 1 ? sc + 1 : nullptr, 1.f, A + ke + c0 * lda, lda, 0,
+                 nullptr, A16lo, split ? B16lo + off : nullptr);
 }
 
 // Cholesky: C22 (lower) -= L21 L21^T with L21 packed once to 16 bits and used
 // as both operands; FP16 scales L21 by a power of two s and the epilogue
-// multiplies by 1/s^2.
+// multiplies by 1/s^2; the split form (lp 2) also packs the remainders.
 int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
                    float *C22, int64_t ldc, int lp, const int32_t *info) {
   const int Kp = (nb + 63) / 64 * 64;
-  uint16_t *A16 = (uint16_t *)ws(WS_T0, (size_t)m * Kp * 2);
+  const bool split = lp == 2;
+  const size_t an = (size_t)m * Kp;
+  uint16_t *A16 = (uint16_t *)ws(WS_T0, an * 2 * (split ? 2 : 1));
   float *sc = (float *)ws(WS_T2, 64);
   if (!A16 || !sc) return MATGB_ERR_NOMEM;
+  uint16_t *A16lo = split ? A16 + an : nullptr;
   unsigned *amax = (unsigned *)(sc + 4);
   cudaStream_t st = ctx()->stream;
-  KtScope kt("lp_pack", 0.0, 6.0 * m * nb);
+  KtScope kt("lp_pack", 0.0, (split ? 8.0 : 6.0) * m * nb);
   dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
   if (lp == 1) {
     pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
@@ -175,11 +216,13 @@ int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
     u12_amax_kernel<<<grid_cap((int64_t)nb * m), 256, 0, st>>>(L21, lda, (int)m,
                                                                 nb, amax);
     MGB_LAUNCHED("l21_amax");
-    pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc);
+    pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc,
+                                          A16lo);
   }
   MGB_LAUNCHED("pack_l21");
   return tc_gemm(lp == 1, m, m, Kp, A16, Kp, A16, Kp, -1.f,
-                 lp == 0 ? sc + 2 : nullptr, 1.f, C22, ldc, 1, info);
+                 lp != 1 ? sc + 2 : nullptr, 1.f, C22, ldc, 1, info, A16lo,
+                 A16lo);
 }
 
 // ---- refinement kernels ------------------------------------------------------------
@@ -305,9 +348,10 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (not_spd) *not_spd = 0;
   if (n <= 0 || nrhs <= 0) return 0;
-  if (o.lp_format < -1 || o.lp_format > 1)
+  if (o.lp_format < -1 || o.lp_format > 2)
     return set_error(MATGB_ERR_ARG,
-                     "lp_format must be 1 (BF16), 0 (FP16) or -1 (FP32)");
+                     "lp_format must be 2 (FP16 split), 1 (BF16), 0 (FP16) or "
+                     "-1 (FP32)");
   if (!g_ir.ready) {
     for (auto &e : g_ir.e) MGB_CUDA(cudaEventCreate(&e));
     g_ir.ready = true;
@@ -349,7 +393,7 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   const bool use_krylov = o.krylov != 0 && nrhs == 1;
   const int kdim = o.krylov_dim > 0 ? (o.krylov_dim < kKrylovMaxDim ? o.krylov_dim
                                                                     : kKrylovMaxDim)
-                                    : 40;
+                                    : 50;
   float ms_factor = 0.f;
   for (int attempt = 0; attempt < 2; attempt++) {
     MGB_CUDA(cudaEventRecord(g_ir.e[0], st));
@@ -400,10 +444,16 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
         // residual that meets the backward-error target with room to spare
         const double atol =
             refinements == 0 ? 0.0 : 0.25 * tol * (anorm * xn_known + bn[0]);
+        // with 16-bit factors and a fallback available, a first cycle that
+        // has not gained three orders of magnitude in 24 steps gives up
+        int stalled = 0;
+        const bool may_abort = lp >= 0 && o.fp32_fallback && refinements == 0;
         MGB_TRY(fgmres_cycle(spd, n, A, lda, W, piv + n, V, Z, RF, mcap, 1e-10,
-                             atol, D, &inner, &est));
+                             atol, may_abort ? 24 : 1 << 30, 1e-3, D, &inner,
+                             &est, &stalled));
         it += inner;
         ksteps += inner;
+        if (stalled) break;
         add_vec_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, X, D);
         MGB_LAUNCHED("add_vec");
         refinements++;
@@ -425,7 +475,7 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
           converged = 1;
           break;
         }
-        if (!(eta < 0.5 * prev)) break;  // stagnation or divergence
+        if (!(eta < 0.9 * prev)) break;  // stagnation or divergence
         prev = eta;
       }
     }
@@ -521,18 +571,18 @@ using namespace mgb;
 extern "C" {
 
 void matgb_ir_default_opts(MatIROpts *o) {
-  o->lp_format = 1;
+  o->lp_format = 2;
   o->max_iter = 100;
   o->tol = 0.0;
   o->fp32_fallback = 1;
   o->krylov = 1;
-  o->krylov_dim = 40;
+  o->krylov_dim = 50;
 }
 
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
                        int32_t *perm, int lp_format) {
   if (lda < n) return set_error(MATGB_ERR_ARG, "getrf_lp: lda < n");
-  if (lp_format < -1 || lp_format > 1)
+  if (lp_format < -1 || lp_format > 2)
     return set_error(MATGB_ERR_ARG, "getrf_lp: lp_format");
   return getrf_t<float>((int64_t)n, A, (int64_t)lda, ipiv, perm, 0.f,
                         lp_format);

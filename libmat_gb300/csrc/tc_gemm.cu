@@ -7,18 +7,27 @@
 // update (mat.h:6021-6023): the bulk of the FLOPs run on the 5th-generation
 // tensor cores with FP32 accumulation in TMEM, the trailing matrix stays FP32.
 //
+// Split form (three products): with A = Ah + Al and B = Bh + Bl (16-bit hi
+// parts and the rounding remainders), A B^T ~= Ah Bh^T + Ah Bl^T + Al Bh^T,
+// the dropped Al Bl^T being ~2^-22 of the product -- FP32-level updates from
+// FP16 tensor cores.  The three products are one GEMM over a K axis of three
+// segments, [Ah|Ah|Al] . [Bh|Bl|Bh]^T: the producer picks the hi or lo tensor
+// map per segment, so C is read and written once.
+//
 // One CTA computes one 128 x 256 tile (UMMA M=128, N=256, K=16, cta_group::1):
-//   warp 8  : TMA producer -- K/64 loads of a 128x64 A box and a 256x64 B box
-//             (128-byte swizzle), one mbarrier per 64-wide K block;
-//   warp 9  : TMEM allocator and single-thread MMA issuer (4 MMAs per K block),
-//             then tcgen05.commit to the "accumulator ready" mbarrier;
-//   warps 0-7: epilogue -- tcgen05.ld 32 columns at a time from TMEM (warp w
+//   warp 8  : TMA producer -- for each 64-wide K block a 128x64 A box and a
+//             256x64 B box (128-byte swizzle) into a 2-stage ring (full /
+//             empty mbarriers);
+//   warp 9  : TMEM allocator and single-thread MMA issuer (4 MMAs per K
+//             block, tcgen05.commit to the stage's empty barrier), then a
+//             final commit to the "accumulator ready" mbarrier;
+//   warps 0-7: epilogue -- tcgen05.ld 16 columns at a time from TMEM (warp w
 //             reads lane quarter w%4, column half w/4), then a coalesced
 //             read-modify-write of C (consecutive lanes = consecutive rows).
-// K <= 128 keeps the whole K extent resident (96 KB of smem), so two CTAs fit
-// per SM and one CTA's epilogue overlaps the other's loads and MMAs.
-// Every wait is bounded; on a timeout the CTA records an error flag, stops
-// issuing work, still frees its TMEM and returns.
+// 96 KB of smem, so two CTAs fit per SM and one CTA's epilogue overlaps the
+// other's loads and MMAs.  Every wait is bounded; on a timeout the CTA records
+// an error flag, stops issuing work, waits (bounded) for its copies in
+// flight, still frees its TMEM and returns.
 #include <cudaTypedefs.h>
 
 #include "internal.cuh"
@@ -27,24 +36,30 @@
 namespace mgb {
 
 constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 64;
-constexpr int kTcMaxK = 128;
-constexpr int kTcKB = kTcMaxK / kTcBK;
+constexpr int kTcStages = 2;
+constexpr int kTcMaxKB = 64;  // K blocks per launch (all segments)
 constexpr int kTcThreads = 320;
 constexpr uint32_t kTcWaitLimit = 1u << 24;  // ~1.5 s of polling
 
 struct TcSmem {
   // 1024-byte aligned swizzle atoms
-  uint16_t a[kTcKB][kTcBM * kTcBK];
-  uint16_t b[kTcKB][kTcBN * kTcBK];
-  uint64_t full[kTcKB];
+  uint16_t a[kTcStages][kTcBM * kTcBK];
+  uint16_t b[kTcStages][kTcBN * kTcBK];
+  uint64_t full[kTcStages];
+  uint64_t empty[kTcStages];
   uint64_t done;
   uint32_t tmem_base;
-  int timeout;
+  volatile int timeout;
 };
 
+// Segment s of the K axis (kps K blocks each) reads A from tmA1 when bit s of
+// amask is set (else tmA0), B likewise with bmask.
 __global__ void __launch_bounds__(kTcThreads, 2)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
-                   const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0,
+                   const __grid_constant__ CUtensorMap tmA1,
+                   const __grid_constant__ CUtensorMap tmB0,
+                   const __grid_constant__ CUtensorMap tmB1, int M, int N,
+                   int kps, int nseg, unsigned amask, unsigned bmask,
                    float alpha, const float *__restrict__ alpha_scale,
                    float beta, float *__restrict__ C, int64_t ldc,
                    uint32_t idesc, int lower, const int32_t *__restrict__ skip,
@@ -55,7 +70,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
-  const int nkb = K / kTcBK;
+  const int nkb = kps * nseg;
   // whole-CTA exits before any barrier or TMEM allocation: a failed earlier
   // step (skip flag) or, for a lower-triangular update, a tile strictly above
   // the diagonal
@@ -63,7 +78,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   if (lower && n0 >= m0 + kTcBM) return;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < kTcKB; i++) tc::mbar_init(&s.full[i], 1);
+    for (int i = 0; i < kTcStages; i++) {
+      tc::mbar_init(&s.full[i], 1);
+      tc::mbar_init(&s.empty[i], 1);
+    }
     tc::mbar_init(&s.done, 1);
     s.timeout = 0;
     tc::fence_barrier_init();
@@ -75,23 +93,38 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const uint32_t tmem = s.tmem_base;
 
   if (warp == 8 && lane == 0) {
-    tc::prefetch_tmap(&tmA);
-    tc::prefetch_tmap(&tmB);
+    tc::prefetch_tmap(&tmA0);
+    tc::prefetch_tmap(&tmB0);
+    int issued = 0;
     for (int kb = 0; kb < nkb; kb++) {
-      tc::mbar_arrive_expect_tx(&s.full[kb],
-                                (kTcBM + kTcBN) * kTcBK * 2);
-      tc::tma_load_2d(s.a[kb], &tmA, kb * kTcBK, m0, &s.full[kb]);
-      tc::tma_load_2d(s.b[kb], &tmB, kb * kTcBK, n0, &s.full[kb]);
+      const int st = kb % kTcStages, use = kb / kTcStages;
+      if (use > 0 && !tc::mbar_wait(&s.empty[st], (use - 1) & 1, kTcWaitLimit)) {
+        s.timeout = 1;
+        break;
+      }
+      if (s.timeout) break;
+      const int seg = kb / kps, kx = (kb % kps) * kTcBK;
+      const CUtensorMap *ma = ((amask >> seg) & 1) ? &tmA1 : &tmA0;
+      const CUtensorMap *mb = ((bmask >> seg) & 1) ? &tmB1 : &tmB0;
+      tc::mbar_arrive_expect_tx(&s.full[st], (kTcBM + kTcBN) * kTcBK * 2);
+      tc::tma_load_2d(s.a[st], ma, kx, m0, &s.full[st]);
+      tc::tma_load_2d(s.b[st], mb, kx, n0, &s.full[st]);
+      issued = kb + 1;
     }
+    // no copy may still be in flight when the CTA leaves: wait (bounded) for
+    // the last load issued into each stage
+    for (int kb = issued - kTcStages > 0 ? issued - kTcStages : 0; kb < issued; kb++)
+      tc::mbar_wait(&s.full[kb % kTcStages], (kb / kTcStages) & 1, kTcWaitLimit);
   } else if (warp == 9 && lane == 0) {
     bool ok = true;
-    for (int kb = 0; kb < nkb && ok; kb++) {
-      if (!tc::mbar_wait(&s.full[kb], 0, kTcWaitLimit)) {
+    for (int kb = 0; kb < nkb; kb++) {
+      const int st = kb % kTcStages, use = kb / kTcStages;
+      if (s.timeout || !tc::mbar_wait(&s.full[st], use & 1, kTcWaitLimit)) {
         ok = false;
         break;
       }
       tc::tc_fence_after();
-      const uint32_t a0 = tc::smem_u32(s.a[kb]), b0 = tc::smem_u32(s.b[kb]);
+      const uint32_t a0 = tc::smem_u32(s.a[st]), b0 = tc::smem_u32(s.b[st]);
 #pragma unroll
       for (int kk = 0; kk < kTcBK / 16; kk++) {
         // advance 16 elements (32 bytes) along K inside the 128-byte atom
@@ -99,17 +132,16 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         const uint64_t bd = tc::desc_k_sw128(b0 + kk * 32);
         tc::mma_f16(tmem, ad, bd, idesc, (kb | kk) ? 1u : 0u);
       }
+      tc::mma_commit(&s.empty[st]);  // the stage is free once these finish
     }
     if (ok) {
       tc::mma_commit(&s.done);
     } else {
+      // the commit still fires once the MMAs already issued have finished,
+      // so TMEM is not freed under them
       s.timeout = 1;
       atomicExch(err, 1);
-      // wait (bounded) for the TMA copies still in flight before leaving
-      for (int kb = 0; kb < nkb; kb++) tc::mbar_wait(&s.full[kb], 0, kTcWaitLimit);
-      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
-                       tc::smem_u32(&s.done))
-                   : "memory");
+      tc::mma_commit(&s.done);
     }
   } else if (warp < 8) {
     // Epilogue: warp w reads TMEM lane quarter w%4 (rows q*32..q*32+31) and
@@ -210,31 +242,45 @@ static int make_map(CUtensorMap *m, const void *ptr, int bf16, int64_t rows,
 }
 
 // C = beta*C + alpha*(*alpha_scale if given)*A*B^T.  A: M x K, B: N x K,
-// K-contiguous 16-bit (bf16 != 0: BF16, else FP16); K a multiple of 64 and
-// <= 128; lda, ldb multiples of 8 elements; 16-byte aligned bases.
+// K-contiguous 16-bit (bf16 != 0: BF16, else FP16); K a multiple of 64;
+// lda, ldb multiples of 8 elements; 16-byte aligned bases.  With Alo and Blo
+// (the remainders A - Ah, B - Bh, same layout) the three-product split form.
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
-            int lower, const int32_t *skip) {
+            int lower, const int32_t *skip, const void *Alo, const void *Blo) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (M <= 0 || N <= 0) return 0;
-  if (K <= 0 || K % kTcBK || K > kTcMaxK || lda % 8 || ldb % 8 ||
-      ((uintptr_t)A & 15) || ((uintptr_t)B & 15) || M > INT32_MAX ||
+  const bool split = Alo && Blo;
+  const int nseg = split ? 3 : 1;
+  if (K <= 0 || K % kTcBK || (K / kTcBK) * nseg > kTcMaxKB || lda % 8 ||
+      ldb % 8 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15) ||
+      ((uintptr_t)Alo & 15) || ((uintptr_t)Blo & 15) || M > INT32_MAX ||
       N > INT32_MAX)
     return set_error(MATGB_ERR_ARG, "tc_gemm: unsupported shape/alignment");
   MGB_TRY(tc_setup());
-  CUtensorMap ma, mb;
+  CUtensorMap ma, mb, mal, mbl;
   MGB_TRY(make_map(&ma, A, bf16, M, K, lda, kTcBM));
   MGB_TRY(make_map(&mb, B, bf16, N, K, ldb, kTcBN));
+  if (split) {
+    MGB_TRY(make_map(&mal, Alo, bf16, M, K, lda, kTcBM));
+    MGB_TRY(make_map(&mbl, Blo, bf16, N, K, ldb, kTcBN));
+  } else {
+    mal = ma;
+    mbl = mb;
+  }
   dim3 grid((unsigned)((M + kTcBM - 1) / kTcBM), (unsigned)((N + kTcBN - 1) / kTcBN));
   const uint32_t idesc = tc::idesc_f16(bf16 ? 1 : 0, kTcBM, kTcBN);
   const double frac = lower ? 0.5 : 1.0;
-  KtScope kt("tc_gemm", 2.0 * M * N * K * frac,
-             4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N * frac + 2.0 * (M + N) * K);
+  // segments: [Ah|Ah|Al] . [Bh|Bl|Bh]
+  const unsigned amask = split ? 4u : 0u, bmask = split ? 2u : 0u;
+  KtScope kt(split ? "tc_gemm_split" : "tc_gemm", 2.0 * M * N * K * frac * nseg,
+             4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N * frac +
+                 2.0 * (M + N) * K * (split ? 2 : 1));
   tc_gemm_kernel<<<grid, kTcThreads, sizeof(TcSmem) + 1024, cx->stream>>>(
-      ma, mb, (int)M, (int)N, (int)K, alpha, alpha_scale, beta, C, ldc, idesc,
-      lower, skip, g_tc_err);
+      ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,
+      alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, g_tc_err);
   MGB_LAUNCHED("tc_gemm");
   return 0;
 }
@@ -259,7 +305,18 @@ int matgb_tc_gemm_dev(int bf16, size_t M, size_t N, size_t K, const void *A,
   if (ldc < M) return set_error(MATGB_ERR_ARG, "tc_gemm: ldc < M");
   return tc_gemm(bf16, (int64_t)M, (int64_t)N, (int64_t)K, A, (int64_t)lda, B,
                  (int64_t)ldb, alpha, nullptr, beta, C, (int64_t)ldc, 0,
-                 nullptr);
+                 nullptr, nullptr, nullptr);
+}
+
+int matgb_tc_gemm_split_dev(size_t M, size_t N, size_t K, const void *Ah,
+                            const void *Al, size_t lda, const void *Bh,
+                            const void *Bl, size_t ldb, float alpha, float beta,
+                            float *C, size_t ldc) {
+  if (ldc < M) return set_error(MATGB_ERR_ARG, "tc_gemm_split: ldc < M");
+  if (!Al || !Bl) return set_error(MATGB_ERR_ARG, "tc_gemm_split: null remainder");
+  return tc_gemm(0, (int64_t)M, (int64_t)N, (int64_t)K, Ah, (int64_t)lda, Bh,
+                 (int64_t)ldb, alpha, nullptr, beta, C, (int64_t)ldc, 0,
+                 nullptr, Al, Bl);
 }
 
 int matgb_tc_status(void) {

@@ -2,22 +2,29 @@
 // mat_solve_tril / _tril_unit / _triu / _trilt kernels, mat.h:4580-4803, and
 // every refinement step of the mixed-precision solvers).
 //
-// One CTA per 64-row block of x.  CTAs take blocks in the order they start
-// (atomic ticket), so a block only ever waits on blocks owned by CTAs that
-// are already running: no deadlock whatever the residency.  A CTA folds in
-// the off-diagonal tiles T_bj x_j as their x_j blocks become ready (per-block
-// flags, checked for a whole range at a time), then solves its 64x64 diagonal
-// block with one warp (x_k broadcast by shuffle, non-unit diagonals divided
-// by), publishes x_b and raises its flag.  Flags carry an epoch so they never
-// need clearing.  Every wait is bounded: after ~1 s the CTA records an error
-// flag and returns.
+// One CTA per RB-row block of x (RB = 64 or 128, 4*RB threads).  CTAs take
+// blocks in the order they start (atomic ticket), so a block only ever waits
+// on blocks owned by CTAs that are already running: no deadlock whatever the
+// residency.  The critical path is the chain of diagonal solves, so
+// everything that does not depend on x happens before the wait: the CTA
+// stages its diagonal block and the reciprocals of its diagonal in shared
+// memory and loads the matrix entries of its next off-diagonal tile into
+// registers.  It then folds in the tiles T_bj x_j as their x_j blocks become
+// ready (one thread waits on the next flag, all threads then count how many
+// more are ready), solves its diagonal block with one warp (x_k broadcast by
+// shuffle, multiplication by the staged reciprocal), publishes x_b and raises
+// its flag.  Flags carry an epoch so they never need clearing.  Every wait is
+// bounded: after ~1 s the CTA records an error flag and returns.
+//
+// Tile mapping (coalesced either way): op(T) = T, thread (row rr, group g)
+// takes columns g*RB/4 .. +RB/4 of row rr; op(T) = T^T (memory contiguous
+// along op's columns), warp w takes rows w, w+NW, ... with lanes across
+// columns, and the per-row sums are reduced across lanes once at the end.
 #include "internal.cuh"
 
 namespace mgb {
 
-constexpr int kTvRows = 64;
-constexpr int kTvThreads = 256;
-constexpr uint32_t kTvSpinLimit = 1u << 20;  // ~1 s of polling
+constexpr uint32_t kTvSpinLimit = 1u << 22;  // ~1 s of polling
 
 struct TvState {
   int ticket;
@@ -35,162 +42,210 @@ __device__ __forceinline__ void st_release(int *p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+template <typename T, int RB>
+struct TvSmem {
+  T Dg[RB][RB + 1];  // diagonal block of op(T), row-major
+  T rd[RB];          // reciprocals of its diagonal
+  T part[4][RB];     // partial sums (op(T) = T)
+  T xs[RB];
+};
+
 // EL: op(T) lower (forward); TR: op(T) = T^T; UNIT: unit diagonal.
-template <typename T, bool EL, bool TR, bool UNIT>
-__global__ void __launch_bounds__(kTvThreads)
+template <typename T, int RB, bool EL, bool TR, bool UNIT>
+__global__ void __launch_bounds__(4 * RB)
     trsv_kernel(int64_t n, const T *__restrict__ Tm, int64_t ldt,
                 T *__restrict__ x, int *__restrict__ flags,
                 TvState *__restrict__ stt, int epoch) {
-  __shared__ int sb;
-  __shared__ int s_ready;
-  __shared__ T part[4][kTvRows];
-  __shared__ T Dg[kTvRows][kTvRows + 1];
-  __shared__ T xs[kTvRows];
+  constexpr int NT = 4 * RB;
+  constexpr int NW = NT / 32;
+  constexpr int CPT = RB / 4;      // tile entries per thread
+  constexpr int RPW = RB / NW;     // TR: rows per warp (8)
+  constexpr int LPC = RB / 32;     // TR: columns per lane (2 or 4)
+  extern __shared__ __align__(16) unsigned char tv_raw[];
+  TvSmem<T, RB> &sm = *reinterpret_cast<TvSmem<T, RB> *>(tv_raw);
+  __shared__ int sb, s_fail;
+  __shared__ int s_ready[2];  // by iteration parity: reset and read never race
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nb = (int)((n + kTvRows - 1) / kTvRows);
-  if (tid == 0) sb = atomicAdd(&stt->ticket, 1);
+  const int nb = (int)((n + RB - 1) / RB);
+  if (tid == 0) {
+    sb = atomicAdd(&stt->ticket, 1);
+    s_fail = 0;
+  }
   __syncthreads();
   const int t = sb;
   if (t >= nb) return;
   const int b = EL ? t : nb - 1 - t;
-  const int64_t r0 = (int64_t)b * kTvRows;
-  const int rows = (int)((n - r0) < kTvRows ? (n - r0) : kTvRows);
-  // op(T)(i, j) in memory
+  const int64_t r0 = (int64_t)b * RB;
+  const int rows = (int)((n - r0) < RB ? (n - r0) : RB);
   auto el = [&](int64_t i, int64_t j) -> T {
     return TR ? Tm[j + i * ldt] : Tm[i + j * ldt];
   };
+  // stage the diagonal block (coalesced: contiguous index fastest)
+  for (int e = tid; e < RB * RB; e += NT) {
+    const int i = TR ? e / RB : e % RB, j = TR ? e % RB : e / RB;
+    sm.Dg[i][j] = (i < rows && j < rows) ? el(r0 + i, r0 + j) : T(0);
+  }
+  __syncthreads();
+  if (!UNIT && tid < RB) sm.rd[tid] = tid < rows ? T(1) / sm.Dg[tid][tid] : T(1);
 
-  // partial sums: thread (rr = tid % 64, grp = tid / 64) for !TR, or
-  // (cc = tid % 64, grp = tid / 64) for TR
-  T acc[kTvRows / 4];
-#pragma unroll
-  for (int q = 0; q < kTvRows / 4; q++) acc[q] = T(0);
-  T accr = T(0);
-  int done = 0;  // number of off-diagonal blocks folded in, in solve order
   const int need = t;  // blocks before this one in solve order
-  uint32_t spins = 0;
-  bool failed = false;
+  auto tile_col0 = [&](int k) -> int64_t {
+    return (int64_t)(EL ? k : nb - 1 - k) * RB;
+  };
+  // the off-diagonal entries of tile k this thread folds in
+  auto load_tile = [&](int k, T (&v)[CPT]) {
+    const int64_t c0 = tile_col0(k);
+    const int cols = (int)((n - c0) < RB ? (n - c0) : RB);
+    if (!TR) {
+      const int rr = tid % RB, g = tid / RB;
+#pragma unroll
+      for (int q = 0; q < CPT; q++) {
+        const int c = g * CPT + q;
+        v[q] = (rr < rows && c < cols) ? el(r0 + rr, c0 + c) : T(0);
+      }
+    } else {
+#pragma unroll
+      for (int a = 0; a < RPW; a++) {
+        const int r = warp + a * NW;
+#pragma unroll
+        for (int m = 0; m < LPC; m++) {
+          const int c = lane + 32 * m;
+          v[a * LPC + m] = (r < rows && c < cols) ? el(r0 + r, c0 + c) : T(0);
+        }
+      }
+    }
+  };
+  T cur[CPT], nxt[CPT];
+  T acc[TR ? RPW : 1];
+#pragma unroll
+  for (int a = 0; a < (TR ? RPW : 1); a++) acc[a] = T(0);
+  if (need > 0) load_tile(0, cur);
+
+  int done = 0, par = 0;
   while (done < need) {
-    // how many consecutive blocks (in solve order) are ready from `done`
-    if (tid == 0) s_ready = 0x7fffffff;
+    // wait for tile `done`, then count the ready tiles after it
+    if (tid == 0) {
+      const int jb = EL ? done : nb - 1 - done;
+      uint32_t spins = 0;
+      while (ld_acquire(&flags[jb]) != epoch) {
+        if (++spins > kTvSpinLimit) {
+          s_fail = 1;
+          break;
+        }
+        __nanosleep(32);
+      }
+      s_ready[par] = 0x7fffffff;
+    }
     __syncthreads();
-    {
-      const int k = done + tid;
+    if (s_fail) break;
+    if (need - done > 1) {  // more than one tile pending: count the ready ones
+      const int k = done + 1 + tid;
       int ok = 0;
-      if (k < need) {
-        const int jb = EL ? k : nb - 1 - k;
-        ok = ld_acquire(&flags[jb]) == epoch;
-      }
-      // first not-ready position among the 256 checked
-      unsigned bal = __ballot_sync(0xffffffffu, !ok && k < need);
-      if (lane == 0) atomicMin(&s_ready, warp * 32 + (bal ? __ffs(bal) - 1 : 32));
+      if (k < need) ok = ld_acquire(&flags[EL ? k : nb - 1 - k]) == epoch;
+      const unsigned bal = __ballot_sync(0xffffffffu, !ok && k < need);
+      if (lane == 0 && (bal || warp == NW - 1))
+        atomicMin(&s_ready[par], warp * 32 + (bal ? __ffs(bal) - 1 : 32));
+      __syncthreads();
     }
-    __syncthreads();
-    int ready = s_ready;
+    int ready = need - done > 1 ? 1 + s_ready[par] : 1;
+    par ^= 1;
     if (ready > need - done) ready = need - done;
-    if (ready == 0) {
-      if (++spins > kTvSpinLimit) {
-        failed = true;
-        break;
-      }
-      __nanosleep(100);
-      continue;
-    }
     for (int q = 0; q < ready; q++) {
       const int k = done + q;
-      const int jb = EL ? k : nb - 1 - k;
-      const int64_t c0 = (int64_t)jb * kTvRows;
-      const int cols = (int)((n - c0) < kTvRows ? (n - c0) : kTvRows);
+      if (k + 1 < need) load_tile(k + 1, nxt);
+      const int64_t c0 = tile_col0(k);
       if (!TR) {
-        // thread: row rr, columns grp*16 .. +16 (coalesced down a column)
-        const int rr = tid % kTvRows, grp = tid / kTvRows;
-        if (rr < rows) {
-#pragma unroll 4
-          for (int c = grp * 16; c < grp * 16 + 16; c++)
-            if (c < cols) accr = fma(el(r0 + rr, c0 + c), __ldcg(&x[c0 + c]), accr);
+        const int g = tid / RB;
+#pragma unroll
+        for (int qq = 0; qq < CPT; qq++) {
+          const int64_t c = c0 + g * CPT + qq;
+          const T xv = c < n ? __ldcg(&x[c]) : T(0);
+          acc[0] = fma(cur[qq], xv, acc[0]);
         }
       } else {
-        // thread: column cc, rows grp*16 .. +16 (coalesced along cc)
-        const int cc = tid % kTvRows, grp = tid / kTvRows;
-        if (cc < cols) {
-          const T xc = __ldcg(&x[c0 + cc]);
+        T xv[LPC];
 #pragma unroll
-          for (int q2 = 0; q2 < kTvRows / 4; q2++) {
-            const int r = grp * 16 + q2;
-            if (r < rows) acc[q2] = fma(el(r0 + r, c0 + cc), xc, acc[q2]);
+        for (int m = 0; m < LPC; m++) {
+          const int64_t c = c0 + lane + 32 * m;
+          xv[m] = c < n ? __ldcg(&x[c]) : T(0);
+        }
+#pragma unroll
+        for (int a = 0; a < RPW; a++)
+#pragma unroll
+          for (int m = 0; m < LPC; m++) acc[a] = fma(cur[a * LPC + m], xv[m], acc[a]);
+      }
+#pragma unroll
+      for (int qq = 0; qq < CPT; qq++) cur[qq] = nxt[qq];
+    }
+    done += ready;
+  }
+  if (s_fail) {
+    if (tid == 0) atomicExch(&stt->err, 1);
+    return;
+  }
+  // s = b - (sum of the folded tiles) for the block's rows
+  if (!TR) {
+    sm.part[tid / RB][tid % RB] = acc[0];
+  } else {
+#pragma unroll
+    for (int a = 0; a < RPW; a++) {
+      T v = acc[a];
+      for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0) sm.part[0][warp + a * NW] = v;
+    }
+  }
+  __syncthreads();
+  if (tid < RB) {
+    T s = T(0);
+    if (tid < rows) {
+      s = sm.part[0][tid];
+      if (!TR) s += sm.part[1][tid] + sm.part[2][tid] + sm.part[3][tid];
+      s = __ldcg(&x[r0 + tid]) - s;
+    }
+    sm.xs[tid] = s;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    constexpr int YR = RB / 32;  // rows per lane
+    T y[YR];
+#pragma unroll
+    for (int m = 0; m < YR; m++) y[m] = sm.xs[lane + 32 * m];
+    if (EL) {
+#pragma unroll
+      for (int m0 = 0; m0 < YR; m0++) {
+#pragma unroll 8
+        for (int kk = 0; kk < 32; kk++) {
+          const int k = m0 * 32 + kk;
+          if (k < rows) {
+            T yk = __shfl_sync(0xffffffffu, y[m0], kk);
+            if (!UNIT) yk *= sm.rd[k];
+            if (lane == kk) y[m0] = yk;
+#pragma unroll
+            for (int m = 0; m < YR; m++)
+              if (lane + 32 * m > k) y[m] = fma(-sm.Dg[lane + 32 * m][k], yk, y[m]);
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int m0 = YR - 1; m0 >= 0; m0--) {
+#pragma unroll 8
+        for (int kk = 31; kk >= 0; kk--) {
+          const int k = m0 * 32 + kk;
+          if (k < rows) {
+            T yk = __shfl_sync(0xffffffffu, y[m0], kk);
+            if (!UNIT) yk *= sm.rd[k];
+            if (lane == kk) y[m0] = yk;
+#pragma unroll
+            for (int m = 0; m < YR; m++)
+              if (lane + 32 * m < k) y[m] = fma(-sm.Dg[lane + 32 * m][k], yk, y[m]);
           }
         }
       }
     }
-    done += ready;
-  }
-  if (failed) {
-    if (tid == 0) atomicExch(&stt->err, 1);
-    return;
-  }
-  // reduce partial sums to s[r] for the block's rows
-  if (!TR) {
-    part[tid / kTvRows][tid % kTvRows] = accr;
-  } else {
-    // sum over cc: 64 threads (2 warps) per row group; rows grp*16+q2
-    const int grp = tid / kTvRows;
 #pragma unroll
-    for (int q2 = 0; q2 < kTvRows / 4; q2++) {
-      T v = acc[q2];
-      for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-      acc[q2] = v;
-    }
-    __syncthreads();
-    if (lane == 0) {
-      const int half = (tid % kTvRows) / 32;  // which warp of the pair
-#pragma unroll
-      for (int q2 = 0; q2 < kTvRows / 4; q2++) Dg[grp * 16 + q2][half] = acc[q2];
-    }
-    __syncthreads();
-    if (tid < kTvRows) part[0][tid] = Dg[tid][0] + Dg[tid][1];
-    if (tid < kTvRows) part[1][tid] = part[2][tid] = part[3][tid] = T(0);
-  }
-  __syncthreads();
-  // diagonal block into shared memory
-  for (int e = tid; e < kTvRows * kTvRows; e += kTvThreads) {
-    const int i = e % kTvRows, j = e / kTvRows;
-    Dg[i][j] = (i < rows && j < rows) ? el(r0 + i, r0 + j) : T(0);
-  }
-  if (tid < kTvRows)
-    xs[tid] = tid < rows ? __ldcg(&x[r0 + tid]) - (part[0][tid] + part[1][tid] +
-                                          part[2][tid] + part[3][tid])
-                         : T(0);
-  __syncthreads();
-  if (warp == 0) {
-    T y0 = xs[lane], y1 = xs[lane + 32];
-    if (EL) {
-#pragma unroll 4
-      for (int k = 0; k < kTvRows; k++) {
-        if (k >= rows) break;
-        const int own = k & 31;
-        T yk = __shfl_sync(0xffffffffu, k < 32 ? y0 : y1, own);
-        if (!UNIT) yk = yk / Dg[k][k];
-        if (lane == own) {
-          if (k < 32) y0 = yk; else y1 = yk;
-        }
-        if (lane > k) y0 = fma(-Dg[lane][k], yk, y0);
-        if (lane + 32 > k) y1 = fma(-Dg[lane + 32][k], yk, y1);
-      }
-    } else {
-      for (int k = kTvRows - 1; k >= 0; k--) {
-        if (k >= rows) continue;
-        const int own = k & 31;
-        T yk = __shfl_sync(0xffffffffu, k < 32 ? y0 : y1, own);
-        if (!UNIT) yk = yk / Dg[k][k];
-        if (lane == own) {
-          if (k < 32) y0 = yk; else y1 = yk;
-        }
-        if (lane < k) y0 = fma(-Dg[lane][k], yk, y0);
-        if (lane + 32 < k) y1 = fma(-Dg[lane + 32][k], yk, y1);
-      }
-    }
-    if (lane < rows) x[r0 + lane] = y0;
-    if (lane + 32 < rows) x[r0 + lane + 32] = y1;
+    for (int m = 0; m < YR; m++)
+      if (lane + 32 * m < rows) x[r0 + lane + 32 * m] = y[m];
     __syncwarp();
     if (lane == 0) {
       __threadfence();
@@ -207,9 +262,9 @@ struct TvBufs {
 };
 static TvBufs g_tv;
 
-template <typename T, bool EL, bool TR, bool UNIT>
+template <typename T, int RB, bool EL, bool TR, bool UNIT>
 static int launch_trsv(int64_t n, const T *Tm, int64_t ldt, T *x) {
-  const int nb = (int)((n + kTvRows - 1) / kTvRows);
+  const int nb = (int)((n + RB - 1) / RB);
   if (g_tv.cap < nb) {
     if (g_tv.flags) {
       cudaStreamSynchronize(ctx()->stream);
@@ -223,13 +278,19 @@ static int launch_trsv(int64_t n, const T *Tm, int64_t ldt, T *x) {
     g_tv.epoch = 0;
   }
   g_tv.epoch++;
+  auto k = trsv_kernel<T, RB, EL, TR, UNIT>;
+  const size_t smem = sizeof(TvSmem<T, RB>);
+  MGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
   MGB_CUDA(cudaMemsetAsync(&g_tv.st->ticket, 0, sizeof(int), ctx()->stream));
   KtScope kt("trsv", (double)n * n, (double)sizeof(T) * n * n / 2.0);
-  trsv_kernel<T, EL, TR, UNIT><<<nb, kTvThreads, 0, ctx()->stream>>>(
-      n, Tm, ldt, x, g_tv.flags, g_tv.st, g_tv.epoch);
-  MGB_LAUNCHED("trsv");
-  return 0;
+  k<<<nb, 4 * RB, smem, ctx()->stream>>>(n, Tm, ldt, x, g_tv.flags, g_tv.st,
+                                         g_tv.epoch);
+  return launch_check((const void *)k, "trsv", smem);
 }
+
+// Block rows: 128 once the chain of diagonal solves (n / RB steps) is long.
+static int g_tv_rb_override = 0;
 
 template <typename T>
 int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
@@ -237,9 +298,16 @@ int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
   if (!ctx()) return MATGB_ERR_NO_DEVICE;
   if (n <= 0) return 0;
   const bool el = lower != trans;
+  // 128-row blocks (512 threads) only in float: the double tiles would not
+  // fit the 128 registers a thread may then use
+  int rb = g_tv_rb_override ? g_tv_rb_override : (n >= 4096 ? 128 : 64);
+  if (sizeof(T) != 4) rb = 64;
 #define MGB_TV(E, R, U)                                                        \
-  if (el == E && trans == R && unit == U)                                      \
-    return launch_trsv<T, E, R, U>(n, Tm, ldt, x);
+  if (el == E && trans == R && unit == U) {                                    \
+    if constexpr (sizeof(T) == 4)                                              \
+      if (rb == 128) return launch_trsv<T, 128, E, R, U>(n, Tm, ldt, x);       \
+    return launch_trsv<T, 64, E, R, U>(n, Tm, ldt, x);                         \
+  }
   MGB_TV(true, false, false)
   MGB_TV(true, false, true)
   MGB_TV(true, true, false)
@@ -269,3 +337,11 @@ int trsv_status() {
 }
 
 }  // namespace mgb
+
+// Block-row size of the single-launch triangular solve (64 or 128; 0 picks
+// by size).  For measurement.
+extern "C" int matgb_trsv_block_rows(int rb) {
+  if (rb != 0 && rb != 64 && rb != 128) return MATGB_ERR_ARG;
+  mgb::g_tv_rb_override = rb;
+  return 0;
+}
