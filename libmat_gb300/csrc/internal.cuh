@@ -148,12 +148,17 @@ int tc_error_flag(int clear);
 constexpr int kKrylovMaxDim = 64;
 constexpr int kKrylovMaxParts = 64;
 // A cycle that has not reduced the residual estimate below abort_ratio * |r0|
-// after abort_after steps stops early with *stalled = 1.
+// after abort_after steps stops early with *stalled = 1.  With tg (a cycle
+// starting from x = 0) the cycle also stops once the residual estimate meets
+// tol * (anorm * |d|_inf + bnorm) / 4, |d| checked every 8 steps.
+struct KrylovTarget {
+  double tol, anorm, bnorm;
+};
 int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
                  const float *W, const int32_t *perm, elem_t *V, elem_t *Z,
                  float *F, int m, double rtol, double atol, int abort_after,
-                 double abort_ratio, elem_t *d, int *inner, double *res_est,
-                 int *stalled);
+                 double abort_ratio, const KrylovTarget *tg, elem_t *d,
+                 int *inner, double *res_est, int *stalled);
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm);
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,
           const int32_t *perm, const elem_t *B, int64_t ldb, elem_t *X,

@@ -118,6 +118,34 @@ __global__ void __launch_bounds__(kKrylovThreads)
   if (threadIdx.x == 0) norm_part[blockIdx.x] = ss;
 }
 
+// Part maxima of |w| (NaN propagates).
+template <typename S>
+__global__ void __launch_bounds__(kKrylovThreads)
+    krylov_amax_kernel(int64_t n, const S *__restrict__ w,
+                       double *__restrict__ part) {
+  __shared__ double red[kKrylovThreads / 32];
+  const int NB = gridDim.x;
+  const int64_t per = (n + NB - 1) / NB;
+  const int64_t i0 = (int64_t)blockIdx.x * per;
+  const int64_t i1 = i0 + per < n ? i0 + per : n;
+  double m = 0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += kKrylovThreads) {
+    const double v = fabs((double)w[i]);
+    m = (v > m || v != v) ? v : m;
+  }
+  for (int off = 16; off; off >>= 1) {
+    const double o = __shfl_xor_sync(0xffffffffu, m, off);
+    m = (o > m || o != o) ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0;
+    for (int q = 0; q < kKrylovThreads / 32; q++) r = (red[q] > r || red[q] != red[q]) ? red[q] : r;
+    part[blockIdx.x] = r;
+  }
+}
+
 // v *= s (element type) and f = (float)v (the preconditioner's input).
 template <typename S>
 __global__ void krylov_scale_kernel(int64_t n, S *__restrict__ v, double s,
@@ -147,8 +175,8 @@ static unsigned grid_for(int64_t n) {
 int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
                  const float *W, const int32_t *perm, elem_t *V, elem_t *Z,
                  float *F, int m, double rtol, double atol, int abort_after,
-                 double abort_ratio, elem_t *d, int *inner, double *res_est,
-                 int *stalled) {
+                 double abort_ratio, const KrylovTarget *tg, elem_t *d,
+                 int *inner, double *res_est, int *stalled) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   cudaStream_t st = cx->stream;
@@ -188,10 +216,25 @@ int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
   // Hessenberg (column-major, (m+1) x m), Givens rotations, rhs g
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), gv(m + 1, 0.0);
   gv[0] = beta;
-  const double target = std::fmax(rtol * beta, atol);
+  double target = std::fmax(rtol * beta, atol);
+  std::vector<elem_t> ye(m);
+  // d = Z y with y = R^-1 g over the first kc steps
+  auto form_d = [&](int kc) -> int {
+    std::vector<double> y(kc);
+    for (int i = kc - 1; i >= 0; i--) {
+      double t = gv[i];
+      for (int j = i + 1; j < kc; j++) t -= H[(size_t)j * (m + 1) + i] * y[j];
+      y[i] = t / H[(size_t)i * (m + 1) + i];
+    }
+    for (int i = 0; i < kc; i++) ye[i] = (elem_t)y[i];
+    MGB_CUDA(cudaMemcpyAsync(y_dev, ye.data(), kc * sizeof(elem_t),
+                             cudaMemcpyHostToDevice, st));
+    MGB_TRY(gemv_t<elem_t>(n, kc, elem_t(1), Z, n, y_dev, elem_t(0), d));
+    return 0;
+  };
   int k = 0;
   for (; k < m; k++) {
-    elem_t *vk = V + (size_t)k * n, *zk = Z + (size_t)k * n;
+    elem_t *zk = Z + (size_t)k * n;
     elem_t *w = V + (size_t)(k + 1) * n;
     // z_k = M^-1 v_k in FP32
     if (spd) {
@@ -241,7 +284,22 @@ int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
     gv[k + 1] = -sn[k] * gv[k];
     gv[k] = cs[k] * gv[k];
     *res_est = std::fabs(gv[k + 1]);
-    const bool done = *res_est <= target || !(hn > 0);
+    bool done = *res_est <= target || !(hn > 0);
+    // every 8 steps of a first cycle: the correction so far gives |x|, and
+    // with it the residual the backward-error target actually asks for
+    if (!done && tg && (k + 1) % 8 == 0) {
+      MGB_TRY(form_d(k + 1));
+      krylov_amax_kernel<elem_t><<<NBU, kKrylovThreads, 0, st>>>(n, d, dnorm);
+      MGB_LAUNCHED("krylov_amax");
+      MGB_CUDA(cudaMemcpyAsync(host.data(), dnorm, NBU * sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+      MGB_CUDA(cudaStreamSynchronize(st));
+      double xn = 0;
+      for (int c = 0; c < NBU; c++) xn = (host[c] > xn || host[c] != host[c]) ? host[c] : xn;
+      const double t2 = 0.25 * tg->tol * (tg->anorm * xn + tg->bnorm);
+      if (t2 > target) target = t2;
+      done = *res_est <= target;
+    }
     // too slow for these factors: leave the cycle (the caller refactors)
     if (!done && k + 1 >= abort_after && *res_est > abort_ratio * beta) {
       *stalled = 1;
@@ -263,17 +321,7 @@ int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
     MGB_CUDA(cudaMemsetAsync(d, 0, (size_t)n * sizeof(elem_t), st));
     return 0;
   }
-  std::vector<double> y(k);
-  for (int i = k - 1; i >= 0; i--) {
-    double s = gv[i];
-    for (int j = i + 1; j < k; j++) s -= H[(size_t)j * (m + 1) + i] * y[j];
-    y[i] = s / H[(size_t)i * (m + 1) + i];
-  }
-  std::vector<elem_t> ye(k);
-  for (int i = 0; i < k; i++) ye[i] = (elem_t)y[i];
-  MGB_CUDA(cudaMemcpyAsync(y_dev, ye.data(), k * sizeof(elem_t),
-                           cudaMemcpyHostToDevice, st));
-  MGB_TRY(gemv_t<elem_t>(n, k, elem_t(1), Z, n, y_dev, elem_t(0), d));
+  MGB_TRY(form_d(k));
   MGB_CUDA(cudaStreamSynchronize(st));  // ye is pageable host memory
   return 0;
 }

@@ -448,9 +448,11 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
         // has not gained three orders of magnitude in 24 steps gives up
         int stalled = 0;
         const bool may_abort = lp >= 0 && o.fp32_fallback && refinements == 0;
+        const KrylovTarget tg{tol, anorm, bn[0]};
         MGB_TRY(fgmres_cycle(spd, n, A, lda, W, piv + n, V, Z, RF, mcap, 1e-10,
-                             atol, may_abort ? 24 : 1 << 30, 1e-3, D, &inner,
-                             &est, &stalled));
+                             atol, may_abort ? 24 : 1 << 30, 1e-3,
+                             refinements == 0 ? &tg : nullptr, D, &inner, &est,
+                             &stalled));
         it += inner;
         ksteps += inner;
         if (stalled) break;
