@@ -429,15 +429,16 @@ def run_plain_f32(mg, steps=3, warmup=3):
 
 
 def run_spd(mg, n=16384, nrhs=64):
-    """SPD solve with 64 right-hand sides: mixed Cholesky + refinement for
-    lambda in [1,1e3] (BF16) and [1,1e6] (FP16), and the plain FP64 Cholesky."""
+    """SPD solve with 64 right-hand sides: mixed Cholesky (FP16 split
+    tensor-core SYRK updates) + refinement for lambda log-uniform in [1,1e3]
+    and [1,1e6], and the plain FP64 Cholesky."""
     import torch
     L = mg.load("f64")
     mats, B = spd_set(n, (1e3, 1e6), nrhs, 77)
     X = torch.empty_like(B)
     flops = n ** 3 / 3 + 2 * nrhs * 2 * n * n
     out = {}
-    for lm, lp in ((1e3, 1), (1e6, 0)):
+    for lm, lp in ((1e3, 2), (1e6, 2)):
         opts = L.ir_opts(lp_format=lp)
         rep = mg.MatIRReport()
         for rnd in range(2):

@@ -113,9 +113,10 @@ template <typename T>
 int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
             int lp);
 // Tensor-core trailing update of columns [c0,c1) after outer block [kb,ke)
-// (mixed.cu); pack = pack L21 and all of U12[:, ke:n] to 16 bits first.
+// (mixed.cu): packs U12[:, c0:c1] to 16 bits, and L21 too on the block's
+// first call (first = true).
 int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
-                       int64_t ke, int64_t c0, int64_t c1, int lp, bool pack);
+                       int64_t ke, int64_t c0, int64_t c1, int lp, bool first);
 template <typename T>
 int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
             const int32_t *perm, const T *B, int64_t ldb, T *X, int64_t ldx);

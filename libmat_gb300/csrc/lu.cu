@@ -884,18 +884,19 @@ struct StreamSwap {
 
 // Trailing update C[ke:n, c0:c1] -= L21 * U12[:, c0:c1] for outer block
 // [kb, ke): SIMT GEMM in T (lp < 0) or the tensor-core path (lp >= 0, float
-// only: L21/U12 packed to 16 bits once per block, see mixed.cu).
+// only: L21 packed to 16 bits on the block's first call, U12 per call, see
+// mixed.cu).
 template <typename T>
 static int trailing_update(int64_t n, T *A, int64_t lda, int64_t kb,
                            int64_t ke, int64_t c0, int64_t c1, int lp,
-                           bool pack) {
+                           bool first) {
   if (c1 <= c0 || ke >= n) return 0;
   if (lp < 0)
     return gemm_skip_t<T>(false, false, n - ke, c1 - c0, ke - kb, T(-1),
                           A + ke + kb * lda, lda, A + kb + c0 * lda, lda, T(1),
                           A + ke + c0 * lda, lda, 0, nullptr);
   if (sizeof(T) != 4) return set_error(MATGB_ERR_ARG, "tensor-core LU is float");
-  return lp_trailing_update(n, (float *)A, lda, kb, ke, c0, c1, lp, pack);
+  return lp_trailing_update(n, (float *)A, lda, kb, ke, c0, c1, lp, first);
 }
 
 template <typename T>
@@ -925,15 +926,23 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     }
     MGB_CUDA(cudaEventRecord(g_la.ev[1], hi));
     MGB_CUDA(cudaStreamWaitEvent(main, g_la.ev[1], 0));
-    MGB_TRY(laswp_t<T>(A, lda, 0, kb, ke, n, ipiv, kb, ke, perm));
+    const int64_t nn = (n - ke) < NB ? (n - ke) : NB;
     if (ke < n) {
-      MGB_TRY(trsm_unit_lower<T>((int)nb, n - ke, A + kb + kb * lda, lda,
+      // look-ahead: the next block's columns are swapped, solved and updated
+      // first, then the panel stream is released; everything else (the other
+      // columns, the columns left of the block, the permutation) follows
+      // off the critical path
+      MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
+      MGB_TRY(trsm_unit_lower<T>((int)nb, nn, A + kb + kb * lda, lda,
                                  A + kb + ke * lda, lda));
-      // look-ahead: the next block's columns first, then signal the panel
-      const int64_t nn = (n - ke) < NB ? (n - ke) : NB;
       MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true));
       MGB_CUDA(cudaEventRecord(g_la.ev[2], main));
       MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[2], 0));
+    }
+    MGB_TRY(laswp_t<T>(A, lda, 0, kb, ke + nn, n, ipiv, kb, ke, perm));
+    if (ke + nn < n) {
+      MGB_TRY(trsm_unit_lower<T>((int)nb, n - ke - nn, A + kb + kb * lda, lda,
+                                 A + kb + (ke + nn) * lda, lda));
       MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, n, lp, false));
     }
   }

@@ -138,57 +138,69 @@ static unsigned grid_cap(int64_t tot, int per = 256) {
 
 // lp: 1 BF16, 0 FP16 (U12 scaled by a power of two), 2 FP16 split (both
 // operands scaled and split into hi + remainder; three tensor-core products).
+// first: the block's first call -- L21 is packed (and, for the split, its
+// scale found); every call packs the U12 columns [c0, c1) it updates, with a
+// scale of its own (kept in a slot per call, so the two calls of a block --
+// the look-ahead columns, then the rest -- never share one).
 int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
-                       int64_t ke, int64_t c0, int64_t c1, int lp, bool pack) {
+                       int64_t ke, int64_t c0, int64_t c1, int lp, bool first) {
   const int nb = (int)(ke - kb);
   const int Kp = (nb + 63) / 64 * 64;
-  const int64_t m = n - ke, ncols = n - ke;
+  const int64_t m = n - ke, ncols = n - ke, nc = c1 - c0;
   const bool split = lp == 2;
   const size_t an = (size_t)m * Kp, bn_ = (size_t)ncols * Kp;
   uint16_t *A16 = (uint16_t *)ws(WS_T0, an * 2 * (split ? 2 : 1));
   uint16_t *B16 = (uint16_t *)ws(WS_T1, bn_ * 2 * (split ? 2 : 1));
-  float *sc = (float *)ws(WS_T2, 64);
-  if (!A16 || !B16 || !sc) return MATGB_ERR_NOMEM;
+  float *scb = (float *)ws(WS_T2, 256);
+  if (!A16 || !B16 || !scb) return MATGB_ERR_NOMEM;
   uint16_t *A16lo = split ? A16 + an : nullptr;
   uint16_t *B16lo = split ? B16 + bn_ : nullptr;
-  unsigned *amax = (unsigned *)(sc + 4);  // [0] U12, [1] L21
+  // slots: [0..3] scales of the first call, [8..11] of the second;
+  // [16] amax of L21 (split), [17], [18] amax of each call's U12 columns
+  float *sc = scb + (first ? 0 : 8);
+  unsigned *amax_l = (unsigned *)(scb + 16);
+  unsigned *amax_u = (unsigned *)(scb + (first ? 17 : 18));
   cudaStream_t st = ctx()->stream;
-  if (pack) {
-    KtScope kt("lp_pack", 0.0, (split ? 10.0 : 6.0) * (m + ncols) * nb);
-    dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
+  const int64_t off = (c0 - ke) * Kp;
+  {
+    KtScope kt("lp_pack", 0.0,
+               (split ? 10.0 : 6.0) * ((first ? m : 0) + nc) * nb);
     const float *L21 = A + ke + kb * lda;
-    const float *U12 = A + kb + ke * lda;
+    const float *U12 = A + kb + c0 * lda;
     if (lp != 1) {
-      MGB_CUDA(cudaMemsetAsync(amax, 0, 2 * sizeof(unsigned), st));
-      u12_amax_kernel<<<grid_cap((int64_t)nb * ncols), 256, 0, st>>>(
-          U12, lda, nb, ncols, amax);
+      MGB_CUDA(cudaMemsetAsync(amax_u, 0, sizeof(unsigned), st));
+      u12_amax_kernel<<<grid_cap((int64_t)nb * nc), 256, 0, st>>>(U12, lda, nb,
+                                                                  nc, amax_u);
       MGB_LAUNCHED("u12_amax");
     }
-    if (split) {
-      u12_amax_kernel<<<grid_cap((int64_t)nb * m), 256, 0, st>>>(
-          L21, lda, (int)m, nb, amax + 1);
-      MGB_LAUNCHED("l21_amax");
-      pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax + 1,
-                                            nullptr, A16lo);
-    } else if (lp == 1) {
-      pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr,
-                                            nullptr);
-    } else {
-      pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr,
-                                            nullptr);
+    if (first) {
+      dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
+      if (split) {
+        MGB_CUDA(cudaMemsetAsync(amax_l, 0, sizeof(unsigned), st));
+        u12_amax_kernel<<<grid_cap((int64_t)nb * m), 256, 0, st>>>(
+            L21, lda, (int)m, nb, amax_l);
+        MGB_LAUNCHED("l21_amax");
+        pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax_l,
+                                              nullptr, A16lo);
+      } else if (lp == 1) {
+        pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16,
+                                              nullptr, nullptr);
+      } else {
+        pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16,
+                                              nullptr, nullptr);
+      }
+      MGB_LAUNCHED("pack_l21");
     }
-    MGB_LAUNCHED("pack_l21");
     if (lp == 1)
-      pack_u12_kernel<1><<<grid_cap((int64_t)Kp * ncols), 256, 0, st>>>(
-          U12, lda, nb, Kp, ncols, nullptr, sc, B16);
+      pack_u12_kernel<1><<<grid_cap((int64_t)Kp * nc), 256, 0, st>>>(
+          U12, lda, nb, Kp, nc, nullptr, sc, B16 + off);
     else
-      pack_u12_kernel<0><<<grid_cap((int64_t)Kp * ncols), 256, 0, st>>>(
-          U12, lda, nb, Kp, ncols, amax, sc, B16, B16lo,
-          split ? amax + 1 : nullptr);
+      pack_u12_kernel<0><<<grid_cap((int64_t)Kp * nc), 256, 0, st>>>(
+          U12, lda, nb, Kp, nc, amax_u, sc, B16 + off,
+          split ? B16lo + off : nullptr, split ? amax_l : nullptr);
     MGB_LAUNCHED("pack_u12");
   }
-  const int64_t off = (c0 - ke) * Kp;
-  return tc_gemm(lp == 1, m, c1 - c0, Kp, A16, Kp, B16 + off, Kp, -1.f,
+  return tc_gemm(lp == 1, m, nc, Kp, A16, Kp, B16 + off, Kp, -1.f,
                  lp != 1 ? sc + 1 : nullptr, 1.f, A + ke + c0 * lda, lda, 0,
                  nullptr, A16lo, split ? B16lo + off : nullptr);
 }

@@ -129,8 +129,8 @@ def factor_lp(L, A, lp):
 
 
 def round_lp(x, lp):
-    """16-bit rounding of an update operand (lp 2, the split form, and lp -1
-    are modelled as exact FP32)."""
+    """16-bit rounding of an update operand (lp -1: exact FP32; the split
+    form lp 2 is modelled by split16)."""
     if lp == 1:
         return bf16_bits_to_f64(to_bf16_bits(x))
     if lp == 0:
@@ -138,10 +138,23 @@ def round_lp(x, lp):
     return x.astype(np.float64)
 
 
+def split16(x):
+    """The split operand: power-of-two scale s (max |x| s at most 2^14), FP16
+    hi part of x s and the FP16 rounding of the FP32 remainder."""
+    x = np.asarray(x, np.float32)
+    am = np.abs(x).max()
+    s = 2.0 ** (14 - np.frexp(am)[1]) if am > 0 else 1.0
+    xs = (x * np.float32(s)).astype(np.float32)
+    h = xs.astype(np.float16)
+    lo = (xs - h.astype(np.float32)).astype(np.float16)
+    return h.astype(np.float64), lo.astype(np.float64), s
+
+
 def emulate_lp_lu(A, lp, nb=128):
     """numpy model of the mixed LU: FP32 panels and FP32 trailing matrix, the
     trailing products of each nb-column block formed from 16-bit-rounded
-    L21/U12 (FP16 with the per-block power-of-two scale of U12).  Returns the
+    L21/U12 (FP16 with the per-block power-of-two scale of U12; the split form
+    with hi + remainder parts of both, three products).  Returns the
     normwise factorisation error |PA - LU|_max / |A|_max it reaches."""
     M = np.array(A, np.float32)
     n = M.shape[0]
@@ -160,6 +173,12 @@ def emulate_lp_lu(A, lp, nb=128):
             L11 = np.tril(M[kb:ke, kb:ke].astype(np.float64), -1) + np.eye(ke - kb)
             M[kb:ke, ke:] = np.linalg.solve(L11, M[kb:ke, ke:].astype(np.float64))
             U12 = M[kb:ke, ke:].astype(np.float64)
+            if lp == 2:
+                Lh, Ll, sl = split16(M[ke:, kb:ke])
+                Uh, Ul, su = split16(M[kb:ke, ke:])
+                upd = (Lh @ Uh + Lh @ Ul + Ll @ Uh) / (sl * su)
+                M[ke:, ke:] = (M[ke:, ke:].astype(np.float64) - upd).astype(np.float32)
+                continue
             s = 1.0
             if lp == 0 and np.abs(U12).max() > 0:
                 s = 2.0 ** (14 - np.frexp(np.abs(U12).max())[1])
