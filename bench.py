@@ -132,9 +132,24 @@ def ktable(L):
 
 
 # ----------------------------------------------------------------- data
+def _preload_torch_linalg():
+    """torch loads its CUDA linear-algebra library lazily by soname; under a
+    profiler's injection that lookup can fail, so load it by path first."""
+    import ctypes
+    import glob
+    import torch
+    for f in glob.glob(os.path.join(os.path.dirname(torch.__file__), "lib",
+                                    "libtorch_cuda_linalg.so*")):
+        try:
+            ctypes.CDLL(f, mode=ctypes.RTLD_GLOBAL)
+        except OSError:
+            pass
+
+
 def conditioned_set(n, kappas, seed):
     """A_kappa = U diag(sigma_kappa) V^T on the GPU (torch, float64)."""
     import torch
+    _preload_torch_linalg()
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
     U, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float32,
@@ -156,6 +171,7 @@ def conditioned_set(n, kappas, seed):
 def spd_set(n, lam_maxes, nrhs, seed):
     """A = Q diag(lambda) Q^T, lambda log-uniform in [1, lam_max]."""
     import torch
+    _preload_torch_linalg()
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
     Q, _ = torch.linalg.qr(torch.randn(n, n, device="cuda", dtype=torch.float32,
@@ -235,6 +251,8 @@ def run_headline(args, mg):
         d["ms"] = float(np.mean(d["ms"]))
     # independent check of the last solve of each condition number
     for k in KAPPAS:
+        if "%g" % k not in per_kappa:
+            continue
         solve(k)
         L.sync()
         per_kappa["%g" % k]["bwd_err_check"] = bwd_err_T(mats[k], x, b)

@@ -244,28 +244,17 @@ struct RegPanelSmem {
   T kval[2][kW];
 };
 
+// The 24-column elimination of a register-resident panel (rows [k0, n) of
+// A, columns [k0, k0+24)): thread tid of CTA c owns panel rows prow[r]
+// (panel-relative, -1 = none) in a[r][*].  ipiv[k0+kk] (CTA 0) and, when
+// spiv is given, spiv[kk] (every CTA, shared memory) get the global pivot row.
 template <typename T, int R, int NT>
-__global__ void __launch_bounds__(NT, 1)
-    lu_panel_reg_kernel(T *__restrict__ A, int64_t lda, int64_t n, int64_t k0,
-                        int rpc, int32_t *__restrict__ ipiv, T eps) {
-  constexpr int NW = NT / 32;
-  __shared__ RegPanelSmem<T, NT> sm;
-  cg::cluster_group cluster = cg::this_cluster();
-  const int CS = (int)cluster.num_blocks();
-  const int c = (int)cluster.block_rank();
+__device__ __forceinline__ void reg_panel_columns(
+    T (&a)[R][kW], const int (&prow)[R], RegPanelSmem<T, NT> &sm,
+    cg::cluster_group &cluster, int c, int CS, int rbase, int rpc, int64_t k0,
+    int32_t *__restrict__ ipiv, int32_t *spiv, T eps) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int m = (int)(n - k0);
-  const int rbase = c * rpc;
-  int prow[R];
-  T a[R][kW];
-#pragma unroll
-  for (int r = 0; r < R; r++) {
-    const int lr = tid + r * NT;
-    prow[r] = (lr < rpc && rbase + lr < m) ? rbase + lr : -1;
-#pragma unroll
-    for (int j = 0; j < kW; j++)
-      a[r][j] = prow[r] >= 0 ? A[(k0 + prow[r]) + (k0 + j) * lda] : T(0);
-  }
+  constexpr int NW = NT / 32;
 #pragma unroll
   for (int kk = 0; kk < kW; kk++) {
     const int buf = kk & 1;
@@ -323,6 +312,7 @@ __global__ void __launch_bounds__(NT, 1)
     int p, wc;
     pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
     if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
+    if (spiv && tid == 0) spiv[kk] = (int32_t)(k0 + p);
     const T *u = &sm.xval[buf][wc][0];
     const T *kv = &sm.kval[buf][0];
     if (p != kk) {
@@ -353,6 +343,31 @@ __global__ void __launch_bounds__(NT, 1)
         }
     }
   }
+}
+
+template <typename T, int R, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    lu_panel_reg_kernel(T *__restrict__ A, int64_t lda, int64_t n, int64_t k0,
+                        int rpc, int32_t *__restrict__ ipiv, T eps) {
+  __shared__ RegPanelSmem<T, NT> sm;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CS = (int)cluster.num_blocks();
+  const int c = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const int m = (int)(n - k0);
+  const int rbase = c * rpc;
+  int prow[R];
+  T a[R][kW];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int lr = tid + r * NT;
+    prow[r] = (lr < rpc && rbase + lr < m) ? rbase + lr : -1;
+#pragma unroll
+    for (int j = 0; j < kW; j++)
+      a[r][j] = prow[r] >= 0 ? A[(k0 + prow[r]) + (k0 + j) * lda] : T(0);
+  }
+  reg_panel_columns<T, R, NT>(a, prow, sm, cluster, c, CS, rbase, rpc, k0,
+                              ipiv, nullptr, eps);
 #pragma unroll
   for (int r = 0; r < R; r++)
     if (prow[r] >= 0)
@@ -535,6 +550,129 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
   return 0;
 }
 
+// ---- fused block factorisation (mixed-precision path) --------------------
+// One cluster launch factors the whole outer block A[kb:n, kb:kb+bw) (bw a
+// multiple of 24, the block held in L2 between phases): for each 24-column
+// panel -- the register panel elimination (reg_panel_columns), its row swaps
+// applied to the block's other columns, U12 = L11^-1 A12 for the block
+// columns right of the panel, and the rank-24 update of the rows below from
+// the L21 rows still in registers.  A cluster barrier separates the phases;
+// data written by another CTA is read with ld.global.cg (L2), so no stale L1
+// line is ever used.  Pivots are never skipped here (the mixed path's
+// threshold is 0), so the block width is free of the reference's grouping.
+constexpr int kFusedMaxBw = 144;
+
+template <typename T, int NT>
+struct FusedSmem {
+  RegPanelSmem<T, NT> ps;
+  SwapMap map;
+  int32_t spiv[kW];
+  T L11[kW][kW + 1];
+  T U12[kW][kFusedMaxBw - kW];
+};
+
+template <typename T, int R, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    lu_block_fused_kernel(T *__restrict__ A, int64_t lda, int64_t n,
+                          int64_t kb, int bw, int32_t *__restrict__ ipiv) {
+  __shared__ FusedSmem<T, NT> sm;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CS = (int)cluster.num_blocks();
+  const int c = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NWARP = NT / 32;
+  const int np = bw / kW;
+  for (int pn = 0; pn < np; pn++) {
+    const int64_t k0 = kb + (int64_t)pn * kW;
+    const int m = (int)(n - k0);
+    const int rpc = (m + CS - 1) / CS;
+    const int rbase = c * rpc;
+    int prow[R];
+    T a[R][kW];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int lr = tid + r * NT;
+      prow[r] = (lr < rpc && rbase + lr < m) ? rbase + lr : -1;
+#pragma unroll
+      for (int j = 0; j < kW; j++)
+        a[r][j] = prow[r] >= 0 ? __ldcg(&A[(k0 + prow[r]) + (k0 + j) * lda]) : T(0);
+    }
+    reg_panel_columns<T, R, NT>(a, prow, sm.ps, cluster, c, CS, rbase, rpc, k0,
+                                ipiv, sm.spiv, T(0));
+#pragma unroll
+    for (int r = 0; r < R; r++)
+      if (prow[r] >= 0)
+#pragma unroll
+        for (int j = 0; j < kW; j++) A[(k0 + prow[r]) + (k0 + j) * lda] = a[r][j];
+    // the panel's swaps on the block's other columns: [kb, k0) and
+    // [k0+24, kb+bw); CTA c takes every CS-th of them, one warp per column
+    __syncthreads();
+    if (warp == 0) build_swap_map(sm.map, sm.spiv - k0, k0, k0 + kW);
+    __syncthreads();
+    const int nleft = (int)(k0 - kb), nright = bw - (pn + 1) * kW;
+    {
+      const int cnt = sm.map.cnt;
+      for (int t = c + CS * warp; t < nleft + nright; t += CS * NWARP) {
+        const int64_t col = t < nleft ? kb + t : k0 + kW + (t - nleft);
+        T *colp = A + col * lda;
+        T v[2 * kW / 32 + 1];
+#pragma unroll
+        for (int q = 0; q < 2 * kW / 32 + 1; q++) {
+          const int r = lane + 32 * q;
+          if (r < cnt) v[q] = __ldcg(&colp[sm.map.src[r]]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 2 * kW / 32 + 1; q++) {
+          const int r = lane + 32 * q;
+          if (r < cnt) colp[sm.map.pos[r]] = v[q];
+        }
+      }
+    }
+    if (nright <= 0) break;  // the block's last panel: nothing to its right
+    cluster.sync();
+    // U12 = L11^-1 A12 for the right columns (rows k0..k0+23), one warp per
+    // column: lane l holds row l, x_k broadcast by shuffle
+    for (int e = tid; e < kW * kW; e += NT) {
+      const int i = e % kW, j = e / kW;
+      sm.L11[i][j] = __ldcg(&A[(k0 + i) + (k0 + j) * lda]);
+    }
+    __syncthreads();
+    for (int t = c + CS * warp; t < nright; t += CS * NWARP) {
+      T *colp = A + (k0 + kW + t) * lda + k0;
+      T x = lane < kW ? __ldcg(&colp[lane]) : T(0);
+#pragma unroll
+      for (int k = 0; k < kW - 1; k++) {
+        const T xk = __shfl_sync(0xffffffffu, x, k);
+        if (lane > k && lane < kW) x = fma(-sm.L11[lane][k], xk, x);
+      }
+      if (lane < kW) colp[lane] = x;
+    }
+    cluster.sync();
+    // rank-24 update of the rows below the panel, right columns
+    for (int e = tid; e < kW * nright; e += NT) {
+      const int i = e % kW, j = e / kW;
+      sm.U12[i][j] = __ldcg(&A[(k0 + i) + (k0 + kW + j) * lda]);
+    }
+    __syncthreads();
+    for (int j = 0; j < nright; j++) {
+      T uj[kW];
+#pragma unroll
+      for (int k = 0; k < kW; k++) uj[k] = sm.U12[k][j];
+      T *colp = A + (k0 + kW + j) * lda + k0;
+#pragma unroll
+      for (int r = 0; r < R; r++)
+        if (prow[r] >= kW) {
+          T acc = __ldcg(&colp[prow[r]]);
+#pragma unroll
+          for (int k = 0; k < kW; k++) acc = fma(-a[r][k], uj[k], acc);
+          colp[prow[r]] = acc;
+        }
+    }
+    cluster.sync();
+  }
+}
+
 // ---- U12 = L11^{-1} A12 with L11 unit lower (TB x TB) ----------------------
 // One warp per right-hand-side column: lane l holds rows l, l+32, ... of the
 // column in registers, L11 sits in shared memory; step k broadcasts x_k by a
@@ -602,6 +740,7 @@ static int trsm_unit_lower(int tb, int64_t ncols, const T *L, int64_t ldl, T *B,
   if (tb == kRefBlock) return launch_trsm_warp<T, kRefBlock>(ncols, L, ldl, B, ldb);
   if (tb == kOuterBlock) return launch_trsm_warp<T, kOuterBlock>(ncols, L, ldl, B, ldb);
   if (tb == kOuterBlockLp) return launch_trsm_warp<T, kOuterBlockLp>(ncols, L, ldl, B, ldb);
+  if (tb == kFusedMaxBw) return launch_trsm_warp<T, kFusedMaxBw>(ncols, L, ldl, B, ldb);
   return trsm_left_t<T>(true, false, true, tb, ncols, L, ldl, B, ldb, nullptr);
 }
 
@@ -832,6 +971,60 @@ int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
   return 0;
 }
 
+// The fused block factorisation when the block fits one cluster's registers
+// (float; rows n-kb <= 16 CTAs x 1024); *done = false otherwise.
+template <typename T>
+static int try_fused_block(T *A, int64_t lda, int64_t n, int64_t kb, int bw,
+                           int32_t *ipiv, bool *done) {
+  *done = false;
+  if constexpr (sizeof(T) != 4) {
+    return 0;
+  } else {
+    if (bw % kW || bw > kFusedMaxBw) return 0;
+    MGB_TRY(panel_setup<T>());
+    const int maxcs = PanelState<T>::maxcs;
+    const int64_t m = n - kb;
+    int cs = 0, R = 0;
+    for (int c = 1; c <= maxcs && !cs; c *= 2)
+      if ((int64_t)c * 512 >= m) { cs = c; R = 1; }
+    for (int c = 1; c <= maxcs && !cs; c *= 2)
+      if ((int64_t)c * 1024 >= m) { cs = c; R = 2; }
+    if (!cs) return 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = ctx()->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const double mm = (double)m;
+    KtScope kt("lu_block_fused", mm * bw * bw, 2.0 * mm * bw * sizeof(T));
+    cudaError_t e;
+    if (R == 1) {
+      auto kern = lu_block_fused_kernel<T, 1, 512>;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv);
+    } else {
+      auto kern = lu_block_fused_kernel<T, 2, 512>;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv);
+    }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(MATGB_ERR_CUDA, "lu_block_fused launch (cluster %d, R %d): %s",
+                       cs, R, cudaGetErrorString(e));
+    }
+    MGB_LAUNCHED("lu_block_fused");
+    *done = true;
+    return 0;
+  }
+}
+
 // Factor the outer block columns [kb, ke) (rows [kb, n)) with 24-column
 // panels: swaps, U12 solve and update restricted to the block's columns.
 template <typename T>
@@ -916,13 +1109,19 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
   // main -> hi: everything queued so far (input copies, perm init)
   MGB_CUDA(cudaEventRecord(g_la.ev[0], main));
   MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[0], 0));
-  const int64_t NB = lp >= 0 ? kOuterBlockLp : kOuterBlock;
+  // mixed path (float, tensor-core updates): 144-column blocks factored by
+  // one fused cluster launch each where they fit
+  const bool fused = lp >= 0 && sizeof(T) == 4;
+  const int64_t NB = fused ? kFusedMaxBw : lp >= 0 ? kOuterBlockLp : kOuterBlock;
   for (int64_t kb = 0; kb < n; kb += NB) {
     const int64_t nb = (n - kb) < NB ? (n - kb) : NB;
     const int64_t ke = kb + nb;
     {
       StreamSwap sw(hi);
-      MGB_TRY(factor_block<T>(n, A, lda, kb, ke, ipiv, eps));
+      bool done = false;
+      if (fused && nb == NB)
+        MGB_TRY(try_fused_block<T>(A, lda, n, kb, (int)nb, ipiv, &done));
+      if (!done) MGB_TRY(factor_block<T>(n, A, lda, kb, ke, ipiv, eps));
     }
     MGB_CUDA(cudaEventRecord(g_la.ev[1], hi));
     MGB_CUDA(cudaStreamWaitEvent(main, g_la.ev[1], 0));
