@@ -134,10 +134,16 @@ int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
                    float *C22, int64_t ldc, int lp, const int32_t *info);
 template <typename T>
 int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp);
-// Single-launch triangular solve with one right-hand side (trsv.cu).
+// Single-launch triangular solve with one right-hand side (trsv.cu); inv
+// (float only): diagonal sub-blocks through explicit inverses, for the
+// refinement's preconditioner.
 template <typename T>
 int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
-           int64_t ldt, T *x);
+           int64_t ldt, T *x, bool inv = false);
+// The low-precision factors applied to one vector (the FGMRES
+// preconditioner): out = (P^T L U)^-1 in (LU) or (L L^T)^-1 in (spd).
+int precond_solve(bool spd, int64_t n, const float *W, const int32_t *perm,
+                  const float *in, float *out);
 int trsv_status();
 template <typename T>
 int potrs_t(int64_t n, int64_t nrhs, const T *L, int64_t lda, T *B,

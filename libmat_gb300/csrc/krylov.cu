@@ -237,13 +237,7 @@ int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
     elem_t *zk = Z + (size_t)k * n;
     elem_t *w = V + (size_t)(k + 1) * n;
     // z_k = M^-1 v_k in FP32
-    if (spd) {
-      MGB_CUDA(cudaMemcpyAsync(Fout, Fin, (size_t)n * sizeof(float),
-                               cudaMemcpyDeviceToDevice, st));
-      MGB_TRY(potrs_t<float>(n, 1, W, n, Fout, n, nullptr));
-    } else {
-      MGB_TRY(getrs_t<float>(n, 1, W, n, perm, Fin, n, Fout, n));
-    }
+    MGB_TRY(precond_solve(spd, n, W, perm, Fin, Fout));
     krylov_widen_kernel<elem_t><<<g, 256, 0, st>>>(n, Fout, zk);
     MGB_LAUNCHED("krylov_widen");
     // w = A z_k

@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(NT, 1)
 // for t < cnt; every other row is unchanged.  Built by one warp in shared
 // memory: positions [k1,k2) are indexed directly, pivot rows beyond k2 are
 // found by a warp-wide search.
-constexpr int kSwapMax = 128;
+constexpr int kSwapMax = 160;  // pivots per swap block (the fused path uses 144)
 
 struct SwapMap {
   int32_t pos[2 * kSwapMax];
@@ -530,7 +530,7 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
             const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm) {
   const int64_t ncol = (c1 - c0) + (c3 - c2);
   if (k2 <= k1 || (ncol <= 0 && !perm)) return 0;
-  if (k2 - k1 > kSwapMax) return set_error(MATGB_ERR_ARG, "laswp: block > 128");
+  if (k2 - k1 > kSwapMax) return set_error(MATGB_ERR_ARG, "laswp: block > %d", kSwapMax);
   if (!g_swap_ring) MGB_CUDA(cudaMalloc(&g_swap_ring, kSwapRing * sizeof(SwapMap)));
   SwapMap *map = g_swap_ring + g_swap_next;
   g_swap_next = (g_swap_next + 1) % kSwapRing;
@@ -1163,6 +1163,26 @@ int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
   MGB_TRY(trsm_left_t<T>(true, false, true, n, nrhs, LU, lda, X, ldx, nullptr));
   MGB_TRY(trsm_left_t<T>(false, false, false, n, nrhs, LU, lda, X, ldx, nullptr));
   return 0;
+}
+
+int precond_solve(bool spd, int64_t n, const float *W, const int32_t *perm,
+                  const float *in, float *out) {
+  Ctx *cx = ctx();
+  if (!cx) return MATGB_ERR_NO_DEVICE;
+  if (n <= 0) return 0;
+  if (spd) {
+    MGB_CUDA(cudaMemcpyAsync(out, in, (size_t)n * sizeof(float),
+                             cudaMemcpyDeviceToDevice, cx->stream));
+    MGB_TRY(trsv_t<float>(true, false, false, n, W, n, out, true));
+    return trsv_t<float>(true, true, false, n, W, n, out, true);
+  }
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > (int64_t)cx->sms * 16) blocks = (int64_t)cx->sms * 16;
+  gather_rows_kernel<float><<<(unsigned)blocks, 256, 0, cx->stream>>>(
+      n, 1, perm, in, n, out, n);
+  MGB_LAUNCHED("gather_rows");
+  MGB_TRY(trsv_t<float>(true, false, true, n, W, n, out, true));
+  return trsv_t<float>(false, false, false, n, W, n, out, true);
 }
 
 #define MGB_LU_INST(T)                                                         \

@@ -48,10 +48,16 @@ struct TvSmem {
   T rd[RB];          // reciprocals of its diagonal
   T part[4][RB];     // partial sums (op(T) = T)
   T xs[RB];
+  T Dinv[RB / 32][32][33];  // INV: inverses of the 32 x 32 diagonal sub-blocks
 };
 
 // EL: op(T) lower (forward); TR: op(T) = T^T; UNIT: unit diagonal.
-template <typename T, int RB, bool EL, bool TR, bool UNIT>
+// INV: the diagonal block is solved through the explicit inverses of its
+// 32 x 32 sub-blocks, formed while the CTA waits (four short matrix-vector
+// products on the critical path instead of RB dependent steps); accuracy then
+// depends on those sub-blocks' conditioning, so only the refinement's
+// preconditioner uses it.
+template <typename T, int RB, bool EL, bool TR, bool UNIT, bool INV>
 __global__ void __launch_bounds__(4 * RB)
     trsv_kernel(int64_t n, const T *__restrict__ Tm, int64_t ldt,
                 T *__restrict__ x, int *__restrict__ flags,
@@ -86,7 +92,36 @@ __global__ void __launch_bounds__(4 * RB)
     sm.Dg[i][j] = (i < rows && j < rows) ? el(r0 + i, r0 + j) : T(0);
   }
   __syncthreads();
-  if (!UNIT && tid < RB) sm.rd[tid] = tid < rows ? T(1) / sm.Dg[tid][tid] : T(1);
+  if (tid < RB) sm.rd[tid] = (!UNIT && tid < rows) ? T(1) / sm.Dg[tid][tid] : T(1);
+  if (INV) {
+    __syncthreads();
+    // warp s inverts sub-block s: lane j forms column j of its inverse
+    if (warp < RB / 32) {
+      const int s0 = warp * 32, j = lane;
+      T xv[32];
+      if (EL) {
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+          T acc = T(0);
+#pragma unroll
+          for (int k = 0; k < i; k++) acc = fma(sm.Dg[s0 + i][s0 + k], xv[k], acc);
+          const T ri = sm.rd[s0 + i];
+          xv[i] = (i == j) ? ri : -ri * acc;
+        }
+      } else {
+#pragma unroll
+        for (int i = 31; i >= 0; i--) {
+          T acc = T(0);
+#pragma unroll
+          for (int k = i + 1; k < 32; k++) acc = fma(sm.Dg[s0 + i][s0 + k], xv[k], acc);
+          const T ri = sm.rd[s0 + i];
+          xv[i] = (i == j) ? ri : -ri * acc;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 32; i++) sm.Dinv[warp][i][j] = xv[i];
+    }
+  }
 
   const int need = t;  // blocks before this one in solve order
   auto tile_col0 = [&](int k) -> int64_t {
@@ -210,7 +245,27 @@ __global__ void __launch_bounds__(4 * RB)
     T y[YR];
 #pragma unroll
     for (int m = 0; m < YR; m++) y[m] = sm.xs[lane + 32 * m];
-    if (EL) {
+    if (INV) {
+      // sub-block by sub-block: y_s = Dinv_s t_s, then fold y_s into the
+      // sub-blocks still to come
+#pragma unroll
+      for (int q = 0; q < YR; q++) {
+        const int sb = EL ? q : YR - 1 - q;
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < 32; k++)
+          acc = fma(sm.Dinv[sb][lane][k], __shfl_sync(0xffffffffu, y[sb], k), acc);
+        y[sb] = acc;
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+          const T yk = __shfl_sync(0xffffffffu, y[sb], k);
+#pragma unroll
+          for (int m = 0; m < YR; m++)
+            if (EL ? m > sb : m < sb)
+              y[m] = fma(-sm.Dg[lane + 32 * m][sb * 32 + k], yk, y[m]);
+        }
+      }
+    } else if (EL) {
 #pragma unroll
       for (int m0 = 0; m0 < YR; m0++) {
 #pragma unroll 8
@@ -262,7 +317,7 @@ struct TvBufs {
 };
 static TvBufs g_tv;
 
-template <typename T, int RB, bool EL, bool TR, bool UNIT>
+template <typename T, int RB, bool EL, bool TR, bool UNIT, bool INV>
 static int launch_trsv(int64_t n, const T *Tm, int64_t ldt, T *x) {
   const int nb = (int)((n + RB - 1) / RB);
   if (g_tv.cap < nb) {
@@ -278,12 +333,12 @@ static int launch_trsv(int64_t n, const T *Tm, int64_t ldt, T *x) {
     g_tv.epoch = 0;
   }
   g_tv.epoch++;
-  auto k = trsv_kernel<T, RB, EL, TR, UNIT>;
+  auto k = trsv_kernel<T, RB, EL, TR, UNIT, INV>;
   const size_t smem = sizeof(TvSmem<T, RB>);
   MGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
   MGB_CUDA(cudaMemsetAsync(&g_tv.st->ticket, 0, sizeof(int), ctx()->stream));
-  KtScope kt("trsv", (double)n * n, (double)sizeof(T) * n * n / 2.0);
+  KtScope kt(INV ? "trsv_inv" : "trsv", (double)n * n, (double)sizeof(T) * n * n / 2.0);
   k<<<nb, 4 * RB, smem, ctx()->stream>>>(n, Tm, ldt, x, g_tv.flags, g_tv.st,
                                          g_tv.epoch);
   return launch_check((const void *)k, "trsv", smem);
@@ -294,7 +349,7 @@ static int g_tv_rb_override = 0;
 
 template <typename T>
 int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
-           int64_t ldt, T *x) {
+           int64_t ldt, T *x, bool inv) {
   if (!ctx()) return MATGB_ERR_NO_DEVICE;
   if (n <= 0) return 0;
   const bool el = lower != trans;
@@ -304,9 +359,13 @@ int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
   if (sizeof(T) != 4) rb = 64;
 #define MGB_TV(E, R, U)                                                        \
   if (el == E && trans == R && unit == U) {                                    \
-    if constexpr (sizeof(T) == 4)                                              \
-      if (rb == 128) return launch_trsv<T, 128, E, R, U>(n, Tm, ldt, x);       \
-    return launch_trsv<T, 64, E, R, U>(n, Tm, ldt, x);                         \
+    if constexpr (sizeof(T) == 4) {                                            \
+      if (inv)                                                                 \
+        return rb == 128 ? launch_trsv<T, 128, E, R, U, true>(n, Tm, ldt, x)   \
+                         : launch_trsv<T, 64, E, R, U, true>(n, Tm, ldt, x);   \
+      if (rb == 128) return launch_trsv<T, 128, E, R, U, false>(n, Tm, ldt, x); \
+    }                                                                          \
+    return launch_trsv<T, 64, E, R, U, false>(n, Tm, ldt, x);                  \
   }
   MGB_TV(true, false, false)
   MGB_TV(true, false, true)
@@ -321,9 +380,9 @@ int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
 }
 
 template int trsv_t<float>(bool, bool, bool, int64_t, const float *, int64_t,
-                           float *);
+                           float *, bool);
 template int trsv_t<double>(bool, bool, bool, int64_t, const double *, int64_t,
-                            double *);
+                            double *, bool);
 
 int trsv_status() {
   if (!g_tv.st) return 0;
