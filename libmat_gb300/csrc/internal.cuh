@@ -50,7 +50,7 @@ struct KtScope {
 // counterpart of the reference's scratch arena, mat.h:865-895).
 enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
-  WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_NSLOTS
+  WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_NSLOTS
 };
 void *ws(int slot, size_t bytes);
 

@@ -386,6 +386,7 @@ constexpr int kSwapMax = 160;  // pivots per swap block (the fused path uses 144
 struct SwapMap {
   int32_t pos[2 * kSwapMax];
   int32_t src[2 * kSwapMax];
+  int32_t piv[kSwapMax];  // the pivot sequence, loaded once in parallel
   int cnt;
 };
 
@@ -396,12 +397,13 @@ __device__ void build_swap_map(SwapMap &sm, const int32_t *__restrict__ ipiv,
   for (int i = lane; i < nk; i += 32) {
     sm.pos[i] = (int32_t)(k1 + i);
     sm.src[i] = (int32_t)(k1 + i);
+    sm.piv[i] = ipiv[k1 + i];  // all loads in flight at once, not one per step
   }
   __syncwarp();
   int nx = 0;  // extra rows (>= k2) at pos[nk .. nk+nx)
   for (int i = 0; i < nk; i++) {
     const int32_t k = (int32_t)(k1 + i);
-    const int32_t p = ipiv[k1 + i];
+    const int32_t p = sm.piv[i];
     if (p == k) continue;
     int slot;
     if (p < k2) {

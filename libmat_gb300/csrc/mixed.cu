@@ -238,29 +238,44 @@ int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
 }
 
 // ---- refinement kernels ------------------------------------------------------------
+// W = (float)A (n x n), and, when rowsum is given, rowsum[i] += sum |A(i,j)|
+// over the thread's chunk of columns: the one pass over A that the
+// factorisation needs anyway also yields |A|_inf.  Thread = row, grid.y =
+// column chunk (coalesced down each column).
 template <typename S>
-__global__ void to_float_kernel(int64_t rows, int64_t cols,
-                                const S *__restrict__ A, int64_t lda,
-                                float *__restrict__ W, int64_t ldw) {
-  const int64_t tot = rows * cols;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e % rows, j = e / rows;
-    W[i + j * ldw] = (float)A[i + j * lda];
-  }
-}
-
-// max over rows of sum_j |A(i,j)| (|A|_inf), via the bit pattern of a
-// non-negative double (monotone as an unsigned integer).
-template <typename S>
-__global__ void row_abs_sum_kernel(int64_t n, const S *__restrict__ A,
-                                   int64_t lda,
-                                   unsigned long long *__restrict__ out) {
+__global__ void to_float_rowsum_kernel(int64_t n, const S *__restrict__ A,
+                                       int64_t lda, float *__restrict__ W,
+                                       int64_t ldw, double *__restrict__ rowsum,
+                                       int chunk) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const int64_t j0 = (int64_t)blockIdx.y * chunk;
+  const int64_t j1 = j0 + chunk < n ? j0 + chunk : n;
   double s = 0;
-  for (int64_t j = 0; j < n; j++) s += fabs((double)A[i + j * lda]);
-  atomicMax(out, (unsigned long long)__double_as_longlong(s));
+#pragma unroll 8
+  for (int64_t j = j0; j < j1; j++) {
+    const S v = A[i + j * lda];
+    W[i + j * ldw] = (float)v;
+    s += fabs((double)v);
+  }
+  if (rowsum) atomicAdd(&rowsum[i], s);
+}
+
+// out = max_i rowsum[i] as the bit pattern of a non-negative double
+// (monotone as an unsigned integer; NaN propagates as the largest pattern).
+__global__ void rowmax_kernel(int64_t n, const double *__restrict__ rowsum,
+                              unsigned long long *__restrict__ out) {
+  unsigned long long m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(rowsum[i]);
+    m = b > m ? b : m;
+  }
+  for (int off = 16; off; off >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, off);
+    m = o > m ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 // Per-column max |R(:,c)| and max |X(:,c)| (bit patterns of non-negative
@@ -382,18 +397,16 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   const dim3 cg(grid_cap(n) < 64 ? grid_cap(n) : 64, (unsigned)nrhs);
   const unsigned gnn = grid_cap(n * nrhs);
 
-  // |A|_inf and per-column |B|_inf
+  // per-column |B|_inf now; |A|_inf from the first conversion of A
+  double *rowsum = (double *)ws(WS_RS, (size_t)n * sizeof(double));
+  if (!rowsum) return MATGB_ERR_NOMEM;
   MGB_CUDA(cudaMemsetAsync(red, 0, (size_t)(2 * nrhs + 8) * sizeof(unsigned long long), st));
-  row_abs_sum_kernel<elem_t><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(
-      n, A, lda, red);
-  MGB_LAUNCHED("row_abs_sum");
+  MGB_CUDA(cudaMemsetAsync(rowsum, 0, (size_t)n * sizeof(double), st));
   col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, B, ldb, B, ldb, rs);
   MGB_LAUNCHED("col_amax");
   std::vector<double> hv(2 * nrhs + 8);
-  MGB_TRY(fetch(red, hv.data(), 2 * (int)nrhs + 8));
-  const double anorm = hv[0];
+  double anorm = 0;
   std::vector<double> bn(nrhs);
-  for (int64_t c = 0; c < nrhs; c++) bn[c] = hv[8 + 2 * c];
   const double eps = sizeof(elem_t) == 8 ? 1.1102230246251565e-16
                                          : 5.960464477539063e-08;
   const double tol = o.tol > 0 ? o.tol : (double)n * eps;
@@ -409,14 +422,28 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   float ms_factor = 0.f;
   for (int attempt = 0; attempt < 2; attempt++) {
     MGB_CUDA(cudaEventRecord(g_ir.e[0], st));
-    to_float_kernel<elem_t><<<grid_cap(n * n), 256, 0, st>>>(n, n, A, lda, W, n);
-    MGB_LAUNCHED("to_float");
+    {
+      constexpr int kChunk = 64;
+      const dim3 g((unsigned)((n + 255) / 256), (unsigned)((n + kChunk - 1) / kChunk));
+      to_float_rowsum_kernel<elem_t><<<g, 256, 0, st>>>(
+          n, A, lda, W, n, attempt == 0 ? rowsum : nullptr, kChunk);
+      MGB_LAUNCHED("to_float");
+      if (attempt == 0) {
+        rowmax_kernel<<<grid_cap(n), 256, 0, st>>>(n, rowsum, red);
+        MGB_LAUNCHED("rowmax");
+      }
+    }
     if (spd)
       MGB_TRY(potrf_t<float>(n, W, n, info, lp));
     else
       MGB_TRY(getrf_t<float>(n, W, n, piv, piv + n, 0.f, lp));
     MGB_CUDA(cudaEventRecord(g_ir.e[1], st));
     MGB_CUDA(cudaEventSynchronize(g_ir.e[1]));
+    if (attempt == 0) {
+      MGB_TRY(fetch(red, hv.data(), 2 * (int)nrhs + 8));
+      anorm = hv[0];
+      for (int64_t c = 0; c < nrhs; c++) bn[c] = hv[8 + 2 * c];
+    }
     float f = 0.f;
     cudaEventElapsedTime(&f, g_ir.e[0], g_ir.e[1]);
     ms_factor += f;
