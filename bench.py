@@ -333,11 +333,12 @@ def tc_roofline(kt):
     gbs = by / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
     tpk = pk.get("bf16_tflops_sustained") or pk.get("bf16_tflops")
     hpk = pk["hbm_gbs"]
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "tc_gemm_traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            traffic = json.load(f).get("bytes_per_launch")
+    # DRAM bytes / algorithmic bytes of one full-size launch measured with ncu
+    # (M = 7904, N = 7760, K = 192, split form: 444.8 MB of 502.7 MB, the
+    # rest of the C traffic served by L2); the C traffic grows with M*N, so
+    # the per-launch traffic here is that ratio times the algorithmic bytes
+    tc_traffic_ratio = 444.76 / 502.7
+    traffic = tc_traffic_ratio * by / cnt if cnt else None
     hbm = {"achieved": gbs, "peak": hpk, "unit": "GB/s", "frac": gbs / hpk}
     ten = {"achieved": tflops, "peak": tpk, "unit": "TFLOP/s",
            "frac": tflops / tpk if tpk else None}
@@ -347,6 +348,8 @@ def tc_roofline(kt):
             "achieved": head["achieved"], "peak": head["peak"],
             "unit": head["unit"], "frac": head["frac"], "traffic": traffic,
             "algorithmic_bytes_per_launch": by / cnt if cnt else None,
+            "traffic_source": "ncu dram__bytes_read+write of one n=8192 launch "
+                              "scaled by algorithmic bytes (0.885 ratio)",
             "hbm": hbm, "tensor": ten,
             "peak_source": f"{src} peaks: hbm_gbs, bf16_tflops_sustained "
                            "(kernel timed inside a long step)"}
@@ -562,10 +565,21 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
         L.dfree(v)
     pk, src = peaks()
     gbs = byt / (ms * 1e-3) / 1e9
+    # algorithmic FLOPs of the reference's path: PLU 2n^3/3, Cholesky n^3/3,
+    # plus the two triangular solves 2n^2 (the kernel's Gauss-Jordan form
+    # does more); the mean intensity (~12 FLOP/B) is above the FP32 FFMA
+    # ridge, so the FP32 fraction is given beside the HBM one
+    nn = ns.astype(np.float64)
+    flops = float(np.sum(np.where(kinds == 0, 2 * nn ** 3 / 3, nn ** 3 / 3) + 2 * nn ** 2))
+    fp32_peak = pk.get("fp32_tflops") or L.c.matgb_measure_fma_peak(0)
+    tfl = flops / (ms * 1e-3) / 1e12
     return {"workload": "batched_100k_uneven_f32", "ms": ms,
             "solves_per_s": count / (ms * 1e-3), "bytes": byt,
             "hbm_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"],
-            "hbm_peak_source": src, "status_nonzero": int((status != 0).sum()),
+            "hbm_peak_source": src, "flops": flops, "tflops": tfl,
+            "fp32_peak_tflops": fp32_peak,
+            "fp32_frac": tfl / fp32_peak if fp32_peak else None,
+            "status_nonzero": int((status != 0).sum()),
             "bwd_err_sample_max": worst}
 
 

@@ -248,6 +248,15 @@ struct RegPanelSmem {
 // A, columns [k0, k0+24)): thread tid of CTA c owns panel rows prow[r]
 // (panel-relative, -1 = none) in a[r][*].  ipiv[k0+kk] (CTA 0) and, when
 // spiv is given, spiv[kk] (every CTA, shared memory) get the global pivot row.
+//
+// Rotating frame: before column kk every row holds column kk in a[r][0],
+// columns kk+1..23 in a[r][1..23-kk] and its finished columns 0..kk-1 in
+// a[r][24-kk..23]; each step rotates the row left by one (live entries get
+// the rank-1 update on the way, the new multiplier lands in a[r][23]), so
+// after 24 steps every row is back in natural order.  The column loop is an
+// ordinary loop over static register indices -- one copy of the step in the
+// instruction stream instead of 24 -- and the arithmetic is exactly that of
+// the unrolled form (the same FMAs on the same operands).
 template <typename T, int R, int NT>
 __device__ __forceinline__ void reg_panel_columns(
     T (&a)[R][kW], const int (&prow)[R], RegPanelSmem<T, NT> &sm,
@@ -255,7 +264,7 @@ __device__ __forceinline__ void reg_panel_columns(
     int32_t *__restrict__ ipiv, int32_t *spiv, T eps) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = NT / 32;
-#pragma unroll
+#pragma unroll 1
   for (int kk = 0; kk < kW; kk++) {
     const int buf = kk & 1;
     T bk = (T)-2;
@@ -263,7 +272,7 @@ __device__ __forceinline__ void reg_panel_columns(
 #pragma unroll
     for (int r = 0; r < R; r++)
       if (prow[r] >= kk) {
-        const T key = piv_key(a[r][kk], prow[r] == kk);
+        const T key = piv_key(a[r][0], prow[r] == kk);
         if (better(key, prow[r], bk, bi)) { bk = key; bi = prow[r]; }
       }
 #pragma unroll
@@ -327,20 +336,21 @@ __device__ __forceinline__ void reg_panel_columns(
         }
       }
     }
-    const T piv = u[kk];
-    if (!(fabs(piv) < eps)) {
-      const T inv = T(1) / piv;
-      T uj[kW];
+    const T piv = u[0];
+    const bool elim = !(fabs(piv) < eps);
+    const T inv = elim ? T(1) / piv : T(0);
+    const int live = kW - 1 - kk;  // columns right of kk
+    T uj[kW];
 #pragma unroll
-      for (int j = kk + 1; j < kW; j++) uj[j] = u[j];
+    for (int j = 1; j < kW; j++) uj[j] = u[j];
 #pragma unroll
-      for (int r = 0; r < R; r++)
-        if (prow[r] > kk) {
-          const T l = a[r][kk] * inv;
-          a[r][kk] = l;
+    for (int r = 0; r < R; r++) {
+      const bool upd = elim && prow[r] > kk;
+      const T l = upd ? a[r][0] * inv : a[r][0];
 #pragma unroll
-          for (int j = kk + 1; j < kW; j++) a[r][j] = fma(-uj[j], l, a[r][j]);
-        }
+      for (int j = 0; j < kW - 1; j++)
+        a[r][j] = (upd && j < live) ? fma(-uj[j + 1], l, a[r][j + 1]) : a[r][j + 1];
+      a[r][kW - 1] = l;
     }
   }
 }
