@@ -570,9 +570,28 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
 // columns right of the panel, and the rank-24 update of the rows below from
 // the L21 rows still in registers.  A cluster barrier separates the phases;
 // data written by another CTA is read with ld.global.cg (L2), so no stale L1
-// line is ever used.  Pivots are never skipped here (the mixed path's
-// threshold is 0), so the block width is free of the reference's grouping.
+// line is ever used.  The panels keep the reference's 24-column width and its
+// pivot-skip rule (eps), so the plain float LU uses it too.
 constexpr int kFusedMaxBw = 144;
+
+// 24 consecutive values from 16-byte aligned shared memory.
+template <typename T>
+struct VecLoad {
+  static __device__ __forceinline__ void get24(const T *p, T (&o)[kW]) {
+#pragma unroll
+    for (int k = 0; k < kW; k++) o[k] = p[k];
+  }
+};
+template <>
+struct VecLoad<float> {
+  static __device__ __forceinline__ void get24(const float *p, float (&o)[kW]) {
+#pragma unroll
+    for (int k = 0; k < kW; k += 4) {
+      const float4 v = *reinterpret_cast<const float4 *>(p + k);
+      o[k] = v.x; o[k + 1] = v.y; o[k + 2] = v.z; o[k + 3] = v.w;
+    }
+  }
+};
 
 template <typename T, int NT>
 struct FusedSmem {
@@ -580,13 +599,13 @@ struct FusedSmem {
   SwapMap map;
   int32_t spiv[kW];
   T L11[kW][kW + 1];
-  T U12[kW][kFusedMaxBw - kW];
+  __align__(16) T U12t[kFusedMaxBw - kW][kW];  // U12 transposed: k contiguous
 };
 
 template <typename T, int R, int NT>
 __global__ void __launch_bounds__(NT, 1)
     lu_block_fused_kernel(T *__restrict__ A, int64_t lda, int64_t n,
-                          int64_t kb, int bw, int32_t *__restrict__ ipiv) {
+                          int64_t kb, int bw, int32_t *__restrict__ ipiv, T eps) {
   __shared__ FusedSmem<T, NT> sm;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
@@ -610,7 +629,7 @@ __global__ void __launch_bounds__(NT, 1)
         a[r][j] = prow[r] >= 0 ? __ldcg(&A[(k0 + prow[r]) + (k0 + j) * lda]) : T(0);
     }
     reg_panel_columns<T, R, NT>(a, prow, sm.ps, cluster, c, CS, rbase, rpc, k0,
-                                ipiv, sm.spiv, T(0));
+                                ipiv, sm.spiv, eps);
 #pragma unroll
     for (int r = 0; r < R; r++)
       if (prow[r] >= 0)
@@ -661,25 +680,41 @@ __global__ void __launch_bounds__(NT, 1)
       if (lane < kW) colp[lane] = x;
     }
     cluster.sync();
-    // rank-24 update of the rows below the panel, right columns
+    // rank-24 update of the rows below the panel, right columns; eight
+    // columns at a time so their L2 loads are all in flight together
     for (int e = tid; e < kW * nright; e += NT) {
       const int i = e % kW, j = e / kW;
-      sm.U12[i][j] = __ldcg(&A[(k0 + i) + (k0 + kW + j) * lda]);
+      sm.U12t[j][i] = __ldcg(&A[(k0 + i) + (k0 + kW + j) * lda]);
     }
     __syncthreads();
-    for (int j = 0; j < nright; j++) {
-      T uj[kW];
-#pragma unroll
-      for (int k = 0; k < kW; k++) uj[k] = sm.U12[k][j];
-      T *colp = A + (k0 + kW + j) * lda + k0;
+    constexpr int JB = 8;
+    T *base = A + (k0 + kW) * lda + k0;
+    for (int j0 = 0; j0 < nright; j0 += JB) {
+      T v[R][JB];
 #pragma unroll
       for (int r = 0; r < R; r++)
-        if (prow[r] >= kW) {
-          T acc = __ldcg(&colp[prow[r]]);
 #pragma unroll
-          for (int k = 0; k < kW; k++) acc = fma(-a[r][k], uj[k], acc);
-          colp[prow[r]] = acc;
+        for (int jj = 0; jj < JB; jj++)
+          v[r][jj] = (prow[r] >= kW && j0 + jj < nright)
+                         ? __ldcg(&base[(int64_t)(j0 + jj) * lda + prow[r]])
+                         : T(0);
+#pragma unroll
+      for (int jj = 0; jj < JB; jj++) {
+        if (j0 + jj < nright) {
+          T uj[kW];
+          VecLoad<T>::get24(&sm.U12t[j0 + jj][0], uj);
+#pragma unroll
+          for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int k = 0; k < kW; k++) v[r][jj] = fma(-a[r][k], uj[k], v[r][jj]);
         }
+      }
+#pragma unroll
+      for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int jj = 0; jj < JB; jj++)
+          if (prow[r] >= kW && j0 + jj < nright)
+            base[(int64_t)(j0 + jj) * lda + prow[r]] = v[r][jj];
     }
     cluster.sync();
   }
@@ -987,7 +1022,7 @@ int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
 // (float; rows n-kb <= 16 CTAs x 1024); *done = false otherwise.
 template <typename T>
 static int try_fused_block(T *A, int64_t lda, int64_t n, int64_t kb, int bw,
-                           int32_t *ipiv, bool *done) {
+                           int32_t *ipiv, T eps, bool *done) {
   *done = false;
   if constexpr (sizeof(T) != 4) {
     return 0;
@@ -1020,11 +1055,11 @@ static int try_fused_block(T *A, int64_t lda, int64_t n, int64_t kb, int bw,
     if (R == 1) {
       auto kern = lu_block_fused_kernel<T, 1, 512>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps);
     } else {
       auto kern = lu_block_fused_kernel<T, 2, 512>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps);
     }
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -1121,9 +1156,9 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
   // main -> hi: everything queued so far (input copies, perm init)
   MGB_CUDA(cudaEventRecord(g_la.ev[0], main));
   MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[0], 0));
-  // mixed path (float, tensor-core updates): 144-column blocks factored by
-  // one fused cluster launch each where they fit
-  const bool fused = lp >= 0 && sizeof(T) == 4;
+  // float (plain and mixed): 144-column blocks factored by one fused cluster
+  // launch each where they fit
+  const bool fused = sizeof(T) == 4;
   const int64_t NB = fused ? kFusedMaxBw : lp >= 0 ? kOuterBlockLp : kOuterBlock;
   for (int64_t kb = 0; kb < n; kb += NB) {
     const int64_t nb = (n - kb) < NB ? (n - kb) : NB;
@@ -1132,7 +1167,7 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       StreamSwap sw(hi);
       bool done = false;
       if (fused && nb == NB)
-        MGB_TRY(try_fused_block<T>(A, lda, n, kb, (int)nb, ipiv, &done));
+        MGB_TRY(try_fused_block<T>(A, lda, n, kb, (int)nb, ipiv, eps, &done));
       if (!done) MGB_TRY(factor_block<T>(n, A, lda, kb, ke, ipiv, eps));
     }
     MGB_CUDA(cudaEventRecord(g_la.ev[1], hi));
