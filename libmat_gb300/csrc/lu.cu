@@ -197,13 +197,40 @@ __global__ void __launch_bounds__(kPanelThreads, 1)
   }
 }
 
+// A float pivot key as an unsigned integer with the same order: the special
+// keys -3 (empty) < -2 (no candidate) < -1 (NaN below the top) map to 0, 1,
+// 2, and |a| >= 0 (+inf for a NaN at the top) to its bit pattern + 4
+// (non-negative floats order like their bit patterns).
+__device__ __forceinline__ unsigned ukey(float k) {
+  return k >= 0.f ? __float_as_uint(k) + 4u : (k == -1.f ? 2u : k == -2.f ? 1u : 0u);
+}
+
+// Warp-wide best (key, index): largest key, then smallest index (two redux
+// operations); every lane gets the winner's key code and index.
+__device__ __forceinline__ void warp_best(unsigned uk, int idx, unsigned &bk,
+                                          int &bi) {
+  bk = __reduce_max_sync(0xffffffffu, uk);
+  const unsigned mi = __reduce_min_sync(0xffffffffu, uk == bk ? (unsigned)idx : 0xffffffffu);
+  bi = (int)mi;
+}
+
 // Best (key, index) of cnt <= 32 candidates in shared memory, reduced across
-// the warp by shuffles (every lane gets the result and the winner's slot).
-// Ties between real candidates cannot happen (their indices are distinct).
+// the warp (every lane gets the result and the winner's slot).  Ties between
+// real candidates cannot happen (their indices are distinct).
 template <typename T>
 __device__ __forceinline__ void pick_best(const T *keys, const int *idxs,
                                           int cnt, T &bk, int &bi, int &bw) {
   const int lane = threadIdx.x & 31;
+  if constexpr (sizeof(T) == 4) {
+    const T k = lane < cnt ? keys[lane] : (T)-3;
+    const int i = lane < cnt ? idxs[lane] : INT_MAX;
+    unsigned ub;
+    warp_best(ukey(k), i, ub, bi);
+    const unsigned hit = __ballot_sync(0xffffffffu, lane < cnt && i == bi && ukey(k) == ub);
+    bw = hit ? __ffs(hit) - 1 : 0;
+    bk = __shfl_sync(0xffffffffu, k, bw);
+    return;
+  }
   T k = lane < cnt ? keys[lane] : (T)-3;
   int i = lane < cnt ? idxs[lane] : INT_MAX;
   int w = lane;
@@ -234,15 +261,42 @@ constexpr int kW = kRefBlock;
 
 template <typename T, int NT>
 struct RegPanelSmem {
-  T wrow[NT / 32][kW];
-  T krow[kW];
+  __align__(16) T wrow[NT / 32][kW];
+  __align__(16) T krow[kW];
   T wkey[NT / 32];
   int widx[NT / 32];
-  T xval[2][16][kW];
+  __align__(16) T xval[2][16][kW];
   T xkey[2][16];
   int xidx[2][16];
-  T kval[2][kW];
+  __align__(16) T kval[2][kW];
 };
+
+// A 24-value row to / from 16-byte aligned shared memory (vector accesses
+// for float).
+template <typename T>
+__device__ __forceinline__ void row_put(T *dst, const T (&v)[kW]) {
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll
+    for (int j = 0; j < kW; j += 4)
+      *reinterpret_cast<float4 *>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < kW; j++) dst[j] = v[j];
+  }
+}
+template <typename T>
+__device__ __forceinline__ void row_get(const T *src, T (&v)[kW]) {
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll
+    for (int j = 0; j < kW; j += 4) {
+      const float4 f = *reinterpret_cast<const float4 *>(src + j);
+      v[j] = f.x; v[j + 1] = f.y; v[j + 2] = f.z; v[j + 3] = f.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kW; j++) v[j] = src[j];
+  }
+}
 
 // The 24-column elimination of a register-resident panel (rows [k0, n) of
 // A, columns [k0, k0+24)): thread tid of CTA c owns panel rows prow[r]
@@ -275,23 +329,23 @@ __device__ __forceinline__ void reg_panel_columns(
         const T key = piv_key(a[r][0], prow[r] == kk);
         if (better(key, prow[r], bk, bi)) { bk = key; bi = prow[r]; }
       }
+    if constexpr (sizeof(T) == 4) {
+      unsigned ub;
+      warp_best(ukey(bk), bi, ub, bi);
+      bk = __shfl_sync(0xffffffffu, bk, __ffs(__ballot_sync(0xffffffffu, ukey(bk) == ub)) - 1);
+    } else {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const T ok = __shfl_xor_sync(0xffffffffu, bk, off);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-      if (better(ok, oi, bk, bi)) { bk = ok; bi = oi; }
+      for (int off = 16; off > 0; off >>= 1) {
+        const T ok = __shfl_xor_sync(0xffffffffu, bk, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (better(ok, oi, bk, bi)) { bk = ok; bi = oi; }
+      }
     }
     // every lane now holds the warp's best; its owner stages the row
 #pragma unroll
     for (int r = 0; r < R; r++) {
-      if (prow[r] >= 0 && prow[r] == bi) {
-#pragma unroll
-        for (int j = 0; j < kW; j++) sm.wrow[warp][j] = a[r][j];
-      }
-      if (prow[r] == kk) {
-#pragma unroll
-        for (int j = 0; j < kW; j++) sm.krow[j] = a[r][j];
-      }
+      if (prow[r] >= 0 && prow[r] == bi) row_put<T>(&sm.wrow[warp][0], a[r]);
+      if (prow[r] == kk) row_put<T>(&sm.krow[0], a[r]);
     }
     if (lane == 0) { sm.wkey[warp] = bk; sm.widx[warp] = bi; }
     __syncthreads();
@@ -341,8 +395,7 @@ __device__ __forceinline__ void reg_panel_columns(
     const T inv = elim ? T(1) / piv : T(0);
     const int live = kW - 1 - kk;  // columns right of kk
     T uj[kW];
-#pragma unroll
-    for (int j = 1; j < kW; j++) uj[j] = u[j];
+    row_get<T>(u, uj);
 #pragma unroll
     for (int r = 0; r < R; r++) {
       const bool upd = elim && prow[r] > kk;
