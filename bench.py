@@ -266,7 +266,7 @@ def run_headline(args, mg):
     L.sync()
     kt = ktable(L)
     L.c.matgb_ktime_enable(0)
-    rl = tc_roofline(kt)
+    rl = roofline_block(kt)
 
     # plain FP64 GPU LU + solve of the kappa = 1e4 system (same API family)
     A = mats[1e4]
@@ -318,41 +318,61 @@ def run_headline(args, mg):
     }
 
 
-def tc_roofline(kt):
-    """Roofline of the tensor-core trailing update: a rank-128 update reads and
-    writes its FP32 C tile once for 2*128 (x3 split) flops per element, so it
-    is bound by HBM unless the tensor fraction is the larger one; both are
-    given, the binding one is the headline."""
+def kernel_roofline(kt, name, traffic_ratio=None, note=None):
+    """Roofline of one kernel from the library's per-kernel event timing:
+    achieved algorithmic bytes/s against the measured HBM peak and
+    algorithmic FLOP/s against the measured BF16 (tensor) peak; the larger
+    fraction is the binding one."""
     pk, src = peaks()
     tot = sum(r[2] for r in kt) or 1.0
-    tc = [r for r in kt if r[0].startswith("tc_gemm")]
-    if not tc:
+    rows = [r for r in kt if r[0] == name]
+    if not rows:
         return None
-    name, cnt, ms, fl, by = tc[0]
+    _, cnt, ms, fl, by = rows[0]
     tflops = fl / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
     gbs = by / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
     tpk = pk.get("bf16_tflops_sustained") or pk.get("bf16_tflops")
     hpk = pk["hbm_gbs"]
-    # DRAM bytes / algorithmic bytes of one full-size launch measured with ncu
-    # (M = 7904, N = 7760, K = 192, split form: 444.8 MB of 502.7 MB, the
-    # rest of the C traffic served by L2); the C traffic grows with M*N, so
-    # the per-launch traffic here is that ratio times the algorithmic bytes
-    tc_traffic_ratio = 444.76 / 502.7
-    traffic = tc_traffic_ratio * by / cnt if cnt else None
     hbm = {"achieved": gbs, "peak": hpk, "unit": "GB/s", "frac": gbs / hpk}
     ten = {"achieved": tflops, "peak": tpk, "unit": "TFLOP/s",
            "frac": tflops / tpk if tpk else None}
     bound = "hbm" if hbm["frac"] >= (ten["frac"] or 0) else "tensor"
     head = hbm if bound == "hbm" else ten
-    return {"kernel": name, "bound": bound, "launches": cnt, "share": ms / tot,
-            "achieved": head["achieved"], "peak": head["peak"],
-            "unit": head["unit"], "frac": head["frac"], "traffic": traffic,
-            "algorithmic_bytes_per_launch": by / cnt if cnt else None,
-            "traffic_source": "ncu dram__bytes_read+write of one n=8192 launch "
-                              "scaled by algorithmic bytes (0.885 ratio)",
-            "hbm": hbm, "tensor": ten,
-            "peak_source": f"{src} peaks: hbm_gbs, bf16_tflops_sustained "
-                           "(kernel timed inside a long step)"}
+    out = {"kernel": name, "bound": bound, "launches": cnt, "share": ms / tot,
+           "ms_total": ms, "achieved": head["achieved"], "peak": head["peak"],
+           "unit": head["unit"], "frac": head["frac"],
+           "traffic": traffic_ratio * by / cnt if (traffic_ratio and cnt) else None,
+           "algorithmic_bytes_per_launch": by / cnt if cnt else None,
+           "algorithmic_flop_per_launch": fl / cnt if cnt else None,
+           "hbm": hbm, "tensor": ten,
+           "peak_source": f"{src} peaks: hbm_gbs, bf16_tflops_sustained "
+                          "(kernels timed inside a long step)"}
+    if note:
+        out["note"] = note
+    return out
+
+
+def roofline_block(kt):
+    """The dominant kernel (most GPU time in a solve) is the fused block
+    factorisation -- the critical path, bound by the latency of one cluster
+    exchange per column, far below both roofs; the split tensor-core update
+    beside it is HBM-bound."""
+    top = kt[0][0] if kt else None
+    rl = kernel_roofline(
+        kt, top,
+        note="latency-bound panel chain: one cluster-wide pivot exchange "
+             "(DSMEM + barrier.cluster) per column; algorithmic bytes = the "
+             "144-column block read and written once (2*m*144*4), FLOP = m*144^2"
+        if top == "lu_block_fused" else None)
+    # DRAM bytes / algorithmic bytes of one full-size tensor-core launch
+    # measured with ncu (M = 7904, N = 7760, K = 192, split form: 444.8 MB of
+    # 502.7 MB, the rest of the C traffic served by L2); the C traffic grows
+    # with M*N, so the per-launch traffic is that ratio times the algorithmic
+    # bytes
+    tc = next((r[0] for r in kt if r[0].startswith("tc_gemm")), None)
+    if rl is not None and tc is not None and tc != top:
+        rl["tensor_update"] = kernel_roofline(kt, tc, traffic_ratio=444.76 / 502.7)
+    return rl
 
 
 def e2e_mixed(L, mg, A, b, flops, opts, ke):
@@ -548,6 +568,12 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
     L.check(L.c.matgb_event_record(1), "ev")
     L.sync()
     ms = L.c.matgb_event_elapsed_ms(0, 1) / steps
+    # per-queue kernel times of one more pass
+    L.c.matgb_ktime_enable(1)
+    run()
+    L.sync()
+    kt = ktable(L)
+    L.c.matgb_ktime_enable(0)
     byt = 4 * (totA + 2 * totv)
     status = np.empty(count, np.int32)
     L.d2h(status, st)
@@ -580,7 +606,8 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
             "fp32_peak_tflops": fp32_peak,
             "fp32_frac": tfl / fp32_peak if fp32_peak else None,
             "status_nonzero": int((status != 0).sum()),
-            "bwd_err_sample_max": worst}
+            "bwd_err_sample_max": worst,
+            "kernels": [{"name": r[0], "ms": round(r[2], 4)} for r in kt]}
 
 
 # ----------------------------------------------------------------- CPU legs

@@ -78,11 +78,32 @@ struct SlotLen {
   static constexpr int v = NB + 4;
 };
 
+// Pivot keys: float |a| as an unsigned integer with the same order (see
+// fkey), so a warp finds its best candidate with two redux operations; the
+// double build compares the values themselves.
+template <typename T>
+struct PivKey {
+  using type = T;
+};
+template <>
+struct PivKey<float> {
+  using type = unsigned;
+};
+
+// Unsigned key of a float pivot candidate: no candidate 0 < NaN below the top
+// row 1 < |a| (its bit pattern + 2; non-negative floats order like their
+// bits); a NaN in the top row ranks as +inf, as bkey does.
+__device__ __forceinline__ unsigned fkey(float v, bool first) {
+  const float a = fabsf(v);
+  if (a != a) return first ? 0x7f800002u : 1u;
+  return __float_as_uint(a) + 2u;
+}
+
 template <typename T, int NB>
 struct BatchSmem {
   __align__(16) T slot[2][Warps<NB>::v][SlotLen<NB>::v];  // by step parity
-  T wkey[2][Warps<NB>::v];
-  int widx[2][Warps<NB>::v];
+  __align__(16) typename PivKey<T>::type wkey[2][4];        // per warp
+  __align__(16) int widx[2][4];
 };
 
 template <typename T>
@@ -112,24 +133,33 @@ struct VecOf<double> {
   }
 };
 
-// Write the owned row (its live entries) and its right-hand side into a slot
-// with 16-byte stores: slot[3] = a[0], then (a[Wg+1..Wg+W]) at slot[4+Wg], the
-// last group ending with the right-hand side at slot[NB+3].
+// Write the owned row and its right-hand side into a slot with 16-byte
+// stores: slot[3] = a[0], then a[1..NB-1] and the right-hand side at
+// slot[4..NB+3], in chunks of Chunk columns -- a chunk is written when it
+// holds a live entry (the test shift_update makes before reading it), else
+// only the right-hand side, when it falls in the last chunk.
 template <typename T, int NB>
 __device__ __forceinline__ void put_row(T *slot, const T (&a)[NB], T rb,
                                         int n_live) {
   constexpr int W = VecOf<T>::w;
+  constexpr int C = Chunk<NB>::v;
+  constexpr int NC = NB / C;
   slot[3] = a[0];
 #pragma unroll
-  for (int g = 0; g < NB / W; g++) {
-    if (W * g + 1 < n_live || g == NB / W - 1) {
-      T v[W];
+  for (int c = 0; c < NC; c++) {
+    if (c * C + 1 < n_live) {
 #pragma unroll
-      for (int q = 0; q < W; q++) {
-        const int k = W * g + 1 + q;
-        v[q] = k < NB ? a[k] : rb;
+      for (int g = c * C / W; g < (c + 1) * C / W; g++) {
+        T v[W];
+#pragma unroll
+        for (int q = 0; q < W; q++) {
+          const int k = W * g + 1 + q;
+          v[q] = k < NB ? a[k] : rb;
+        }
+        VecOf<T>::put(slot + 4 + W * g, v);
       }
-      VecOf<T>::put(slot + 4 + W * g, v);
+    } else if (c == NC - 1) {
+      slot[NB + 3] = rb;
     }
   }
 }
@@ -210,35 +240,64 @@ __device__ int solve_one(const T *__restrict__ A, int n,
     int pw = 0;
     if (KIND == 0 && K < n - 1) {
       const bool cand = act && lr >= K;
-      T key = cand ? bkey(a[0], lr == K) : (T)-2;
-      int idx = cand ? lr : 0x7fffffff;
-#pragma unroll
-      for (int off = (NB <= 16 ? 8 : 16); off > 0; off >>= 1) {
-        const T ok = __shfl_xor_sync(gm, key, off);
-        const int oi = __shfl_xor_sync(gm, idx, off);
-        if (ok > key || (ok == key && oi < idx)) {
-          key = ok;
-          idx = oi;
+      if constexpr (sizeof(T) == 4 && NB >= 32) {
+        // warp best by two redux operations on the integer keys: the
+        // largest key, then the smallest logical row holding it
+        const unsigned key = cand ? fkey(a[0], lr == K) : 0u;
+        const unsigned wk = __reduce_max_sync(0xffffffffu, key);
+        const unsigned wi = __reduce_min_sync(
+            0xffffffffu, (cand && key == wk) ? (unsigned)lr : 0x7fffffffu);
+        // lane 0 publishes the warp's best as (key, row << 2 | warp); the
+        // rows are distinct, so the smallest code among the best keys is
+        // the smallest row and names its warp's slot
+        if ((i & 31) == 0) {
+          sm.wkey[par][w] = wk;
+          sm.widx[par][w] = (int)((wi << 2) | (unsigned)w);
         }
-      }
-      // every warp publishes its best key (-2: no candidate left in it)
-      if ((i & 31) == 0) {
-        sm.wkey[par][w] = key;
-        sm.widx[par][w] = idx;
-      }
-      if (cand && lr == idx) put_row<T, NB>(sm.slot[par][w], a, rb, live);
-      gsync<NB>();
-      p = sm.widx[par][0];
-      if constexpr (Warps<NB>::v > 1) {
-        T bk = sm.wkey[par][0];
+        if (cand && (unsigned)lr == wi) put_row<T, NB>(sm.slot[par][w], a, rb, live);
+        gsync<NB>();
+        if constexpr (Warps<NB>::v == 1) {
+          p = (int)wi;
+        } else {
+          const int lane = i & 31;
+          const unsigned ck = lane < Warps<NB>::v ? sm.wkey[par][lane] : 0u;
+          const unsigned ci = lane < Warps<NB>::v ? (unsigned)sm.widx[par][lane] : 0xffffffffu;
+          const unsigned bk = __reduce_max_sync(0xffffffffu, ck);
+          const unsigned bi = __reduce_min_sync(0xffffffffu, ck == bk ? ci : 0xffffffffu);
+          p = (int)(bi >> 2);
+          pw = (int)(bi & 3u);
+        }
+      } else {
+        T key = cand ? bkey(a[0], lr == K) : (T)-2;
+        int idx = cand ? lr : 0x7fffffff;
 #pragma unroll
-        for (int q = 1; q < Warps<NB>::v; q++) {
-          const T kq = sm.wkey[par][q];
-          const int iq = sm.widx[par][q];
-          if (kq > bk || (kq == bk && iq < p)) {
-            bk = kq;
-            p = iq;
-            pw = q;
+        for (int off = (NB <= 16 ? 8 : 16); off > 0; off >>= 1) {
+          const T ok = __shfl_xor_sync(gm, key, off);
+          const int oi = __shfl_xor_sync(gm, idx, off);
+          if (ok > key || (ok == key && oi < idx)) {
+            key = ok;
+            idx = oi;
+          }
+        }
+        // every warp publishes its best key (-2: no candidate left in it)
+        if ((i & 31) == 0) {
+          sm.wkey[par][w] = key;
+          sm.widx[par][w] = idx;
+        }
+        if (cand && lr == idx) put_row<T, NB>(sm.slot[par][w], a, rb, live);
+        gsync<NB>();
+        p = sm.widx[par][0];
+        if constexpr (Warps<NB>::v > 1) {
+          T bk = sm.wkey[par][0];
+#pragma unroll
+          for (int q = 1; q < Warps<NB>::v; q++) {
+            const T kq = sm.wkey[par][q];
+            const int iq = sm.widx[par][q];
+            if (kq > bk || (kq == bk && iq < p)) {
+              bk = kq;
+              p = iq;
+              pw = q;
+            }
           }
         }
       }
