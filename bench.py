@@ -268,8 +268,12 @@ def run_headline(args, mg):
     L.c.matgb_ktime_enable(0)
     rl = roofline_block(kt)
 
-    # plain FP64 GPU LU + solve of the kappa = 1e4 system (same API family)
+    # end to end through mat_solve_ir with pinned host buffers (kappa = 1e4),
+    # measured before the long FP64 leg below
     A = mats[1e4]
+    e2e = e2e_mixed(L, mg, A, b, flops, opts, max(3, min(args.steps, 5)))
+
+    # plain FP64 GPU LU + solve of the kappa = 1e4 system (same API family)
     Aw = torch.empty_like(A)
     piv = torch.empty(2 * n, device="cuda", dtype=torch.int32)
     xp = torch.empty_like(b)
@@ -294,8 +298,6 @@ def run_headline(args, mg):
                                   for kk, d in per_kappa.items()}}
     del Aw, xp
 
-    # end to end through mat_solve_ir with pinned host buffers (kappa = 1e4)
-    e2e = e2e_mixed(L, mg, A, b, flops, opts, max(1, min(args.steps, 3)))
     for k in list(mats):
         del mats[k]
     torch.cuda.empty_cache()
@@ -392,17 +394,23 @@ def e2e_mixed(L, mg, A, b, flops, opts, ke):
     rep = mg.MatIRReport()
     L.check(L.c.mat_solve_ir(C.byref(MX), C.byref(MA), C.byref(MB),
                              C.byref(opts), C.byref(rep)), "mat_solve_ir")
-    t0 = time.perf_counter()
+    # each call timed on its own (host clock: it includes the copies and the
+    # synchronisation); the median is reported, every sample beside it
+    samples = []
+    ok = 1
     for _ in range(ke):
+        t0 = time.perf_counter()
         L.check(L.c.mat_solve_ir(C.byref(MX), C.byref(MA), C.byref(MB),
                                  C.byref(opts), C.byref(rep)), "mat_solve_ir")
-    ms = (time.perf_counter() - t0) / ke * 1e3
-    ok = rep.converged
+        samples.append((time.perf_counter() - t0) * 1e3)
+        ok = ok and rep.converged
+    ms = float(np.median(samples))
     for p in (hA, hb, hx):
         L.c.matgb_host_free(p)
     return {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
             "h2d_bytes_per_step": n * n * es + n * es, "d2h_bytes_per_step": n * es,
-            "ms_per_step": ms, "converged": int(ok),
+            "ms_per_step": ms, "ms_samples": [round(v, 2) for v in samples],
+            "converged": int(ok),
             "api": "mat_solve_ir (host Mat/Vec, pinned), kappa = 1e4"}
 
 

@@ -4,6 +4,8 @@
 // the kernels compile in parallel.
 #pragma once
 
+#include <type_traits>
+
 #include "internal.cuh"
 
 namespace mgb {
@@ -328,6 +330,104 @@ __device__ int solve_one(const T *__restrict__ A, int n,
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// SPD systems: LDL^T elimination on the lower triangle (all that mat_chol
+// reads), thread i owning row i, no exchanges.  Before step K row i >= K
+// holds A^(K)[i][K..i] in a[0..i-K] (shifted frame, pivot column in a[0]).
+// Step K: every row i >= K publishes its a[0] -- column K of the Schur
+// complement, d_K = the pivot at its head -- and row K its right-hand side
+// y_K; after the group barrier every row i > K takes l = a[0]/d_K and
+// a[m] <- a[m+1] - l * col_K[m+1] over its i-K live entries, y_i -= l*y_K.
+// A pivot d_K <= 0 (mat_chol's test, NaN passes) makes the status -1 and
+// leaves x untouched.  A warp whose rows are all done takes no updates.
+// The published columns stay in shared memory (triangular, each column's
+// entries 16-byte aligned for the vector loads) and give the back
+// substitution x_K = (y_K - sum_{i>K} col_K[i-K] x_i) * (1/d_K), one unknown
+// per barrier, every row folding each new x into its own sum.
+template <int NB>
+struct SpdCols {
+  // sum over K of roundup4(NB - K + 3), plus the reach of one chunk past
+  // the last column's entries
+  static constexpr int v = [] {
+    int s = 0;
+    for (int K = 0; K < NB; K++) s += (NB - K + 3 + 3) / 4 * 4;
+    return s + 40;
+  }();
+};
+
+template <typename T, int NB>
+struct SpdSmem {
+  __align__(16) T cols[SpdCols<NB>::v];
+  T ys[NB];
+  T xs[NB];
+};
+
+template <typename T, int NB>
+__device__ int solve_spd(const T *__restrict__ A, int n,
+                         const T *__restrict__ b, T *__restrict__ x,
+                         SpdSmem<T, NB> &sm, int i) {
+  constexpr int C = Chunk<NB>::v;
+  constexpr int W = VecOf<T>::w;
+  constexpr int GW = NB < 32 ? NB : 32;  // rows of one warp (half warp)
+  const bool act = i < n;
+  T a[NB];
+  T rb = act ? b[i] : T(0);
+#pragma unroll
+  for (int j = 0; j < NB; j++) a[j] = (act && j <= i && j < n) ? A[i + (int64_t)j * n] : T(0);
+  // last row of this thread's warp (half warp) that belongs to the system
+  const int wlast = ((i | (GW - 1)) < n - 1 ? (i | (GW - 1)) : n - 1);
+  T rdg = T(1);  // 1 / this row's pivot
+  int myoff = 0;
+  int off = 0;
+  for (int K = 0; K < n; K++) {
+    T *col = sm.cols + off;
+    if (act && i >= K) col[3 + (i - K)] = a[0];
+    if (i == K) {
+      sm.ys[K] = rb;
+      myoff = off;
+    }
+    gsync<NB>();
+    const T d = col[3];
+    if (d <= T(0)) return -1;  // NaN passes, as in mat_chol
+    const T rd = T(1) / d;
+    if (i == K) rdg = rd;
+    const int n_out = wlast - K;  // the warp's longest remaining row
+    if (n_out > 0) {
+      const T l = (act && i > K) ? a[0] * rd : T(0);
+#pragma unroll
+      for (int c = 0; c < NB / C; c++) {
+        if (c * C < n_out) {
+#pragma unroll
+          for (int j0 = c * C; j0 < c * C + C; j0 += W) {
+            T u[W];
+            VecOf<T>::get(col + j0 + 4, u);
+#pragma unroll
+            for (int q = 0; q < W; q++) {
+              const int j = j0 + q;
+              if (j + 1 < NB) a[j] = fma(-u[q], l, a[j + 1]);
+            }
+          }
+        }
+      }
+      rb = fma(-sm.ys[K], l, rb);
+    }
+    off += (n - K + 3 + 3) / 4 * 4;
+  }
+  // back substitution, rb = y_i: one unknown per barrier from the last up,
+  // every earlier row folding it into its sum
+  T xi = T(0);
+  for (int K = n - 1; K >= 0; K--) {
+    if (i == K) {
+      xi = rb * rdg;
+      sm.xs[K] = xi;
+    }
+    gsync<NB>();
+    if (act && i < K) rb = fma(-sm.cols[myoff + 3 + (K - i)], sm.xs[K], rb);
+  }
+  if (act) x[i] = xi;
+  return 0;
+}
+
 // Resident CTAs per SM asked of the register allocator for the two largest
 // buckets (the row itself takes NB registers): 3 x 128 and 4 x 96 threads.
 template <int NB>
@@ -344,7 +444,8 @@ __global__ void __launch_bounds__(Tpg<NB>::v *GROUPS, MinCtas<NB>::v)
                    const int64_t *__restrict__ offv, const T *__restrict__ b,
                    T *__restrict__ x, int32_t *__restrict__ status, T eps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  BatchSmem<T, NB> *smem = reinterpret_cast<BatchSmem<T, NB> *>(smem_raw);
+  using Smem = typename std::conditional<KIND == 1, SpdSmem<T, NB>, BatchSmem<T, NB>>::type;
+  Smem *smem = reinterpret_cast<Smem *>(smem_raw);
   __shared__ int take[GROUPS];
   constexpr int TPG = Tpg<NB>::v;
   const int g = threadIdx.x / TPG, i = threadIdx.x % TPG;
@@ -360,8 +461,12 @@ __global__ void __launch_bounds__(Tpg<NB>::v *GROUPS, MinCtas<NB>::v)
     const int s = list[base + t];
     const int n = nvec[s];
     if (n < 1 || n > NB) continue;  // unsupported order: reported by the driver
-    const int st = solve_one<T, NB, KIND>(A + offA[s], n, b + offv[s],
-                                          x + offv[s], smem[g], i, eps);
+    int st;
+    if constexpr (KIND == 1)
+      st = solve_spd<T, NB>(A + offA[s], n, b + offv[s], x + offv[s], smem[g], i);
+    else
+      st = solve_one<T, NB, KIND>(A + offA[s], n, b + offv[s], x + offv[s],
+                                  smem[g], i, eps);
     if (i == 0) status[s] = st;
     gsync<NB>();
   }
@@ -374,7 +479,8 @@ int launch_batched_queue(int queue, const int32_t *list, BatchQueues *q,
                          int32_t *status, T eps) {
   auto k = batched_kernel<T, NB, GROUPS, KIND>;
   constexpr int threads = Tpg<NB>::v * GROUPS;
-  const size_t smem = sizeof(BatchSmem<T, NB>) * GROUPS;
+  using Smem = typename std::conditional<KIND == 1, SpdSmem<T, NB>, BatchSmem<T, NB>>::type;
+  const size_t smem = sizeof(Smem) * GROUPS;
   static bool attr = false;
   if (!attr) {
     MGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
