@@ -27,6 +27,8 @@ int d2h(void *h, const void *d, size_t bytes) {
 }
 int sync() {
   MGB_CUDA(cudaStreamSynchronize(ctx()->stream));
+  if (lu_wait_error(1))
+    return set_error(MATGB_ERR_TIMEOUT, "LU panel exchange gave up waiting");
   return 0;
 }
 

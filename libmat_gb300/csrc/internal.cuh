@@ -149,6 +149,9 @@ template <typename T>
 int potrs_t(int64_t n, int64_t nrhs, const T *L, int64_t lda, T *B,
             int64_t ldb, const int32_t *info);
 int tc_error_flag(int clear);
+// 1 when an LU panel's column exchange gave up waiting (lu.cu); read after a
+// stream synchronisation.
+int lu_wait_error(int clear);
 // Flexible GMRES for the refinement correction (krylov.cu): solves A d = r0
 // with r0 in V(:, 0) on entry; V holds m + 1 and Z m vectors of length n, F
 // 2n floats; stops when the residual estimate is <= max(rtol*|r0|, atol).

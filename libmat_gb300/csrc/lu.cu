@@ -255,7 +255,8 @@ __device__ __forceinline__ void pick_best(const T *keys, const int *idxs,
 // registers; the column loop is unrolled so every register index is static.
 // Per column: arg-max over owned rows, warp shuffles, each warp's candidate
 // row staged in shared memory, CTA-level pick, DSMEM publication of the CTA
-// candidate (and of row kk) to every CTA, one cluster barrier, swap, scale,
+// candidate (and of row kk) to every CTA by st.async completing on the
+// receiver's own mbarrier (no cluster barrier per column), swap, scale,
 // rank-1 update in registers.
 constexpr int kW = kRefBlock;
 
@@ -266,10 +267,116 @@ struct RegPanelSmem {
   T wkey[NT / 32];
   int widx[NT / 32];
   __align__(16) T xval[2][16][kW];
-  T xkey[2][16];
+  __align__(8) T xkey[2][16];
   int xidx[2][16];
   __align__(16) T kval[2][kW];
+  // exchange barriers by step parity: the arm (with the step's expected
+  // bytes from the other CTAs), one arrival per local warp once its share of
+  // the local copy is stored, and the other CTAs' st.async bytes
+  __align__(8) uint64_t xbar[2];
 };
+
+// Device flag: a panel exchange gave up waiting (never expected; a lost
+// transfer ends the wait instead of hanging the GPU).
+__device__ int g_lu_wait_err = 0;
+
+namespace xch {
+__device__ __forceinline__ uint32_t saddr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// the same shared-memory offset in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t mapa(uint32_t a, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+__device__ __forceinline__ void fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void arm(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Bounded wait for the phase with the given parity (acquire at cluster
+// scope: the bytes were written by other CTAs' st.async).  Gives up after
+// about 2^25 cycles (~16 ms; a column's exchange takes microseconds), or at
+// once when an earlier wait has already given up, so a lost transfer costs
+// one timeout, not one per column.
+__device__ __forceinline__ bool wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t a = saddr(bar);
+  long long t0 = 0;
+  for (int i = 0;; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 15) == 15) {
+      const long long now = clock64();
+      if (t0 == 0)
+        t0 = now;
+      else if (now - t0 > (1ll << 25))
+        return false;
+      if (*reinterpret_cast<volatile int *>(&g_lu_wait_err)) return false;
+    }
+  }
+}
+__device__ __forceinline__ void put16(uint32_t dst, const void *src, uint32_t bar) {
+  const uint4 v = *reinterpret_cast<const uint4 *>(src);
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];"
+      ::"r"(dst), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void put4(uint32_t dst, uint32_t v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];"
+               ::"r"(dst), "r"(v), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void put8(uint32_t dst, uint64_t v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];"
+               ::"r"(dst), "l"(v), "r"(bar)
+               : "memory");
+}
+}  // namespace xch
+
+// Bytes a CTA receives from the other CTAs per column: each one's candidate
+// row, key and index, plus row kk when another CTA owns it (a CTA's own
+// contributions are plain shared-memory stores).
+template <typename T>
+__host__ __device__ constexpr uint32_t xch_bytes(int cs, bool kk_remote) {
+  return (uint32_t)((cs - 1) * (kW * sizeof(T) + sizeof(T) + sizeof(int)) +
+                    (kk_remote ? kW * sizeof(T) : 0));
+}
+
+// Exchange set-up at the start of a panel kernel: both barriers initialised
+// (one arrival for the arm plus one per warp) and armed for the first two
+// columns (owner0/owner1: CTAs holding their rows kk), then one cluster
+// barrier so no CTA sends before every receiver's barriers exist.
+template <typename T, int NT>
+__device__ __forceinline__ void xch_setup(RegPanelSmem<T, NT> &sm, cg::cluster_group &cluster,
+                                          int cs, int c, int owner0, int owner1) {
+  if (threadIdx.x == 0) {
+    xch::init(&sm.xbar[0], 1 + NT / 32);
+    xch::init(&sm.xbar[1], 1 + NT / 32);
+    xch::fence_init();
+    xch::arm(&sm.xbar[0], xch_bytes<T>(cs, owner0 != c));
+    xch::arm(&sm.xbar[1], xch_bytes<T>(cs, owner1 != c));
+  }
+  cluster.sync();
+}
 
 // A 24-value row to / from 16-byte aligned shared memory (vector accesses
 // for float).
@@ -311,16 +418,28 @@ __device__ __forceinline__ void row_get(const T *src, T (&v)[kW]) {
 // ordinary loop over static register indices -- one copy of the step in the
 // instruction stream instead of 24 -- and the arithmetic is exactly that of
 // the unrolled form (the same FMAs on the same operands).
+// step: this kernel's running column count (the exchange barriers' phase),
+// nsteps: its total columns (no barrier is armed past the last).
 template <typename T, int R, int NT>
 __device__ __forceinline__ void reg_panel_columns(
     T (&a)[R][kW], const int (&prow)[R], RegPanelSmem<T, NT> &sm,
     cg::cluster_group &cluster, int c, int CS, int rbase, int rpc, int64_t k0,
-    int32_t *__restrict__ ipiv, int32_t *spiv, T eps) {
+    int32_t *__restrict__ ipiv, int32_t *spiv, T eps, int &step, int nsteps) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = NT / 32;
+  (void)cluster;
 #pragma unroll 1
-  for (int kk = 0; kk < kW; kk++) {
-    const int buf = kk & 1;
+  for (int kk = 0; kk < kW; kk++, step++) {
+    const int buf = step & 1;
+    // arm the other barrier for the next column before this CTA sends this
+    // column's data (no CTA can send column step+1 before receiving ours);
+    // its previous phase (column step-1) completed at the last wait.  The
+    // next column's row kk lives in CTA (kk+1)/rpc, or in CTA 0 when it
+    // opens the next panel.
+    if (tid == 0 && step >= 1 && step + 1 < nsteps) {
+      const int nown = kk + 1 < kW ? (kk + 1) / rpc : 0;
+      xch::arm(&sm.xbar[buf ^ 1], xch_bytes<T>(CS, nown != c));
+    }
     T bk = (T)-2;
     int bi = INT_MAX;
 #pragma unroll
@@ -353,24 +472,62 @@ __device__ __forceinline__ void reg_panel_columns(
     int ci, cw;
     pick_best<T>(sm.wkey, sm.widx, NW, ck, ci, cw);
     const bool own_k = (kk >= rbase && kk < rbase + rpc);
-    const int nval = CS * kW;
-    const int total = nval + CS + (own_k ? nval : 0);
-    for (int t = tid; t < total; t += NT) {
-      if (t < nval) {
-        const int q = t / kW, j = t % kW;
-        T *dst = cluster.map_shared_rank(&sm.xval[buf][c][0], q);
-        dst[j] = ci != INT_MAX ? sm.wrow[cw][j] : T(0);
-      } else if (t < nval + CS) {
-        const int q = t - nval;
-        *cluster.map_shared_rank(&sm.xkey[buf][c], q) = ck;
-        *cluster.map_shared_rank(&sm.xidx[buf][c], q) = ci;
+    // 16-byte pieces of a row; per receiver: the candidate row, its key and
+    // index, and row kk when this CTA owns it.  Other CTAs get st.async
+    // (completing bytes on their barrier), this CTA plain stores; every warp
+    // then arrives on the local barrier, so its completion also means every
+    // local sender has read its staging row
+    constexpr int NV = kW * (int)sizeof(T) / 16;
+    const int per = NV + 2 + (own_k ? NV : 0);
+    const uint32_t lbar = xch::saddr(&sm.xbar[buf]);
+    const T *srow = ci != INT_MAX ? &sm.wrow[cw][0] : nullptr;
+    for (int t = tid; t < CS * per; t += NT) {
+      const int q = t / per, e = t % per;
+      if (q == c) {
+        if (e < NV) {
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (srow) v = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(srow) + 16 * e);
+          *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.xval[buf][c][0]) + 16 * e) = v;
+        } else if (e == NV) {
+          sm.xkey[buf][c] = ck;
+        } else if (e == NV + 1) {
+          sm.xidx[buf][c] = ci;
+        } else {
+          const int o = 16 * (e - NV - 2);
+          *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.kval[buf][0]) + o) =
+              *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(&sm.krow[0]) + o);
+        }
+        continue;
+      }
+      const uint32_t rbar = xch::mapa(lbar, q);
+      if (rbar & 7u) {  // never expected: a misaligned barrier is flagged, not used
+        g_lu_wait_err = 2;
+        continue;
+      }
+      if (e < NV) {
+        const uint32_t dst = xch::mapa(xch::saddr(&sm.xval[buf][c][0]), q) + 16 * e;
+        if (srow) {
+          xch::put16(dst, reinterpret_cast<const char *>(srow) + 16 * e, rbar);
+        } else {
+          const uint4 z = make_uint4(0, 0, 0, 0);
+          xch::put16(dst, &z, rbar);
+        }
+      } else if (e == NV) {
+        const uint32_t dst = xch::mapa(xch::saddr(&sm.xkey[buf][c]), q);
+        if constexpr (sizeof(T) == 4)
+          xch::put4(dst, __float_as_uint((float)ck), rbar);
+        else
+          xch::put8(dst, (uint64_t)__double_as_longlong((double)ck), rbar);
+      } else if (e == NV + 1) {
+        xch::put4(xch::mapa(xch::saddr(&sm.xidx[buf][c]), q), (uint32_t)ci, rbar);
       } else {
-        const int u = t - nval - CS;
-        const int q = u / kW, j = u % kW;
-        *cluster.map_shared_rank(&sm.kval[buf][j], q) = sm.krow[j];
+        const uint32_t dst = xch::mapa(xch::saddr(&sm.kval[buf][0]), q) + 16 * (e - NV - 2);
+        xch::put16(dst, reinterpret_cast<const char *>(&sm.krow[0]) + 16 * (e - NV - 2), rbar);
       }
     }
-    cluster.sync();
+    __syncwarp();
+    if (lane == 0) xch::arrive(&sm.xbar[buf]);
+    if (!xch::wait(&sm.xbar[buf], (uint32_t)(step >> 1) & 1u)) g_lu_wait_err = 1;
     T gk;
     int p, wc;
     pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
@@ -429,8 +586,10 @@ __global__ void __launch_bounds__(NT, 1)
     for (int j = 0; j < kW; j++)
       a[r][j] = prow[r] >= 0 ? A[(k0 + prow[r]) + (k0 + j) * lda] : T(0);
   }
+  xch_setup<T, NT>(sm, cluster, CS, c, 0, 1 / rpc);
+  int step = 0;
   reg_panel_columns<T, R, NT>(a, prow, sm, cluster, c, CS, rbase, rpc, k0,
-                              ipiv, nullptr, eps);
+                              ipiv, nullptr, eps, step, kW);
 #pragma unroll
   for (int r = 0; r < R; r++)
     if (prow[r] >= 0)
@@ -666,6 +825,11 @@ __global__ void __launch_bounds__(NT, 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NWARP = NT / 32;
   const int np = bw / kW;
+  {
+    const int rpc0 = (int)((n - kb) + CS - 1) / CS;  // the first panel's rows per CTA
+    xch_setup<T, NT>(sm.ps, cluster, CS, c, 0, 1 / rpc0);
+  }
+  int step = 0;
   for (int pn = 0; pn < np; pn++) {
     const int64_t k0 = kb + (int64_t)pn * kW;
     const int m = (int)(n - k0);
@@ -682,7 +846,7 @@ __global__ void __launch_bounds__(NT, 1)
         a[r][j] = prow[r] >= 0 ? __ldcg(&A[(k0 + prow[r]) + (k0 + j) * lda]) : T(0);
     }
     reg_panel_columns<T, R, NT>(a, prow, sm.ps, cluster, c, CS, rbase, rpc, k0,
-                                ipiv, sm.spiv, eps);
+                                ipiv, sm.spiv, eps, step, np * kW);
 #pragma unroll
     for (int r = 0; r < R; r++)
       if (prow[r] >= 0)
@@ -950,9 +1114,9 @@ static int launch_reg_panel(T *A, int64_t lda, int64_t n, int64_t k0, int cs,
   }
   const double m = (double)(n - k0);
   KtScope kt("lu_panel", m * kW * kW, 2.0 * m * kW * sizeof(T));
-  if (cs == 1) {
-    kern<<<1, NT, 0, ctx()->stream>>>(A, lda, n, k0, rpc, ipiv, eps);
-  } else {
+  // always a cluster launch (of one CTA too): the column exchange uses
+  // cluster shared-memory addressing
+  {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cs);
     cfg.blockDim = dim3(NT);
@@ -1296,6 +1460,18 @@ int precond_solve(bool spd, int64_t n, const float *W, const int32_t *perm,
 MGB_LU_INST(float)
 MGB_LU_INST(double)
 #undef MGB_LU_INST
+
+// Whether a panel exchange gave up waiting since the last clear (call after
+// the stream has been synchronised).
+int lu_wait_error(int clear) {
+  int h = 0;
+  MGB_CUDA(cudaMemcpyFromSymbol(&h, g_lu_wait_err, sizeof(int)));
+  if (clear && h) {
+    const int z = 0;
+    MGB_CUDA(cudaMemcpyToSymbol(g_lu_wait_err, &z, sizeof(int)));
+  }
+  return h;
+}
 
 int laswp(elem_t *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2,
           int64_t c3, const int32_t *ipiv, int64_t k1, int64_t k2) {
