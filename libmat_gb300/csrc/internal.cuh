@@ -50,7 +50,8 @@ struct KtScope {
 // counterpart of the reference's scratch arena, mat.h:865-895).
 enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
-  WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_NSLOTS
+  WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_SWM, WS_SWG,
+  WS_NSLOTS
 };
 void *ws(int slot, size_t bytes);
 
@@ -101,9 +102,12 @@ template <typename T>
 int trsm_left_t(bool lower, bool trans, bool unit, int64_t n, int64_t nrhs,
                 const T *Tm, int64_t ldt, T *B, int64_t ldb,
                 const int32_t *info);
+struct SwapMap;
+// keep (may be null): also leave the block's net swap map there
 template <typename T>
 int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
-            const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm);
+            const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm,
+            SwapMap *keep = nullptr);
 template <typename T>
 int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
                T eps, int *w_used);

@@ -751,17 +751,19 @@ static int g_swap_next = 0;
 
 template <typename T>
 int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
-            const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm) {
+            const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm,
+            SwapMap *keep) {
   const int64_t ncol = (c1 - c0) + (c3 - c2);
-  if (k2 <= k1 || (ncol <= 0 && !perm)) return 0;
+  if (k2 <= k1 || (ncol <= 0 && !perm && !keep)) return 0;
   if (k2 - k1 > kSwapMax) return set_error(MATGB_ERR_ARG, "laswp: block > %d", kSwapMax);
   if (!g_swap_ring) MGB_CUDA(cudaMalloc(&g_swap_ring, kSwapRing * sizeof(SwapMap)));
-  SwapMap *map = g_swap_ring + g_swap_next;
-  g_swap_next = (g_swap_next + 1) % kSwapRing;
+  // keep: the block's net map is also wanted later (deferred swaps)
+  SwapMap *map = keep ? keep : g_swap_ring + g_swap_next;
+  if (!keep) g_swap_next = (g_swap_next + 1) % kSwapRing;
   int64_t blocks = (ncol + kSwapCols - 1) / kSwapCols;
   if (blocks < 1) blocks = 1;
   KtScope kt("laswp", 0.0, 4.0 * (k2 - k1) * ncol * sizeof(T));
-  if (blocks <= 8) {
+  if (blocks <= 8 && !keep) {
     laswp_kernel<T, true><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
         A, lda, c0, c1, c2, c3, nullptr, ipiv, k1, k2, perm);
   } else {
@@ -771,6 +773,87 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
         A, lda, c0, c1, c2, c3, map, ipiv, k1, k2, perm);
   }
   MGB_LAUNCHED("laswp");
+  return 0;
+}
+
+// ---- deferred row swaps on the factored columns --------------------------
+// A right-looking factorisation never reads the columns of a finished block
+// again, so the swaps of later blocks' pivots can reach those columns at the
+// end, in one pass, instead of block by block: for column block b, rows
+// [ke_b, n) are gathered through G_b = s_{b+1} o s_{b+2} o ... (s_k: block
+// k's net swap map as a gather, row pos[t] <- row src[t]).  The same moves as
+// swapping block by block, so L is identical; the pass reads and writes each
+// column once, coalesced, instead of touching scattered rows per block.
+// G_b for every block, built backwards in one CTA with a dense map in shared
+// memory (n entries).
+__global__ void __launch_bounds__(1024)
+    swap_compose_kernel(const SwapMap *__restrict__ maps, int nblk, int64_t n,
+                        int64_t nb, int32_t *__restrict__ G) {
+  extern __shared__ int32_t dmap[];
+  const int tid = threadIdx.x;
+  for (int64_t i = tid; i < n; i += 1024) dmap[i] = (int32_t)i;
+  __syncthreads();
+  for (int b = nblk - 2; b >= 0; b--) {
+    const SwapMap &m = maps[b + 1];
+    const int cnt = m.cnt;
+    for (int t = tid; t < cnt; t += 1024) dmap[m.pos[t]] = m.src[t];
+    __syncthreads();
+    const int64_t r0 = (int64_t)(b + 1) * nb;      // rows below block b
+    const int64_t r1 = (int64_t)(b + 2) * nb;      // rows below block b + 1
+    for (int64_t i = r0 + tid; i < n; i += 1024) {
+      const int32_t g1 = (i < r1 || b + 1 == nblk - 1) ? (int32_t)i : G[(int64_t)(b + 1) * n + i];
+      G[(int64_t)b * n + i] = dmap[g1];
+    }
+    __syncthreads();
+    for (int t = tid; t < cnt; t += 1024) dmap[m.pos[t]] = m.pos[t];
+    __syncthreads();
+  }
+}
+
+// One CTA per column of the first nblk-1 blocks: the column's rows below its
+// block into shared memory (coalesced), then written back through G_b.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    left_gather_kernel(T *__restrict__ A, int64_t lda, int64_t n, int64_t nb,
+                       const int32_t *__restrict__ G) {
+  extern __shared__ __align__(16) unsigned char lg_raw[];
+  T *col = reinterpret_cast<T *>(lg_raw);
+  const int64_t j = blockIdx.x;
+  const int64_t b = j / nb;
+  const int64_t r0 = (b + 1) * nb;
+  T *cp = A + j * lda;
+  for (int64_t i = r0 + threadIdx.x; i < n; i += 256) col[i - r0] = cp[i];
+  __syncthreads();
+  const int32_t *g = G + b * n;
+  for (int64_t i = r0 + threadIdx.x; i < n; i += 256) {
+    const int64_t s = g[i];
+    if (s >= r0 && s < n) cp[i] = col[s - r0];  // always true: later swaps stay below the block
+  }
+}
+
+template <typename T>
+static int apply_deferred_swaps(T *A, int64_t lda, int64_t n, int64_t nb, int nblk,
+                                const SwapMap *maps, int32_t *G) {
+  cudaStream_t st = ctx()->stream;
+  const size_t dsm = (size_t)n * sizeof(int32_t);
+  static bool attr = false;
+  if (!attr) {
+    MGB_CUDA(cudaFuncSetAttribute(swap_compose_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
+    MGB_CUDA(cudaFuncSetAttribute(left_gather_kernel<T>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
+    attr = true;
+  }
+  {
+    KtScope kt("swap_compose", 0.0, 8.0 * n * nblk);
+    swap_compose_kernel<<<1, 1024, dsm, st>>>(maps, nblk, n, nb, G);
+    MGB_LAUNCHED("swap_compose");
+  }
+  const int64_t ncols = (int64_t)(nblk - 1) * nb;
+  KtScope kt("left_gather", 0.0, 2.0 * sizeof(T) * (double)ncols * (n - nb) / 2.0);
+  left_gather_kernel<T><<<(unsigned)ncols, 256, (size_t)(n - nb) * sizeof(T), st>>>(
+      A, lda, n, nb, G);
+  MGB_LAUNCHED("left_gather");
   return 0;
 }
 
@@ -1377,6 +1460,21 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
   // launch each where they fit
   const bool fused = sizeof(T) == 4;
   const int64_t NB = fused ? kFusedMaxBw : lp >= 0 ? kOuterBlockLp : kOuterBlock;
+  // the swaps on the columns left of each block are deferred to one pass at
+  // the end when a column below the first block fits in shared memory
+  const int nblk = (int)((n + NB - 1) / NB);
+  SwapMap *maps = nullptr;
+  int32_t *gmap = nullptr;
+  if (nblk >= 2 && (n - NB) * (int64_t)sizeof(T) <= 200 * 1024 && n * 4 <= 200 * 1024) {
+    maps = (SwapMap *)ws(WS_SWM, (size_t)nblk * sizeof(SwapMap));
+    gmap = (int32_t *)ws(WS_SWG, (size_t)nblk * n * sizeof(int32_t));
+    if (!maps || !gmap) {
+      maps = nullptr;
+      gmap = nullptr;
+      matgb_clear_error();
+    }
+  }
+  const bool defer = maps != nullptr;
   for (int64_t kb = 0; kb < n; kb += NB) {
     const int64_t nb = (n - kb) < NB ? (n - kb) : NB;
     const int64_t ke = kb + nb;
@@ -1389,6 +1487,7 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     }
     MGB_CUDA(cudaEventRecord(g_la.ev[1], hi));
     MGB_CUDA(cudaStreamWaitEvent(main, g_la.ev[1], 0));
+
     const int64_t nn = (n - ke) < NB ? (n - ke) : NB;
     if (ke < n) {
       // look-ahead: the next block's columns are swapped, solved and updated
@@ -1402,13 +1501,18 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       MGB_CUDA(cudaEventRecord(g_la.ev[2], main));
       MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[2], 0));
     }
-    MGB_TRY(laswp_t<T>(A, lda, 0, kb, ke + nn, n, ipiv, kb, ke, perm));
+    // the columns right of the look-ahead (and, unless deferred, the columns
+    // left of the block) and the permutation; a deferred pass keeps this
+    // block's net map
+    MGB_TRY(laswp_t<T>(A, lda, 0, defer ? 0 : kb, ke + nn, n, ipiv, kb, ke, perm,
+                       defer && kb > 0 ? &maps[kb / NB] : nullptr));
     if (ke + nn < n) {
       MGB_TRY(trsm_unit_lower<T>((int)nb, n - ke - nn, A + kb + kb * lda, lda,
                                  A + kb + (ke + nn) * lda, lda));
       MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, n, lp, false));
     }
   }
+  if (defer) MGB_TRY(apply_deferred_swaps<T>(A, lda, n, NB, nblk, maps, gmap));
   return 0;
 }
 
@@ -1451,7 +1555,8 @@ int precond_solve(bool spd, int64_t n, const float *W, const int32_t *perm,
 
 #define MGB_LU_INST(T)                                                         \
   template int laswp_t<T>(T *, int64_t, int64_t, int64_t, int64_t, int64_t,    \
-                          const int32_t *, int64_t, int64_t, int32_t *);       \
+                          const int32_t *, int64_t, int64_t, int32_t *,        \
+                          SwapMap *);                                          \
   template int lu_panel_t<T>(T *, int64_t, int64_t, int64_t, int, int32_t *,  \
                              T, int *);                                        \
   template int getrf_t<T>(int64_t, T *, int64_t, int32_t *, int32_t *, T, int); \
