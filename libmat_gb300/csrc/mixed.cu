@@ -85,25 +85,34 @@ __global__ void pack_l21_kernel(const float *__restrict__ A, int64_t lda,
   }
 }
 
-// FP16 scale of U12: s = 2^(14 - ceil(log2 max|U12|)), so the largest entry
-// maps to at most 2^14; scale[0] = s, scale[1] = 1/s (both exact).
-__global__ void u12_amax_kernel(const float *__restrict__ A, int64_t lda,
-                                int nb, int64_t ncols,
-                                unsigned *__restrict__ amax_bits) {
+// max |A(0:rows, 0:cols)| (column-major, leading dimension lda) into
+// *amax_bits (atomicMax on the bit pattern: non-negative floats order like
+// their bits).  A warp takes a (column, 1024-row chunk) task at a time, lanes
+// down the column; NaN is ignored here and propagates through the GEMM.
+__global__ void amax_kernel(const float *__restrict__ A, int64_t lda, int rows,
+                            int64_t cols, unsigned *__restrict__ amax_bits) {
+  const int lane = threadIdx.x & 31;
+  const int nchunk = (rows + 1023) >> 10;
+  const int64_t ntask = cols * nchunk;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   float m = 0.f;
-  const int64_t tot = (int64_t)nb * ncols;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const float v = fabsf(A[(e % nb) + (e / nb) * lda]);
-    if (v > m) m = v;  // NaN is ignored here; it propagates through the GEMM
+  for (int64_t t = w0; t < ntask; t += nw) {
+    const int64_t j = t / nchunk;
+    const int r0 = (int)(t - j * nchunk) << 10;
+    const int r1 = r0 + 1024 < rows ? r0 + 1024 : rows;
+    const float *c = A + j * lda;
+    for (int k = r0 + lane; k < r1; k += 32) m = fmaxf(m, fabsf(c[k]));
   }
   for (int off = 16; off; off >>= 1) m = fmaxf(m, __shfl_xor_sync(~0u, m, off));
-  if ((threadIdx.x & 31) == 0) atomicMax(amax_bits, __float_as_uint(m));
+  if (lane == 0) atomicMax(amax_bits, __float_as_uint(m));
 }
 
-// out[j*Kp + k] = s * A[k + j*lda] (k < nb), 0 for nb <= k < Kp.
+// out[j*Kp + k] = s * A[k + j*lda] (k < nb), 0 for nb <= k < Kp, with
+// s = fp16_scale(*amax_bits) (FP16) or 1 (BF16, or no amax).
 // scale[1] = 1/s, or 1/(s * sL) when the L21 operand was scaled by
-// sL = fp16_scale(*amax_l); out_lo (optional) gets the remainders.
+// sL = fp16_scale(*amax_l); out_lo (optional) gets the remainders.  A warp per
+// column, two values per lane in one 32-bit store.
 template <int BF16>
 __global__ void pack_u12_kernel(const float *__restrict__ A, int64_t lda,
                                 int nb, int Kp, int64_t ncols,
@@ -118,15 +127,24 @@ __global__ void pack_u12_kernel(const float *__restrict__ A, int64_t lda,
     scale[0] = s;
     scale[1] = 1.f / (s * sl);  // powers of two: exact
   }
-  const int64_t tot = (int64_t)Kp * ncols;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e % Kp);
-    const int64_t j = e / Kp;
-    const float v = k < nb ? s * A[k + j * lda] : 0.f;
-    const uint16_t h = to16<BF16>(v);
-    out[e] = h;
-    if (out_lo) out_lo[e] = to16<BF16>(v - from16<BF16>(h));
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = w0; j < ncols; j += nw) {
+    const float *c = A + j * lda;
+    uint32_t *o = reinterpret_cast<uint32_t *>(out + j * Kp);
+    uint32_t *ol = out_lo ? reinterpret_cast<uint32_t *>(out_lo + j * Kp) : nullptr;
+    for (int k = 2 * lane; k < Kp; k += 64) {
+      const float v0 = k < nb ? s * c[k] : 0.f;
+      const float v1 = k + 1 < nb ? s * c[k + 1] : 0.f;
+      const uint16_t h0 = to16<BF16>(v0), h1 = to16<BF16>(v1);
+      o[k >> 1] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+      if (ol) {
+        const uint16_t l0 = to16<BF16>(v0 - from16<BF16>(h0));
+        const uint16_t l1 = to16<BF16>(v1 - from16<BF16>(h1));
+        ol[k >> 1] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+      }
+    }
   }
 }
 
@@ -169,15 +187,14 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
     const float *U12 = A + kb + c0 * lda;
     if (lp != 1) {
       MGB_CUDA(cudaMemsetAsync(amax_u, 0, sizeof(unsigned), st));
-      u12_amax_kernel<<<grid_cap((int64_t)nb * nc), 256, 0, st>>>(U12, lda, nb,
-                                                                  nc, amax_u);
+      amax_kernel<<<grid_cap(32 * nc), 256, 0, st>>>(U12, lda, nb, nc, amax_u);
       MGB_LAUNCHED("u12_amax");
     }
     if (first) {
       dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
       if (split) {
         MGB_CUDA(cudaMemsetAsync(amax_l, 0, sizeof(unsigned), st));
-        u12_amax_kernel<<<grid_cap((int64_t)nb * m), 256, 0, st>>>(
+        amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
             L21, lda, (int)m, nb, amax_l);
         MGB_LAUNCHED("l21_amax");
         pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax_l,
@@ -192,10 +209,10 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
       MGB_LAUNCHED("pack_l21");
     }
     if (lp == 1)
-      pack_u12_kernel<1><<<grid_cap((int64_t)Kp * nc), 256, 0, st>>>(
+      pack_u12_kernel<1><<<grid_cap(32 * nc), 256, 0, st>>>(
           U12, lda, nb, Kp, nc, nullptr, sc, B16 + off);
     else
-      pack_u12_kernel<0><<<grid_cap((int64_t)Kp * nc), 256, 0, st>>>(
+      pack_u12_kernel<0><<<grid_cap(32 * nc), 256, 0, st>>>(
           U12, lda, nb, Kp, nc, amax_u, sc, B16 + off,
           split ? B16lo + off : nullptr, split ? amax_l : nullptr);
     MGB_LAUNCHED("pack_u12");
@@ -225,8 +242,8 @@ int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
     pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
   } else {
     MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
-    u12_amax_kernel<<<grid_cap((int64_t)nb * m), 256, 0, st>>>(L21, lda, (int)m,
-                                                                nb, amax);
+    amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
+        L21, lda, (int)m, nb, amax);
     MGB_LAUNCHED("l21_amax");
     pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc,
                                           A16lo);
