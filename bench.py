@@ -397,6 +397,7 @@ def e2e_mixed(L, mg, A, b, flops, opts, ke):
     # each call timed on its own (host clock: it includes the copies and the
     # synchronisation); the median is reported, every sample beside it
     samples = []
+    detail = []
     ok = 1
     for _ in range(ke):
         t0 = time.perf_counter()
@@ -404,12 +405,15 @@ def e2e_mixed(L, mg, A, b, flops, opts, ke):
                                  C.byref(opts), C.byref(rep)), "mat_solve_ir")
         samples.append((time.perf_counter() - t0) * 1e3)
         ok = ok and rep.converged
+        detail.append({"ms_factor": round(rep.ms_factor, 2), "ms_refine": round(rep.ms_refine, 2),
+                       "krylov_steps": rep.krylov_steps, "lp_format": rep.lp_format})
     ms = float(np.median(samples))
     for p in (hA, hb, hx):
         L.c.matgb_host_free(p)
     return {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
             "h2d_bytes_per_step": n * n * es + n * es, "d2h_bytes_per_step": n * es,
             "ms_per_step": ms, "ms_samples": [round(v, 2) for v in samples],
+            "samples_detail": detail,
             "converged": int(ok),
             "api": "mat_solve_ir (host Mat/Vec, pinned), kappa = 1e4"}
 

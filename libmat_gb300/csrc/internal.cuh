@@ -119,8 +119,13 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
 // Tensor-core trailing update of columns [c0,c1) after outer block [kb,ke)
 // (mixed.cu): packs U12[:, c0:c1] to 16 bits, and L21 too on the block's
 // first call (first = true).
+// amax3 (may be null): the block's max slots [|L21|, |U12| look-ahead, |U12|
+// rest], zeroed once per factorisation; l21_ready / u12_ready: already filled
+// by the factorisation kernels.
 int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
-                       int64_t ke, int64_t c0, int64_t c1, int lp, bool first);
+                       int64_t ke, int64_t c0, int64_t c1, int lp, bool first,
+                       unsigned *amax3 = nullptr, bool l21_ready = false,
+                       bool u12_ready = false);
 template <typename T>
 int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
             const int32_t *perm, const T *B, int64_t ldb, T *X, int64_t ldx);

@@ -900,7 +900,8 @@ struct FusedSmem {
 template <typename T, int R, int NT>
 __global__ void __launch_bounds__(NT, 1)
     lu_block_fused_kernel(T *__restrict__ A, int64_t lda, int64_t n,
-                          int64_t kb, int bw, int32_t *__restrict__ ipiv, T eps) {
+                          int64_t kb, int bw, int32_t *__restrict__ ipiv, T eps,
+                          unsigned *__restrict__ amax_l) {
   __shared__ FusedSmem<T, NT> sm;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
@@ -935,6 +936,20 @@ __global__ void __launch_bounds__(NT, 1)
       if (prow[r] >= 0)
 #pragma unroll
         for (int j = 0; j < kW; j++) A[(k0 + prow[r]) + (k0 + j) * lda] = a[r][j];
+    if (amax_l) {
+      // an upper bound of max |L21| (the tensor-core operand's FP16 scale):
+      // the panel's multipliers of every row below its diagonal block -- the
+      // later panels' swaps only permute those rows, so L21 (the rows below
+      // the block at the end) is a subset; NaN ignored as in amax_kernel
+      float mx = 0.f;
+#pragma unroll
+      for (int r = 0; r < R; r++)
+        if (prow[r] >= kW)
+#pragma unroll
+          for (int j = 0; j < kW; j++) mx = fmaxf(mx, fabsf((float)a[r][j]));
+      for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      if (lane == 0 && mx > 0.f) atomicMax(amax_l, __float_as_uint(mx));
+    }
     // the panel's swaps on the block's other columns: [kb, k0) and
     // [k0+24, kb+bw); CTA c takes every CS-th of them, one warp per column
     __syncthreads();
@@ -1028,7 +1043,8 @@ __global__ void __launch_bounds__(NT, 1)
 template <typename T, int TB>
 __global__ void __launch_bounds__(256)
     trsm_unit_warp_kernel(const T *__restrict__ L, int64_t ldl,
-                          T *__restrict__ B, int64_t ldb, int64_t ncols) {
+                          T *__restrict__ B, int64_t ldb, int64_t ncols,
+                          unsigned *__restrict__ amax) {
   constexpr int RPL = (TB + 31) / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Ls = (T *)smem_raw;  // Ls[k*(TB+1) + i] = L(i, k)
@@ -1061,11 +1077,23 @@ __global__ void __launch_bounds__(256)
     const int i = lane + 32 * r;
     if (i > 0 && i < TB) b[i] = x[r];
   }
+  if constexpr (sizeof(T) == 4) {
+    // max |U12| of the column (the FP16 scale of the tensor-core operand),
+    // NaN ignored as in amax_kernel
+    if (amax) {
+      float m = 0.f;
+#pragma unroll
+      for (int r = 0; r < RPL; r++)
+        if (lane + 32 * r < TB) m = fmaxf(m, fabsf((float)x[r]));
+      for (int off = 16; off; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+      if (lane == 0) atomicMax(amax, __float_as_uint(m));
+    }
+  }
 }
 
 template <typename T, int TB>
 static int launch_trsm_warp(int64_t ncols, const T *L, int64_t ldl, T *B,
-                            int64_t ldb) {
+                            int64_t ldb, unsigned *amax) {
   auto k = trsm_unit_warp_kernel<T, TB>;
   const size_t smem = (size_t)TB * (TB + 1) * sizeof(T);
   static bool attr = false;
@@ -1075,19 +1103,27 @@ static int launch_trsm_warp(int64_t ncols, const T *L, int64_t ldl, T *B,
     attr = true;
   }
   KtScope kt("trsm_lu", (double)TB * TB * ncols, (double)sizeof(T) * 2.0 * TB * ncols);
-  k<<<(unsigned)((ncols + 7) / 8), 256, smem, ctx()->stream>>>(L, ldl, B, ldb, ncols);
+  k<<<(unsigned)((ncols + 7) / 8), 256, smem, ctx()->stream>>>(L, ldl, B, ldb, ncols,
+                                                                amax);
   MGB_LAUNCHED("trsm_lu");
   return 0;
 }
 
+// amax (may be null, float only): also atomicMax of max |U12| into it; the
+// fallback path (other block widths) leaves it alone and returns false in
+// *amax_done.
 template <typename T>
 static int trsm_unit_lower(int tb, int64_t ncols, const T *L, int64_t ldl, T *B,
-                           int64_t ldb) {
+                           int64_t ldb, unsigned *amax = nullptr,
+                           bool *amax_done = nullptr) {
+  if (amax_done) *amax_done = amax != nullptr;
   if (ncols <= 0 || tb <= 1) return 0;
-  if (tb == kRefBlock) return launch_trsm_warp<T, kRefBlock>(ncols, L, ldl, B, ldb);
-  if (tb == kOuterBlock) return launch_trsm_warp<T, kOuterBlock>(ncols, L, ldl, B, ldb);
-  if (tb == kOuterBlockLp) return launch_trsm_warp<T, kOuterBlockLp>(ncols, L, ldl, B, ldb);
-  if (tb == kFusedMaxBw) return launch_trsm_warp<T, kFusedMaxBw>(ncols, L, ldl, B, ldb);
+  if (tb == kRefBlock) return launch_trsm_warp<T, kRefBlock>(ncols, L, ldl, B, ldb, amax);
+  if (tb == kOuterBlock) return launch_trsm_warp<T, kOuterBlock>(ncols, L, ldl, B, ldb, amax);
+  if (tb == kOuterBlockLp)
+    return launch_trsm_warp<T, kOuterBlockLp>(ncols, L, ldl, B, ldb, amax);
+  if (tb == kFusedMaxBw) return launch_trsm_warp<T, kFusedMaxBw>(ncols, L, ldl, B, ldb, amax);
+  if (amax_done) *amax_done = false;
   return trsm_left_t<T>(true, false, true, tb, ncols, L, ldl, B, ldb, nullptr);
 }
 
@@ -1322,7 +1358,7 @@ int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
 // (float; rows n-kb <= 16 CTAs x 1024); *done = false otherwise.
 template <typename T>
 static int try_fused_block(T *A, int64_t lda, int64_t n, int64_t kb, int bw,
-                           int32_t *ipiv, T eps, bool *done) {
+                           int32_t *ipiv, T eps, bool *done, unsigned *amax_l) {
   *done = false;
   if constexpr (sizeof(T) != 4) {
     return 0;
@@ -1355,11 +1391,11 @@ static int try_fused_block(T *A, int64_t lda, int64_t n, int64_t kb, int bw,
     if (R == 1) {
       auto kern = lu_block_fused_kernel<T, 1, 512>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps, amax_l);
     } else {
       auto kern = lu_block_fused_kernel<T, 2, 512>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps, amax_l);
     }
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -1429,14 +1465,16 @@ struct StreamSwap {
 template <typename T>
 static int trailing_update(int64_t n, T *A, int64_t lda, int64_t kb,
                            int64_t ke, int64_t c0, int64_t c1, int lp,
-                           bool first) {
+                           bool first, unsigned *amax3 = nullptr,
+                           bool l21_ready = false, bool u12_ready = false) {
   if (c1 <= c0 || ke >= n) return 0;
   if (lp < 0)
     return gemm_skip_t<T>(false, false, n - ke, c1 - c0, ke - kb, T(-1),
                           A + ke + kb * lda, lda, A + kb + c0 * lda, lda, T(1),
                           A + ke + c0 * lda, lda, 0, nullptr);
   if (sizeof(T) != 4) return set_error(MATGB_ERR_ARG, "tensor-core LU is float");
-  return lp_trailing_update(n, (float *)A, lda, kb, ke, c0, c1, lp, first);
+  return lp_trailing_update(n, (float *)A, lda, kb, ke, c0, c1, lp, first, amax3,
+                            l21_ready, u12_ready);
 }
 
 template <typename T>
@@ -1453,9 +1491,6 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
                   256, 0, main>>>(perm, n);
     MGB_LAUNCHED("iota");
   }
-  // main -> hi: everything queued so far (input copies, perm init)
-  MGB_CUDA(cudaEventRecord(g_la.ev[0], main));
-  MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[0], 0));
   // float (plain and mixed): 144-column blocks factored by one fused cluster
   // launch each where they fit
   const bool fused = sizeof(T) == 4;
@@ -1475,14 +1510,31 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     }
   }
   const bool defer = maps != nullptr;
+  // tensor-core path: per-block max slots (|L21|, |U12| look-ahead, |U12|
+  // rest) after the 64 scale floats of the packing scratch, zeroed once here
+  // and filled by the factorisation kernels themselves where they can
+  unsigned *amax_all = nullptr;
+  if (lp == 0 || lp == 2) {
+    float *scb = (float *)ws(WS_T2, 256 + (size_t)12 * (nblk + 1));
+    if (!scb) return MATGB_ERR_NOMEM;
+    amax_all = reinterpret_cast<unsigned *>(scb + 64);
+    MGB_CUDA(cudaMemsetAsync(amax_all, 0, (size_t)12 * (nblk + 1), main));
+  }
+  // main -> hi: everything queued so far (input copies, perm init, slots)
+  MGB_CUDA(cudaEventRecord(g_la.ev[0], main));
+  MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[0], 0));
   for (int64_t kb = 0; kb < n; kb += NB) {
     const int64_t nb = (n - kb) < NB ? (n - kb) : NB;
     const int64_t ke = kb + nb;
+    unsigned *amax3 = amax_all ? amax_all + 3 * (kb / NB) : nullptr;
+    bool l21_ready = false;
     {
       StreamSwap sw(hi);
       bool done = false;
       if (fused && nb == NB)
-        MGB_TRY(try_fused_block<T>(A, lda, n, kb, (int)nb, ipiv, eps, &done));
+        MGB_TRY(try_fused_block<T>(A, lda, n, kb, (int)nb, ipiv, eps, &done,
+                                   lp == 2 ? amax3 : nullptr));
+      l21_ready = done && lp == 2;
       if (!done) MGB_TRY(factor_block<T>(n, A, lda, kb, ke, ipiv, eps));
     }
     MGB_CUDA(cudaEventRecord(g_la.ev[1], hi));
@@ -1495,9 +1547,12 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       // columns, the columns left of the block, the permutation) follows
       // off the critical path
       MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
+      bool u12_ready = false;
       MGB_TRY(trsm_unit_lower<T>((int)nb, nn, A + kb + kb * lda, lda,
-                                 A + kb + ke * lda, lda));
-      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true));
+                                 A + kb + ke * lda, lda, amax3 ? amax3 + 1 : nullptr,
+                                 &u12_ready));
+      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true, amax3,
+                                 l21_ready, u12_ready));
       MGB_CUDA(cudaEventRecord(g_la.ev[2], main));
       MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[2], 0));
     }
@@ -1507,9 +1562,12 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     MGB_TRY(laswp_t<T>(A, lda, 0, defer ? 0 : kb, ke + nn, n, ipiv, kb, ke, perm,
                        defer && kb > 0 ? &maps[kb / NB] : nullptr));
     if (ke + nn < n) {
+      bool u12_ready = false;
       MGB_TRY(trsm_unit_lower<T>((int)nb, n - ke - nn, A + kb + kb * lda, lda,
-                                 A + kb + (ke + nn) * lda, lda));
-      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, n, lp, false));
+                                 A + kb + (ke + nn) * lda, lda,
+                                 amax3 ? amax3 + 2 : nullptr, &u12_ready));
+      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, n, lp, false, amax3,
+                                 l21_ready, u12_ready));
     }
   }
   if (defer) MGB_TRY(apply_deferred_swaps<T>(A, lda, n, NB, nblk, maps, gmap));

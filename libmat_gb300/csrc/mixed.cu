@@ -160,8 +160,13 @@ static unsigned grid_cap(int64_t tot, int per = 256) {
 // scale found); every call packs the U12 columns [c0, c1) it updates, with a
 // scale of its own (kept in a slot per call, so the two calls of a block --
 // the look-ahead columns, then the rest -- never share one).
+// amax3 (may be null): the block's three max slots -- |L21|, |U12| of the
+// look-ahead columns, |U12| of the rest -- zeroed once per factorisation;
+// l21_ready / u12_ready: the factorisation kernels already filled them.
+// Without amax3 the maxima are found here in a zeroed scratch slot.
 int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
-                       int64_t ke, int64_t c0, int64_t c1, int lp, bool first) {
+                       int64_t ke, int64_t c0, int64_t c1, int lp, bool first,
+                       unsigned *amax3, bool l21_ready, bool u12_ready) {
   const int nb = (int)(ke - kb);
   const int Kp = (nb + 63) / 64 * 64;
   const int64_t m = n - ke, ncols = n - ke, nc = c1 - c0;
@@ -176,8 +181,9 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
   // slots: [0..3] scales of the first call, [8..11] of the second;
   // [16] amax of L21 (split), [17], [18] amax of each call's U12 columns
   float *sc = scb + (first ? 0 : 8);
-  unsigned *amax_l = (unsigned *)(scb + 16);
-  unsigned *amax_u = (unsigned *)(scb + (first ? 17 : 18));
+  unsigned *amax_l = amax3 ? amax3 : (unsigned *)(scb + 16);
+  unsigned *amax_u = amax3 ? amax3 + (first ? 1 : 2) : (unsigned *)(scb + (first ? 17 : 18));
+  if (!amax3) l21_ready = u12_ready = false;
   cudaStream_t st = ctx()->stream;
   const int64_t off = (c0 - ke) * Kp;
   {
@@ -185,18 +191,20 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
                (split ? 10.0 : 6.0) * ((first ? m : 0) + nc) * nb);
     const float *L21 = A + ke + kb * lda;
     const float *U12 = A + kb + c0 * lda;
-    if (lp != 1) {
-      MGB_CUDA(cudaMemsetAsync(amax_u, 0, sizeof(unsigned), st));
+    if (lp != 1 && !u12_ready) {
+      if (!amax3) MGB_CUDA(cudaMemsetAsync(amax_u, 0, sizeof(unsigned), st));
       amax_kernel<<<grid_cap(32 * nc), 256, 0, st>>>(U12, lda, nb, nc, amax_u);
       MGB_LAUNCHED("u12_amax");
     }
     if (first) {
       dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
       if (split) {
-        MGB_CUDA(cudaMemsetAsync(amax_l, 0, sizeof(unsigned), st));
-        amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
-            L21, lda, (int)m, nb, amax_l);
-        MGB_LAUNCHED("l21_amax");
+        if (!l21_ready) {
+          if (!amax3) MGB_CUDA(cudaMemsetAsync(amax_l, 0, sizeof(unsigned), st));
+          amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
+              L21, lda, (int)m, nb, amax_l);
+          MGB_LAUNCHED("l21_amax");
+        }
         pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax_l,
                                               nullptr, A16lo);
       } else if (lp == 1) {
