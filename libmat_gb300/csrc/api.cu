@@ -29,6 +29,8 @@ int sync() {
   MGB_CUDA(cudaStreamSynchronize(ctx()->stream));
   if (lu_wait_error(1))
     return set_error(MATGB_ERR_TIMEOUT, "LU panel exchange gave up waiting");
+  MGB_TRY(trsv_status());
+  MGB_TRY(trsm_flag_status());
   return 0;
 }
 

@@ -23,10 +23,13 @@ constexpr int kCholBlockLp = 128;
 
 template <typename T>
 static size_t diag_smem(int nb) { return (size_t)nb * (nb + 1) * sizeof(T); }
+static size_t rows_smem(int NB) { return ((size_t)NB * (NB + 4) + NB) * sizeof(float); }
 template <typename T>
 static size_t ctrsm_smem(int nb) {
   return ((size_t)nb * (nb + 1) + (size_t)nb * 33) * sizeof(T);
 }
+
+constexpr int kDiagMax = 128;  // largest diagonal block (kCholBlock, kCholBlockLp)
 
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -34,37 +37,94 @@ __global__ void __launch_bounds__(256)
                       int32_t *__restrict__ info, int64_t kb) {
   if (*info != 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *Ls = (T *)smem_raw;  // Ls[j*(nb+1)+i]
-  const int tid = threadIdx.x;
+  T *Ls = (T *)smem_raw;  // Ls[j*(nb+1)+i] = A(i, j), lower triangle only
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int ld = nb + 1;
-  for (int e = tid; e < nb * nb; e += 256) {
-    int i = e % nb, j = e / nb;
-    Ls[j * ld + i] = (i >= j) ? A[i + (int64_t)j * lda] : T(0);
-  }
+  for (int j = ty; j < nb; j += 16)
+    for (int i = j + tx; i < nb; i += 16) Ls[j * ld + i] = A[i + (int64_t)j * lda];
   __syncthreads();
+  // Column j: d = A(j,j), L(j,j) = sqrt(d), L(i,j) = A(i,j) * (1/L(j,j)) and
+  // the trailing lower triangle A(i,k) -= L(i,j) L(k,j).  Threads: 16 x 16
+  // over (row, column) of the trailing triangle, no divisions.
+  // the scaled column in its own array, so the update's reads never alias
+  // its writes and the loads pipeline
+  __shared__ T colj[kDiagMax];
   for (int j = 0; j < nb; j++) {
     const T d = Ls[j * ld + j];
-    if (d <= 0) {  // NaN passes, as in the reference's "diag <= 0" test
+    if (d <= T(0)) {  // NaN passes, as in the reference's "diag <= 0" test
       if (tid == 0) *info = (int32_t)(kb + j + 1);
       break;
     }
     const T ljj = sqrt(d);
     const T inv = T(1) / ljj;
-    __syncthreads();  // everyone has read d
-    if (tid == 0) Ls[j * ld + j] = ljj;
-    for (int i = j + 1 + tid; i < nb; i += 256) Ls[j * ld + i] *= inv;
+    for (int i = j + 1 + tid; i < nb; i += 256) {
+      const T l = Ls[j * ld + i] * inv;
+      colj[i] = l;
+      Ls[j * ld + i] = l;
+    }
     __syncthreads();
-    const int r = nb - j - 1;
-    for (int e = tid; e < r * r; e += 256) {
-      const int i = j + 1 + e % r, k = j + 1 + e / r;
-      if (k <= i) Ls[k * ld + i] = fma(-Ls[j * ld + i], Ls[j * ld + k], Ls[k * ld + i]);
+    if (tid == 0) Ls[j * ld + j] = ljj;
+    for (int k = j + 1 + ty; k < nb; k += 16) {
+      const T lkj = colj[k];
+      for (int i = k + tx; i < nb; i += 16) Ls[k * ld + i] = fma(-colj[i], lkj, Ls[k * ld + i]);
     }
     __syncthreads();
   }
   __syncthreads();
-  for (int e = tid; e < nb * nb; e += 256) {
-    int i = e % nb, j = e / nb;
-    if (i >= j) A[i + (int64_t)j * lda] = Ls[j * ld + i];
+  for (int j = ty; j < nb; j += 16)
+    for (int i = j + tx; i < nb; i += 16) A[i + (int64_t)j * lda] = Ls[j * ld + i];
+}
+
+// Float form, one thread per row of the diagonal block (NB threads): before
+// step j row i >= j holds A^(j)(i, j..i) in a[0..i-j] (shifted frame).  Step
+// j: every row publishes a[0] (column j; the pivot d at its head) into a
+// double-buffered shared column, one barrier, then L(j,j) = sqrt(d), row i
+// writes L(i,j) = a[0] * (1/L(j,j)) and updates A(i,k) -= L(i,j) L(k,j),
+// forming each L(k,j) from the published column the same way -- the
+// operands and FMAs of potrf_diag_kernel, with one barrier per column.
+template <int NB>
+__global__ void __launch_bounds__(NB)
+    potrf_diag_rows_kernel(int nb, float *__restrict__ A, int64_t lda,
+                           int32_t *__restrict__ info, int64_t kb) {
+  if (*info != 0) return;
+  __shared__ __align__(16) float colb[2][NB + 8];  // colb[.][3 + (i - j)] = A^(j)(i, j)
+  const int i = threadIdx.x;
+  const bool act = i < nb;
+  const int wlast = ((i | 31) < nb - 1 ? (i | 31) : nb - 1);  // the warp's last row
+  float a[NB];
+#pragma unroll
+  for (int c = 0; c < NB; c++) a[c] = (act && c <= i) ? A[i + (int64_t)c * lda] : 0.f;
+  for (int j = 0; j < nb; j++) {
+    float *cb = colb[j & 1];
+    if (act && i >= j) cb[3 + (i - j)] = a[0];
+    __syncthreads();
+    const float d = cb[3];
+    if (d <= 0.f) {  // NaN passes, as in the reference's "diag <= 0" test
+      if (i == 0) *info = (int32_t)(kb + j + 1);
+      return;
+    }
+    const float ljj = sqrtf(d);
+    const float inv = 1.f / ljj;
+    if (act && i >= j) A[i + (int64_t)j * lda] = i == j ? ljj : a[0] * inv;
+    const int n_out = wlast - j;  // the warp's longest remaining row
+    if (n_out > 0) {
+      const float lij = a[0] * inv;
+      const bool upd = act && i > j;
+#pragma unroll
+      for (int c = 0; c < NB / 32; c++) {
+        if (c * 32 < n_out) {
+#pragma unroll
+          for (int k0 = c * 32; k0 < c * 32 + 32; k0 += 4) {
+            const float4 u = *reinterpret_cast<const float4 *>(cb + 4 + k0);
+            const float uu[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+              if (k0 + q + 1 < NB)
+                a[k0 + q] = upd ? fma(-lij, uu[q] * inv, a[k0 + q + 1]) : a[k0 + q + 1];
+          }
+        }
+      }
+    }
   }
 }
 
@@ -108,6 +168,53 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Float form of the same solve, one thread per row of L21 (128 rows per CTA):
+// row r is independent of the others, x_j = (a_j - sum_{k<j} x_k L(j,k)) /
+// L(j,j).  The row sits in registers in a shifted frame (before step j,
+// a[0..] are its pending columns j, j+1, ...), so the column loop is an
+// ordinary loop over static register indices; step j's column of L11 below
+// the diagonal is read from shared memory with 16-byte broadcast loads.
+// The same FMAs on the same operands as chol_trsm_kernel, in the same order,
+// and no block barrier inside the solve.
+template <int NB>
+__global__ void __launch_bounds__(128)
+    chol_trsm_rows_kernel(int nb, const float *__restrict__ L11, float *__restrict__ A21,
+                          int64_t lda, int64_t m, const int32_t *__restrict__ info) {
+  if (*info != 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float (*Lt)[NB + 4] = reinterpret_cast<float (*)[NB + 4]>(smem_raw);  // Lt[j][k] = L11(j+1+k, j)
+  float *rinv = reinterpret_cast<float *>(smem_raw) + (size_t)NB * (NB + 4);
+  const int tid = threadIdx.x;
+  for (int j = 0; j < nb; j++)
+    for (int k = tid; k < NB; k += 128)
+      Lt[j][k] = (j + 1 + k < nb) ? L11[(j + 1 + k) + (int64_t)j * lda] : 0.f;
+  for (int j = tid; j < nb; j += 128) rinv[j] = 1.f / L11[j + (int64_t)j * lda];
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * 128 + tid;
+  const bool act = r < m;
+  float a[NB];
+#pragma unroll
+  for (int j = 0; j < NB; j++) a[j] = (act && j < nb) ? A21[r + (int64_t)j * lda] : 0.f;
+  for (int j = 0; j < nb; j++) {
+    const float x = a[0] * rinv[j];
+    if (act) A21[r + (int64_t)j * lda] = x;
+    const int n_out = nb - 1 - j;  // pending columns after this step
+#pragma unroll
+    for (int c = 0; c < NB / 32; c++) {
+      if (c * 32 < n_out) {
+#pragma unroll
+        for (int k0 = c * 32; k0 < c * 32 + 32; k0 += 4) {
+          const float4 u = *reinterpret_cast<const float4 *>(&Lt[j][k0]);
+          const float uu[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            if (k0 + q + 1 < NB) a[k0 + q] = fma(-x, uu[q], a[k0 + q + 1]);
+        }
+      }
+    }
+  }
+}
+
 template <typename T>
 int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
   Ctx *cx = ctx();
@@ -131,8 +238,22 @@ int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
     {
       KtScope kt("potrf_diag", nb * (double)nb * nb / 3.0,
                  (double)nb * nb * sizeof(T));
-      kdiag<<<1, 256, diag_smem<T>(nb), cx->stream>>>(nb, A11, lda, info, kb);
-      MGB_TRY(launch_check((const void *)kdiag, "potrf_diag", diag_smem<T>(nb)));
+      if (sizeof(T) == 4 && nb > 64) {
+        if (nb > kCholBlock) {
+          potrf_diag_rows_kernel<kCholBlockLp><<<1, kCholBlockLp, 0, cx->stream>>>(
+              nb, (float *)A11, lda, info, kb);
+          MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlockLp>,
+                               "potrf_diag_rows", 0));
+        } else {
+          potrf_diag_rows_kernel<kCholBlock><<<1, kCholBlock, 0, cx->stream>>>(
+              nb, (float *)A11, lda, info, kb);
+          MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlock>,
+                               "potrf_diag_rows", 0));
+        }
+      } else {
+        kdiag<<<1, 256, diag_smem<T>(nb), cx->stream>>>(nb, A11, lda, info, kb);
+        MGB_TRY(launch_check((const void *)kdiag, "potrf_diag", diag_smem<T>(nb)));
+      }
     }
     const int64_t m = n - kb - nb;
     if (m > 0) {
@@ -140,9 +261,28 @@ int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
       {
         KtScope kt2("chol_trsm", (double)m * nb * nb,
                     2.0 * m * nb * sizeof(T));
-        ktrsm<<<(unsigned)((m + 31) / 32), 256, ctrsm_smem<T>(nb), cx->stream>>>(
-            nb, A11, A21, lda, m, info);
-        MGB_TRY(launch_check((const void *)ktrsm, "chol_trsm", ctrsm_smem<T>(nb)));
+        bool done = false;
+        if constexpr (sizeof(T) == 4) {
+          if (nb == kCholBlockLp || nb == kCholBlock) {
+            const size_t sm = nb == kCholBlockLp ? rows_smem(kCholBlockLp) : rows_smem(kCholBlock);
+            const void *kr = nb == kCholBlockLp ? (const void *)chol_trsm_rows_kernel<kCholBlockLp>
+                                                : (const void *)chol_trsm_rows_kernel<kCholBlock>;
+            MGB_CUDA(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (nb == kCholBlockLp)
+              chol_trsm_rows_kernel<kCholBlockLp><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
+                  nb, (const float *)A11, (float *)A21, lda, m, info);
+            else
+              chol_trsm_rows_kernel<kCholBlock><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
+                  nb, (const float *)A11, (float *)A21, lda, m, info);
+            MGB_TRY(launch_check(kr, "chol_trsm_rows", sm));
+            done = true;
+          }
+        }
+        if (!done) {
+          ktrsm<<<(unsigned)((m + 31) / 32), 256, ctrsm_smem<T>(nb), cx->stream>>>(
+              nb, A11, A21, lda, m, info);
+          MGB_TRY(launch_check((const void *)ktrsm, "chol_trsm", ctrsm_smem<T>(nb)));
+        }
       }
       T *A22 = A + (kb + nb) + (kb + nb) * lda;
       if (lp < 0)

@@ -154,6 +154,12 @@ int trsv_t(bool lower, bool trans, bool unit, int64_t n, const T *Tm,
 int precond_solve(bool spd, int64_t n, const float *W, const int32_t *perm,
                   const float *in, float *out);
 int trsv_status();
+// Triangular solve with many right-hand sides in one launch per 64 columns
+// (trsm_flag.cu); trsm_flag_status() reports a bounded wait that gave up.
+template <typename T>
+int trsm_flag_t(bool lower, bool trans, bool unit, int64_t n, int64_t nrhs,
+                const T *Tm, int64_t ldt, T *B, int64_t ldb, const int32_t *info);
+int trsm_flag_status();
 template <typename T>
 int potrs_t(int64_t n, int64_t nrhs, const T *L, int64_t lda, T *B,
             int64_t ldb, const int32_t *info);

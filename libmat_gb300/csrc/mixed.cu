@@ -605,6 +605,8 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
     return set_error(MATGB_ERR_TIMEOUT, "tensor-core update gave up waiting");
   if (lu_wait_error(1))
     return set_error(MATGB_ERR_TIMEOUT, "LU panel exchange gave up waiting");
+  MGB_TRY(trsv_status());
+  MGB_TRY(trsm_flag_status());
   if (rep) {
     float t = 0;
     cudaEventElapsedTime(&t, g_ir.e[1], g_ir.e[2]);

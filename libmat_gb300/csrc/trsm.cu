@@ -11,6 +11,9 @@
 namespace mgb {
 
 constexpr int kTrsmBlock = 96;
+// 0: the blocked form below (diagonal-block kernel + GEMM updates) instead
+// of the single-launch multi-RHS solver
+static int g_trsm_flag = 1;
 constexpr int kTrsmRhs = 32;
 
 template <typename T>
@@ -125,8 +128,10 @@ int trsm_left_t(bool lower, bool trans, bool unit, int64_t n, int64_t nrhs,
                 const int32_t *info) {
   if (!ctx()) return MATGB_ERR_NO_DEVICE;
   if (n <= 0 || nrhs <= 0) return 0;
-  // one right-hand side: the single-launch solver (no failure flag to honour)
+  // one right-hand side: the single-launch solver (no failure flag to honour);
+  // several: the single-launch multi-RHS solver
   if (nrhs == 1 && !info) return trsv_t<T>(lower, trans, unit, n, Tm, ldt, B);
+  if (g_trsm_flag) return trsm_flag_t<T>(lower, trans, unit, n, nrhs, Tm, ldt, B, ldb, info);
   const bool el = (lower != trans);
   // Pointer to op(T)(r0, c0) for use as a GEMM operand with transpose 'trans'.
   auto sub = [&](int64_t r0, int64_t c0) {
