@@ -244,19 +244,21 @@ int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
   uint16_t *A16lo = split ? A16 + an : nullptr;
   unsigned *amax = (unsigned *)(sc + 4);
   cudaStream_t st = ctx()->stream;
-  KtScope kt("lp_pack", 0.0, (split ? 8.0 : 6.0) * m * nb);
-  dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
-  if (lp == 1) {
-    pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
-  } else {
-    MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
-    amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
-        L21, lda, (int)m, nb, amax);
-    MGB_LAUNCHED("l21_amax");
-    pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc,
-                                          A16lo);
+  {
+    KtScope kt("lp_pack", 0.0, (split ? 8.0 : 6.0) * m * nb);
+    dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
+    if (lp == 1) {
+      pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
+    } else {
+      MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
+      amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
+          L21, lda, (int)m, nb, amax);
+      MGB_LAUNCHED("l21_amax");
+      pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc,
+                                            A16lo);
+    }
+    MGB_LAUNCHED("pack_l21");
   }
-  MGB_LAUNCHED("pack_l21");
   return tc_gemm(lp == 1, m, m, Kp, A16, Kp, A16, Kp, -1.f,
                  lp != 1 ? sc + 2 : nullptr, 1.f, C22, ldc, 1, info, A16lo,
                  A16lo);
