@@ -306,7 +306,7 @@ def run_headline(args, mg):
         "wall_ms_per_step": t_wall * 1e3 / len(seq),
         "dtype": "f64 (FP32 factors, FP16 tensor-core updates, FP32 accumulate)",
         "gpu_launches": launches,
-        "config": {"workload": "mixed_lu_ir_16384_f64", "n": n, "nrhs": 1,
+        "config": {"workload": f"mixed_lu_ir_{n}_f64", "n": n, "nrhs": 1,
                    "kappas": list(KAPPAS), "factor_format": {2: "fp16 split (hi+lo, 3 products)", 1: "bf16",
                                      0: "fp16", -1: "fp32 simt"}[args.lp],
                    "refinement": "FGMRES (FP64) preconditioned by the factors",
@@ -528,7 +528,7 @@ def run_spd(mg, n=16384, nrhs=64):
             out[k]["speedup_vs_plain"] = ms_p / out[k]["ms"]
     del mats, Aw, Xp, X, B
     torch.cuda.empty_cache()
-    return {"workload": "spd_ir_16384_64rhs_f64", **out}
+    return {"workload": f"spd_ir_{n}_{nrhs}rhs_f64", **out}
 
 
 def run_batched(mg, count=100000, steps=5, warmup=3):
