@@ -405,6 +405,12 @@ __device__ __forceinline__ void row_get(const T *src, T (&v)[kW]) {
   }
 }
 
+// Net row map of a panel's swap sequence, kept up to date one pivot at a
+// time by one warp (defined with SwapMap below).
+struct SwapMap;
+__device__ __forceinline__ void swap_map_reset(SwapMap &map, int64_t k0);
+__device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int i, int32_t P);
+
 // The 24-column elimination of a register-resident panel (rows [k0, n) of
 // A, columns [k0, k0+24)): thread tid of CTA c owns panel rows prow[r]
 // (panel-relative, -1 = none) in a[r][*].  ipiv[k0+kk] (CTA 0) and, when
@@ -420,14 +426,22 @@ __device__ __forceinline__ void row_get(const T *src, T (&v)[kW]) {
 // the unrolled form (the same FMAs on the same operands).
 // step: this kernel's running column count (the exchange barriers' phase),
 // nsteps: its total columns (no barrier is armed past the last).
+// map (may be null): the panel's net row map, built by the last warp while
+// it waits for each column's exchange (pivot kk-1 during column kk's wait,
+// the last pivot after the loop); complete once the caller synchronises
+// the CTA.
 template <typename T, int R, int NT>
 __device__ __forceinline__ void reg_panel_columns(
     T (&a)[R][kW], const int (&prow)[R], RegPanelSmem<T, NT> &sm,
     cg::cluster_group &cluster, int c, int CS, int rbase, int rpc, int64_t k0,
-    int32_t *__restrict__ ipiv, int32_t *spiv, T eps, int &step, int nsteps) {
+    int32_t *__restrict__ ipiv, int32_t *spiv, T eps, int &step, int nsteps,
+    SwapMap *map = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = NT / 32;
   (void)cluster;
+  const bool mapper = map && warp == NW - 1;
+  if (mapper) swap_map_reset(*map, k0);
+  int32_t pprev = 0;
 #pragma unroll 1
   for (int kk = 0; kk < kW; kk++, step++) {
     const int buf = step & 1;
@@ -527,12 +541,14 @@ __device__ __forceinline__ void reg_panel_columns(
     }
     __syncwarp();
     if (lane == 0) xch::arrive(&sm.xbar[buf]);
+    if (mapper && kk > 0) swap_map_step(*map, k0, kk - 1, pprev);
     if (!xch::wait(&sm.xbar[buf], (uint32_t)(step >> 1) & 1u)) g_lu_wait_err = 1;
     T gk;
     int p, wc;
     pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
     if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
     if (spiv && tid == 0) spiv[kk] = (int32_t)(k0 + p);
+    pprev = (int32_t)(k0 + p);
     const T *u = &sm.xval[buf][wc][0];
     const T *kv = &sm.kval[buf][0];
     if (p != kk) {
@@ -563,6 +579,7 @@ __device__ __forceinline__ void reg_panel_columns(
       a[r][kW - 1] = l;
     }
   }
+  if (mapper) swap_map_step(*map, k0, kW - 1, pprev);
 }
 
 template <typename T, int R, int NT>
@@ -658,6 +675,48 @@ __device__ void build_swap_map(SwapMap &sm, const int32_t *__restrict__ ipiv,
     __syncwarp();
   }
   if (lane == 0) sm.cnt = nk + nx;
+}
+
+// The same map kept up to date one pivot at a time by one warp (the fused
+// block's panels): reset for the panel starting at row k0, then pivot i
+// (global row P) applied -- the steps of build_swap_map's loop.
+__device__ __forceinline__ void swap_map_reset(SwapMap &map, int64_t k0) {
+  const int lane = threadIdx.x & 31;
+  if (lane < kW) {
+    map.pos[lane] = (int32_t)(k0 + lane);
+    map.src[lane] = (int32_t)(k0 + lane);
+  }
+  if (lane == 0) map.cnt = kW;
+  __syncwarp();
+}
+__device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int i, int32_t P) {
+  const int lane = threadIdx.x & 31;
+  if (P == (int32_t)(k0 + i)) return;
+  int slot;
+  if (P < (int32_t)(k0 + kW)) {
+    slot = P - (int32_t)k0;
+  } else {
+    // rows beyond the panel's first 24 sit at [kW, cnt), at most 24 of them
+    const int cnt = map.cnt;
+    const unsigned hit =
+        __ballot_sync(0xffffffffu, kW + lane < cnt && map.pos[kW + lane] == P);
+    if (hit) {
+      slot = kW + __ffs(hit) - 1;
+    } else {
+      slot = cnt;
+      if (lane == 0) {
+        map.pos[cnt] = P;
+        map.src[cnt] = P;
+        map.cnt = cnt + 1;
+      }
+    }
+  }
+  if (lane == 0) {
+    const int32_t t = map.src[i];
+    map.src[i] = map.src[slot];
+    map.src[slot] = t;
+  }
+  __syncwarp();
 }
 
 // The map is built once per swap block by one warp (swap_map_kernel) into a
@@ -930,7 +989,7 @@ __global__ void __launch_bounds__(NT, 1)
         a[r][j] = prow[r] >= 0 ? __ldcg(&A[(k0 + prow[r]) + (k0 + j) * lda]) : T(0);
     }
     reg_panel_columns<T, R, NT>(a, prow, sm.ps, cluster, c, CS, rbase, rpc, k0,
-                                ipiv, sm.spiv, eps, step, np * kW);
+                                ipiv, sm.spiv, eps, step, np * kW, &sm.map);
 #pragma unroll
     for (int r = 0; r < R; r++)
       if (prow[r] >= 0)
@@ -952,8 +1011,7 @@ __global__ void __launch_bounds__(NT, 1)
     }
     // the panel's swaps on the block's other columns: [kb, k0) and
     // [k0+24, kb+bw); CTA c takes every CS-th of them, one warp per column
-    __syncthreads();
-    if (warp == 0) build_swap_map(sm.map, sm.spiv - k0, k0, k0 + kW);
+    // (the map was built during the panel)
     __syncthreads();
     const int nleft = (int)(k0 - kb), nright = bw - (pn + 1) * kW;
     {
@@ -995,17 +1053,16 @@ __global__ void __launch_bounds__(NT, 1)
       if (lane < kW) colp[lane] = x;
     }
     cluster.sync();
-    // rank-24 update of the rows below the panel, right columns; eight
-    // columns at a time so their L2 loads are all in flight together
+    // rank-24 update of the rows below the panel, right columns, four
+    // columns at a time with the next four columns' L2 loads in flight
     for (int e = tid; e < kW * nright; e += NT) {
       const int i = e % kW, j = e / kW;
       sm.U12t[j][i] = __ldcg(&A[(k0 + i) + (k0 + kW + j) * lda]);
     }
     __syncthreads();
-    constexpr int JB = 8;
+    constexpr int JB = 4;
     T *base = A + (k0 + kW) * lda + k0;
-    for (int j0 = 0; j0 < nright; j0 += JB) {
-      T v[R][JB];
+    auto load_cols = [&](T (&v)[R][JB], int j0) {
 #pragma unroll
       for (int r = 0; r < R; r++)
 #pragma unroll
@@ -1013,6 +1070,8 @@ __global__ void __launch_bounds__(NT, 1)
           v[r][jj] = (prow[r] >= kW && j0 + jj < nright)
                          ? __ldcg(&base[(int64_t)(j0 + jj) * lda + prow[r]])
                          : T(0);
+    };
+    auto update_cols = [&](T (&v)[R][JB], int j0) {
 #pragma unroll
       for (int jj = 0; jj < JB; jj++) {
         if (j0 + jj < nright) {
@@ -1030,6 +1089,14 @@ __global__ void __launch_bounds__(NT, 1)
         for (int jj = 0; jj < JB; jj++)
           if (prow[r] >= kW && j0 + jj < nright)
             base[(int64_t)(j0 + jj) * lda + prow[r]] = v[r][jj];
+    };
+    T v0[R][JB], v1[R][JB];
+    load_cols(v0, 0);
+    for (int j0 = 0; j0 < nright; j0 += 2 * JB) {
+      load_cols(v1, j0 + JB);
+      update_cols(v0, j0);
+      if (j0 + 2 * JB < nright) load_cols(v0, j0 + 2 * JB);
+      update_cols(v1, j0 + JB);
     }
     cluster.sync();
   }
