@@ -405,11 +405,19 @@ __device__ __forceinline__ void row_get(const T *src, T (&v)[kW]) {
   }
 }
 
-// Net row map of a panel's swap sequence, kept up to date one pivot at a
-// time by one warp (defined with SwapMap below).
+// Net row maps of a swap sequence, kept up to date one pivot at a time by
+// one warp (defined with SwapMap below): the panel's (every CTA) and, in one
+// CTA, the whole block's.
 struct SwapMap;
-__device__ __forceinline__ void swap_map_reset(SwapMap &map, int64_t k0);
-__device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int i, int32_t P);
+__device__ __forceinline__ void swap_map_reset(SwapMap &map, int64_t k0, int nk);
+__device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int nk, int i,
+                                              int32_t P);
+struct MapSink {
+  SwapMap *panel;  // this panel's map (null: none kept)
+  SwapMap *block;  // the block's map (null: none kept here)
+  int64_t kb;      // the block's first row
+  int bw;          // the block's width
+};
 
 // The 24-column elimination of a register-resident panel (rows [k0, n) of
 // A, columns [k0, k0+24)): thread tid of CTA c owns panel rows prow[r]
@@ -426,22 +434,27 @@ __device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int i, i
 // the unrolled form (the same FMAs on the same operands).
 // step: this kernel's running column count (the exchange barriers' phase),
 // nsteps: its total columns (no barrier is armed past the last).
-// map (may be null): the panel's net row map, built by the last warp while
-// it waits for each column's exchange (pivot kk-1 during column kk's wait,
-// the last pivot after the loop); complete once the caller synchronises
-// the CTA.
+// maps (may be null): the panel's net row map and the block's, built by the
+// last warp while it waits for each column's exchange (pivot kk-1 during
+// column kk's wait, the last pivot after the loop); complete once the
+// caller synchronises the CTA.
 template <typename T, int R, int NT>
 __device__ __forceinline__ void reg_panel_columns(
     T (&a)[R][kW], const int (&prow)[R], RegPanelSmem<T, NT> &sm,
     cg::cluster_group &cluster, int c, int CS, int rbase, int rpc, int64_t k0,
     int32_t *__restrict__ ipiv, int32_t *spiv, T eps, int &step, int nsteps,
-    SwapMap *map = nullptr) {
+    const MapSink *maps = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = NT / 32;
   (void)cluster;
-  const bool mapper = map && warp == NW - 1;
-  if (mapper) swap_map_reset(*map, k0);
+  const bool mapper = maps && warp == NW - 1;
+  if (mapper) swap_map_reset(*maps->panel, k0, kW);
   int32_t pprev = 0;
+  auto map_pivot = [&](int i) {
+    swap_map_step(*maps->panel, k0, kW, i, pprev);
+    if (maps->block)
+      swap_map_step(*maps->block, maps->kb, maps->bw, (int)(k0 - maps->kb) + i, pprev);
+  };
 #pragma unroll 1
   for (int kk = 0; kk < kW; kk++, step++) {
     const int buf = step & 1;
@@ -541,7 +554,7 @@ __device__ __forceinline__ void reg_panel_columns(
     }
     __syncwarp();
     if (lane == 0) xch::arrive(&sm.xbar[buf]);
-    if (mapper && kk > 0) swap_map_step(*map, k0, kk - 1, pprev);
+    if (mapper && kk > 0) map_pivot(kk - 1);
     if (!xch::wait(&sm.xbar[buf], (uint32_t)(step >> 1) & 1u)) g_lu_wait_err = 1;
     T gk;
     int p, wc;
@@ -579,7 +592,7 @@ __device__ __forceinline__ void reg_panel_columns(
       a[r][kW - 1] = l;
     }
   }
-  if (mapper) swap_map_step(*map, k0, kW - 1, pprev);
+  if (mapper) map_pivot(kW - 1);
 }
 
 template <typename T, int R, int NT>
@@ -678,30 +691,38 @@ __device__ void build_swap_map(SwapMap &sm, const int32_t *__restrict__ ipiv,
 }
 
 // The same map kept up to date one pivot at a time by one warp (the fused
-// block's panels): reset for the panel starting at row k0, then pivot i
+// block's panels): reset for the nk pivots starting at row k0, then pivot i
 // (global row P) applied -- the steps of build_swap_map's loop.
-__device__ __forceinline__ void swap_map_reset(SwapMap &map, int64_t k0) {
+__device__ __forceinline__ void swap_map_reset(SwapMap &map, int64_t k0, int nk) {
   const int lane = threadIdx.x & 31;
-  if (lane < kW) {
-    map.pos[lane] = (int32_t)(k0 + lane);
-    map.src[lane] = (int32_t)(k0 + lane);
+  for (int i = lane; i < nk; i += 32) {
+    map.pos[i] = (int32_t)(k0 + i);
+    map.src[i] = (int32_t)(k0 + i);
   }
-  if (lane == 0) map.cnt = kW;
+  if (lane == 0) map.cnt = nk;
   __syncwarp();
 }
-__device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int i, int32_t P) {
+__device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int nk, int i,
+                                              int32_t P) {
   const int lane = threadIdx.x & 31;
   if (P == (int32_t)(k0 + i)) return;
   int slot;
-  if (P < (int32_t)(k0 + kW)) {
+  if (P < (int32_t)(k0 + nk)) {
     slot = P - (int32_t)k0;
   } else {
-    // rows beyond the panel's first 24 sit at [kW, cnt), at most 24 of them
+    // rows beyond the first nk sit at [nk, cnt), at most nk of them
     const int cnt = map.cnt;
-    const unsigned hit =
-        __ballot_sync(0xffffffffu, kW + lane < cnt && map.pos[kW + lane] == P);
-    if (hit) {
-      slot = kW + __ffs(hit) - 1;
+    int found = -1;
+    for (int base = nk; base < cnt; base += 32) {
+      const unsigned hit =
+          __ballot_sync(0xffffffffu, base + lane < cnt && map.pos[base + lane] == P);
+      if (hit) {
+        found = base + __ffs(hit) - 1;
+        break;
+      }
+    }
+    if (found >= 0) {
+      slot = found;
     } else {
       slot = cnt;
       if (lane == 0) {
@@ -808,6 +829,17 @@ constexpr int kSwapRing = 16;
 static SwapMap *g_swap_ring = nullptr;
 static int g_swap_next = 0;
 
+static SwapMap *swap_ring_slot() {
+  if (!g_swap_ring && cudaMalloc(&g_swap_ring, kSwapRing * sizeof(SwapMap)) != cudaSuccess) {
+    cudaGetLastError();
+    g_swap_ring = nullptr;
+    return nullptr;
+  }
+  SwapMap *m = g_swap_ring + g_swap_next;
+  g_swap_next = (g_swap_next + 1) % kSwapRing;
+  return m;
+}
+
 template <typename T>
 int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
             const int32_t *ipiv, int64_t k1, int64_t k2, int32_t *perm,
@@ -831,6 +863,22 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
     laswp_kernel<T, false><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
         A, lda, c0, c1, c2, c3, map, ipiv, k1, k2, perm);
   }
+  MGB_LAUNCHED("laswp");
+  return 0;
+}
+
+// The same swaps from a net map already on the device (the fused block
+// kernel writes its block's): no map build in the swap stream.
+template <typename T>
+static int laswp_map(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
+                     const SwapMap *map, int32_t *perm, int64_t npiv) {
+  const int64_t ncol = (c1 - c0) + (c3 - c2);
+  if (ncol <= 0 && !perm) return 0;
+  int64_t blocks = (ncol + kSwapCols - 1) / kSwapCols;
+  if (blocks < 1) blocks = 1;
+  KtScope kt("laswp", 0.0, 4.0 * npiv * ncol * sizeof(T));
+  laswp_kernel<T, false><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
+      A, lda, c0, c1, c2, c3, map, nullptr, 0, 0, perm);
   MGB_LAUNCHED("laswp");
   return 0;
 }
@@ -950,7 +998,8 @@ struct VecLoad<float> {
 template <typename T, int NT>
 struct FusedSmem {
   RegPanelSmem<T, NT> ps;
-  SwapMap map;
+  SwapMap map;   // the current panel's net row map
+  SwapMap bmap;  // the block's (CTA 0)
   int32_t spiv[kW];
   T L11[kW][kW + 1];
   __align__(16) T U12t[kFusedMaxBw - kW][kW];  // U12 transposed: k contiguous
@@ -960,7 +1009,7 @@ template <typename T, int R, int NT>
 __global__ void __launch_bounds__(NT, 1)
     lu_block_fused_kernel(T *__restrict__ A, int64_t lda, int64_t n,
                           int64_t kb, int bw, int32_t *__restrict__ ipiv, T eps,
-                          unsigned *__restrict__ amax_l) {
+                          unsigned *__restrict__ amax_l, SwapMap *__restrict__ bmap_out) {
   __shared__ FusedSmem<T, NT> sm;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
@@ -968,6 +1017,11 @@ __global__ void __launch_bounds__(NT, 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NWARP = NT / 32;
   const int np = bw / kW;
+  // the block's net row map (for the swaps of the columns outside the
+  // block) is built by CTA 0's last warp along with the panels' maps
+  const bool keep_block = bmap_out && c == 0;
+  const MapSink sink = {&sm.map, keep_block ? &sm.bmap : nullptr, kb, bw};
+  if (keep_block && warp == NWARP - 1) swap_map_reset(sm.bmap, kb, bw);
   {
     const int rpc0 = (int)((n - kb) + CS - 1) / CS;  // the first panel's rows per CTA
     xch_setup<T, NT>(sm.ps, cluster, CS, c, 0, 1 / rpc0);
@@ -989,7 +1043,7 @@ __global__ void __launch_bounds__(NT, 1)
         a[r][j] = prow[r] >= 0 ? __ldcg(&A[(k0 + prow[r]) + (k0 + j) * lda]) : T(0);
     }
     reg_panel_columns<T, R, NT>(a, prow, sm.ps, cluster, c, CS, rbase, rpc, k0,
-                                ipiv, sm.spiv, eps, step, np * kW, &sm.map);
+                                ipiv, sm.spiv, eps, step, np * kW, &sink);
 #pragma unroll
     for (int r = 0; r < R; r++)
       if (prow[r] >= 0)
@@ -1099,6 +1153,14 @@ __global__ void __launch_bounds__(NT, 1)
       update_cols(v1, j0 + JB);
     }
     cluster.sync();
+  }
+  if (keep_block && warp == NWARP - 1) {
+    const int cnt = sm.bmap.cnt;
+    for (int i = lane; i < cnt; i += 32) {
+      bmap_out->pos[i] = sm.bmap.pos[i];
+      bmap_out->src[i] = sm.bmap.src[i];
+    }
+    if (lane == 0) bmap_out->cnt = cnt;
   }
 }
 
@@ -1425,7 +1487,8 @@ int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
 // (float; rows n-kb <= 16 CTAs x 1024); *done = false otherwise.
 template <typename T>
 static int try_fused_block(T *A, int64_t lda, int64_t n, int64_t kb, int bw,
-                           int32_t *ipiv, T eps, bool *done, unsigned *amax_l) {
+                           int32_t *ipiv, T eps, bool *done, unsigned *amax_l,
+                           SwapMap *bmap) {
   *done = false;
   if constexpr (sizeof(T) != 4) {
     return 0;
@@ -1458,11 +1521,11 @@ static int try_fused_block(T *A, int64_t lda, int64_t n, int64_t kb, int bw,
     if (R == 1) {
       auto kern = lu_block_fused_kernel<T, 1, 512>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps, amax_l);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps, amax_l, bmap);
     } else {
       auto kern = lu_block_fused_kernel<T, 2, 512>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps, amax_l);
+      e = cudaLaunchKernelEx(&cfg, kern, A, lda, n, kb, bw, ipiv, eps, amax_l, bmap);
     }
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -1595,12 +1658,18 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     const int64_t ke = kb + nb;
     unsigned *amax3 = amax_all ? amax_all + 3 * (kb / NB) : nullptr;
     bool l21_ready = false;
+    // a fused block also writes its net row map (into the deferred pass's
+    // slot, or a ring slot), so the swaps below need no map build
+    SwapMap *bmap = nullptr;
     {
       StreamSwap sw(hi);
       bool done = false;
-      if (fused && nb == NB)
+      if (fused && nb == NB) {
+        bmap = defer ? &maps[kb / NB] : swap_ring_slot();
         MGB_TRY(try_fused_block<T>(A, lda, n, kb, (int)nb, ipiv, eps, &done,
-                                   lp == 2 ? amax3 : nullptr));
+                                   lp == 2 ? amax3 : nullptr, bmap));
+      }
+      if (!done) bmap = nullptr;
       l21_ready = done && lp == 2;
       if (!done) MGB_TRY(factor_block<T>(n, A, lda, kb, ke, ipiv, eps));
     }
@@ -1613,7 +1682,10 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       // first, then the panel stream is released; everything else (the other
       // columns, the columns left of the block, the permutation) follows
       // off the critical path
-      MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
+      if (bmap)
+        MGB_TRY(laswp_map<T>(A, lda, ke, ke + nn, 0, 0, bmap, nullptr, nb));
+      else
+        MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
       bool u12_ready = false;
       MGB_TRY(trsm_unit_lower<T>((int)nb, nn, A + kb + kb * lda, lda,
                                  A + kb + ke * lda, lda, amax3 ? amax3 + 1 : nullptr,
@@ -1626,8 +1698,11 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     // the columns right of the look-ahead (and, unless deferred, the columns
     // left of the block) and the permutation; a deferred pass keeps this
     // block's net map
-    MGB_TRY(laswp_t<T>(A, lda, 0, defer ? 0 : kb, ke + nn, n, ipiv, kb, ke, perm,
-                       defer && kb > 0 ? &maps[kb / NB] : nullptr));
+    if (bmap)
+      MGB_TRY(laswp_map<T>(A, lda, 0, defer ? 0 : kb, ke + nn, n, bmap, perm, nb));
+    else
+      MGB_TRY(laswp_t<T>(A, lda, 0, defer ? 0 : kb, ke + nn, n, ipiv, kb, ke, perm,
+                         defer && kb > 0 ? &maps[kb / NB] : nullptr));
     if (ke + nn < n) {
       bool u12_ready = false;
       MGB_TRY(trsm_unit_lower<T>((int)nb, n - ke - nn, A + kb + kb * lda, lda,
