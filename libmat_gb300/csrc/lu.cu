@@ -214,9 +214,32 @@ __device__ __forceinline__ void warp_best(unsigned uk, int idx, unsigned &bk,
   bi = (int)mi;
 }
 
+// Lane holding the best of a warp's float candidates (largest key, then
+// smallest index) when the candidates' indices increase with the lane within
+// each of two ranges, [.., split) before [split, ..): a single max
+// reduction and two ballots instead of a second (index) reduction.
+__device__ __forceinline__ int first_max_lane(unsigned uk, int idx, int split) {
+  const unsigned ub = __reduce_max_sync(0xffffffffu, uk);
+  const unsigned h0 = __ballot_sync(0xffffffffu, uk == ub && idx < split);
+  const unsigned h1 = __ballot_sync(0xffffffffu, uk == ub);
+  return __ffs(h0 ? h0 : h1) - 1;
+}
+
 // Best (key, index) of cnt <= 32 candidates in shared memory, reduced across
 // the warp (every lane gets the result and the winner's slot).  Ties between
 // real candidates cannot happen (their indices are distinct).
+// The same for float candidates whose indices increase with the slot within
+// [.., split) and within [split, ..).
+__device__ __forceinline__ void pick_first(const float *keys, const int *idxs, int cnt,
+                                           int split, float &bk, int &bi, int &bw) {
+  const int lane = threadIdx.x & 31;
+  const float k = lane < cnt ? keys[lane] : -3.f;
+  const int i = lane < cnt ? idxs[lane] : INT_MAX;
+  bw = first_max_lane(ukey(k), i, split);
+  bi = __shfl_sync(0xffffffffu, i, bw);
+  bk = __shfl_sync(0xffffffffu, k, bw);
+}
+
 template <typename T>
 __device__ __forceinline__ void pick_best(const T *keys, const int *idxs,
                                           int cnt, T &bk, int &bi, int &bw) {
@@ -455,6 +478,31 @@ __device__ __forceinline__ void reg_panel_columns(
     if (maps->block)
       swap_map_step(*maps->block, maps->kb, maps->bw, (int)(k0 - maps->kb) + i, pprev);
   };
+  // Exchange pieces (16-byte pieces of a row; per receiver: the candidate
+  // row, its key and index, and row kk when this CTA owns it).  In float
+  // every thread below CS*PER sends one fixed piece to one fixed receiver
+  // every column, so its destinations (both parities) are mapped once here.
+  constexpr int NV = kW * (int)sizeof(T) / 16;
+  constexpr int PER = 2 * NV + 2;
+  constexpr bool kFixed = sizeof(T) == 4 && NT >= 16 * PER;
+  const int sq = tid / PER, se = tid % PER;
+  const bool sender = kFixed && sq < CS;
+  uint32_t sdst0 = 0, sdst1 = 0, sbar0 = 0, sbar1 = 0;
+  if (sender && sq != c) {
+    auto dst_of = [&](int b) -> uint32_t {
+      if (se < NV) return xch::mapa(xch::saddr(&sm.xval[b][c][0]), sq) + 16 * se;
+      if (se == NV) return xch::mapa(xch::saddr(&sm.xkey[b][c]), sq);
+      if (se == NV + 1) return xch::mapa(xch::saddr(&sm.xidx[b][c]), sq);
+      return xch::mapa(xch::saddr(&sm.kval[b][0]), sq) + 16 * (se - NV - 2);
+    };
+    sdst0 = dst_of(0);
+    sdst1 = dst_of(1);
+    sbar0 = xch::mapa(xch::saddr(&sm.xbar[0]), sq);
+    sbar1 = xch::mapa(xch::saddr(&sm.xbar[1]), sq);
+    // never expected: a misaligned barrier is flagged (the receiver's wait
+    // then gives up), never used
+    if ((sbar0 | sbar1) & 7u) g_lu_wait_err = 2;
+  }
 #pragma unroll 1
   for (int kk = 0; kk < kW; kk++, step++) {
     const int buf = step & 1;
@@ -475,7 +523,16 @@ __device__ __forceinline__ void reg_panel_columns(
         const T key = piv_key(a[r][0], prow[r] == kk);
         if (better(key, prow[r], bk, bi)) { bk = key; bi = prow[r]; }
       }
-    if constexpr (sizeof(T) == 4) {
+    // the rows of this CTA: [rbase, rbase+NT) in thread order, then (R = 2)
+    // [rbase+NT, ..) in thread order, so within each range the index grows
+    // with the lane and with the warp
+    const int split = rbase + NT;
+    constexpr bool kOrdered = sizeof(T) == 4 && R <= 2;
+    if constexpr (kOrdered) {
+      const int wl = first_max_lane(ukey(bk), bi, split);
+      bi = __shfl_sync(0xffffffffu, bi, wl);
+      bk = __shfl_sync(0xffffffffu, bk, wl);
+    } else if constexpr (sizeof(T) == 4) {
       unsigned ub;
       warp_best(ukey(bk), bi, ub, bi);
       bk = __shfl_sync(0xffffffffu, bk, __ffs(__ballot_sync(0xffffffffu, ukey(bk) == ub)) - 1);
@@ -497,59 +554,99 @@ __device__ __forceinline__ void reg_panel_columns(
     __syncthreads();
     T ck;
     int ci, cw;
-    pick_best<T>(sm.wkey, sm.widx, NW, ck, ci, cw);
+    if constexpr (kOrdered)
+      pick_first(sm.wkey, sm.widx, NW, split, ck, ci, cw);
+    else
+      pick_best<T>(sm.wkey, sm.widx, NW, ck, ci, cw);
     const bool own_k = (kk >= rbase && kk < rbase + rpc);
     // 16-byte pieces of a row; per receiver: the candidate row, its key and
     // index, and row kk when this CTA owns it.  Other CTAs get st.async
     // (completing bytes on their barrier), this CTA plain stores; every warp
     // then arrives on the local barrier, so its completion also means every
     // local sender has read its staging row
-    constexpr int NV = kW * (int)sizeof(T) / 16;
-    const int per = NV + 2 + (own_k ? NV : 0);
-    const uint32_t lbar = xch::saddr(&sm.xbar[buf]);
     const T *srow = ci != INT_MAX ? &sm.wrow[cw][0] : nullptr;
-    for (int t = tid; t < CS * per; t += NT) {
-      const int q = t / per, e = t % per;
-      if (q == c) {
+    if constexpr (kFixed) {
+      if (sender && (se < NV + 2 || own_k)) {
+        if (sq == c) {
+          if (se < NV) {
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (srow) v = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(srow) + 16 * se);
+            *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.xval[buf][c][0]) + 16 * se) = v;
+          } else if (se == NV) {
+            sm.xkey[buf][c] = ck;
+          } else if (se == NV + 1) {
+            sm.xidx[buf][c] = ci;
+          } else {
+            const int o = 16 * (se - NV - 2);
+            *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.kval[buf][0]) + o) =
+                *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(&sm.krow[0]) + o);
+          }
+        } else if (!((sbar0 | sbar1) & 7u)) {
+          const uint32_t dst = buf ? sdst1 : sdst0, rbar = buf ? sbar1 : sbar0;
+          if (se < NV) {
+            if (srow) {
+              xch::put16(dst, reinterpret_cast<const char *>(srow) + 16 * se, rbar);
+            } else {
+              const uint4 z = make_uint4(0, 0, 0, 0);
+              xch::put16(dst, &z, rbar);
+            }
+          } else if (se == NV) {
+            xch::put4(dst, __float_as_uint((float)ck), rbar);
+          } else if (se == NV + 1) {
+            xch::put4(dst, (uint32_t)ci, rbar);
+          } else {
+            xch::put16(dst, reinterpret_cast<const char *>(&sm.krow[0]) + 16 * (se - NV - 2), rbar);
+          }
+        }
+      }
+    }
+    // otherwise: one loop over all pieces (double rows need more threads)
+    if constexpr (!kFixed) {
+      const int per = NV + 2 + (own_k ? NV : 0);
+      const uint32_t lbar = xch::saddr(&sm.xbar[buf]);
+      for (int t = tid; t < CS * per; t += NT) {
+        const int q = t / per, e = t % per;
+        if (q == c) {
+          if (e < NV) {
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (srow) v = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(srow) + 16 * e);
+            *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.xval[buf][c][0]) + 16 * e) = v;
+          } else if (e == NV) {
+            sm.xkey[buf][c] = ck;
+          } else if (e == NV + 1) {
+            sm.xidx[buf][c] = ci;
+          } else {
+            const int o = 16 * (e - NV - 2);
+            *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.kval[buf][0]) + o) =
+                *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(&sm.krow[0]) + o);
+          }
+          continue;
+        }
+        const uint32_t rbar = xch::mapa(lbar, q);
+        if (rbar & 7u) {  // never expected: a misaligned barrier is flagged, not used
+          g_lu_wait_err = 2;
+          continue;
+        }
         if (e < NV) {
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (srow) v = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(srow) + 16 * e);
-          *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.xval[buf][c][0]) + 16 * e) = v;
+          const uint32_t dst = xch::mapa(xch::saddr(&sm.xval[buf][c][0]), q) + 16 * e;
+          if (srow) {
+            xch::put16(dst, reinterpret_cast<const char *>(srow) + 16 * e, rbar);
+          } else {
+            const uint4 z = make_uint4(0, 0, 0, 0);
+            xch::put16(dst, &z, rbar);
+          }
         } else if (e == NV) {
-          sm.xkey[buf][c] = ck;
+          const uint32_t dst = xch::mapa(xch::saddr(&sm.xkey[buf][c]), q);
+          if constexpr (sizeof(T) == 4)
+            xch::put4(dst, __float_as_uint((float)ck), rbar);
+          else
+            xch::put8(dst, (uint64_t)__double_as_longlong((double)ck), rbar);
         } else if (e == NV + 1) {
-          sm.xidx[buf][c] = ci;
+          xch::put4(xch::mapa(xch::saddr(&sm.xidx[buf][c]), q), (uint32_t)ci, rbar);
         } else {
-          const int o = 16 * (e - NV - 2);
-          *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.kval[buf][0]) + o) =
-              *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(&sm.krow[0]) + o);
+          const uint32_t dst = xch::mapa(xch::saddr(&sm.kval[buf][0]), q) + 16 * (e - NV - 2);
+          xch::put16(dst, reinterpret_cast<const char *>(&sm.krow[0]) + 16 * (e - NV - 2), rbar);
         }
-        continue;
-      }
-      const uint32_t rbar = xch::mapa(lbar, q);
-      if (rbar & 7u) {  // never expected: a misaligned barrier is flagged, not used
-        g_lu_wait_err = 2;
-        continue;
-      }
-      if (e < NV) {
-        const uint32_t dst = xch::mapa(xch::saddr(&sm.xval[buf][c][0]), q) + 16 * e;
-        if (srow) {
-          xch::put16(dst, reinterpret_cast<const char *>(srow) + 16 * e, rbar);
-        } else {
-          const uint4 z = make_uint4(0, 0, 0, 0);
-          xch::put16(dst, &z, rbar);
-        }
-      } else if (e == NV) {
-        const uint32_t dst = xch::mapa(xch::saddr(&sm.xkey[buf][c]), q);
-        if constexpr (sizeof(T) == 4)
-          xch::put4(dst, __float_as_uint((float)ck), rbar);
-        else
-          xch::put8(dst, (uint64_t)__double_as_longlong((double)ck), rbar);
-      } else if (e == NV + 1) {
-        xch::put4(xch::mapa(xch::saddr(&sm.xidx[buf][c]), q), (uint32_t)ci, rbar);
-      } else {
-        const uint32_t dst = xch::mapa(xch::saddr(&sm.kval[buf][0]), q) + 16 * (e - NV - 2);
-        xch::put16(dst, reinterpret_cast<const char *>(&sm.krow[0]) + 16 * (e - NV - 2), rbar);
       }
     }
     __syncwarp();
@@ -558,7 +655,11 @@ __device__ __forceinline__ void reg_panel_columns(
     if (!xch::wait(&sm.xbar[buf], (uint32_t)(step >> 1) & 1u)) g_lu_wait_err = 1;
     T gk;
     int p, wc;
-    pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
+    // CTA q's candidate lies in [q*rpc, (q+1)*rpc): indices grow with q
+    if constexpr (sizeof(T) == 4)
+      pick_first(sm.xkey[buf], sm.xidx[buf], CS, INT_MAX, gk, p, wc);
+    else
+      pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
     if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
     if (spiv && tid == 0) spiv[kk] = (int32_t)(k0 + p);
     pprev = (int32_t)(k0 + p);
