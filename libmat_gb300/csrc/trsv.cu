@@ -123,6 +123,9 @@ __global__ void __launch_bounds__(4 * RB)
     }
   }
 
+  // this block's right-hand side, read before the wait (only this CTA
+  // writes these entries of x)
+  const T bv = (tid < rows) ? __ldcg(&x[r0 + tid]) : T(0);
   const int need = t;  // blocks before this one in solve order
   auto tile_col0 = [&](int k) -> int64_t {
     return (int64_t)(EL ? k : nb - 1 - k) * RB;
@@ -190,13 +193,14 @@ __global__ void __launch_bounds__(4 * RB)
       if (k + 1 < need) load_tile(k + 1, nxt);
       const int64_t c0 = tile_col0(k);
       if (!TR) {
+        // the warp's CPT entries of x_k: one coalesced load, then shuffles
+        // (a warp's threads share g)
         const int g = tid / RB;
+        const int64_t cl = c0 + g * CPT + (lane % CPT);
+        const T xl = cl < n ? __ldcg(&x[cl]) : T(0);
 #pragma unroll
-        for (int qq = 0; qq < CPT; qq++) {
-          const int64_t c = c0 + g * CPT + qq;
-          const T xv = c < n ? __ldcg(&x[c]) : T(0);
-          acc[0] = fma(cur[qq], xv, acc[0]);
-        }
+        for (int qq = 0; qq < CPT; qq++)
+          acc[0] = fma(cur[qq], __shfl_sync(0xffffffffu, xl, qq), acc[0]);
       } else {
         T xv[LPC];
 #pragma unroll
@@ -235,7 +239,7 @@ __global__ void __launch_bounds__(4 * RB)
     if (tid < rows) {
       s = sm.part[0][tid];
       if (!TR) s += sm.part[1][tid] + sm.part[2][tid] + sm.part[3][tid];
-      s = __ldcg(&x[r0 + tid]) - s;
+      s = bv - s;
     }
     sm.xs[tid] = s;
   }
