@@ -871,7 +871,7 @@ __global__ void __launch_bounds__(256)
     laswp_kernel(T *__restrict__ A, int64_t lda, int64_t c0, int64_t c1,
                  int64_t c2, int64_t c3, const SwapMap *__restrict__ map,
                  const int32_t *__restrict__ ipiv, int64_t k1, int64_t k2,
-                 int32_t *__restrict__ perm) {
+                 int32_t *__restrict__ perm, int cpb = kSwapCols) {
   constexpr int RPL = 2 * kSwapMax / 32;  // map entries per lane
   __shared__ SwapMap sm;
   if (BUILD) {
@@ -895,8 +895,8 @@ __global__ void __launch_bounds__(256)
     pos[q] = r < cnt ? sm.pos[r] : 0;
   }
   const int64_t na = c1 - c0, nb = c3 - c2;
-  for (int cc = warp; cc < kSwapCols; cc += 8) {
-    const int64_t t = (int64_t)blockIdx.x * kSwapCols + cc;
+  for (int cc = warp; cc < cpb; cc += 8) {
+    const int64_t t = (int64_t)blockIdx.x * cpb + cc;
     if (t >= na + nb) break;
     T *colp = A + (t < na ? c0 + t : c2 + (t - na)) * lda;
     T v[RPL];
@@ -975,11 +975,14 @@ static int laswp_map(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int6
                      const SwapMap *map, int32_t *perm, int64_t npiv) {
   const int64_t ncol = (c1 - c0) + (c3 - c2);
   if (ncol <= 0 && !perm) return 0;
-  int64_t blocks = (ncol + kSwapCols - 1) / kSwapCols;
+  // few columns (the look-ahead's): one column per warp, so the column
+  // loads of every warp are in flight at once
+  const int cpb = ncol <= 1024 ? 8 : kSwapCols;
+  int64_t blocks = (ncol + cpb - 1) / cpb;
   if (blocks < 1) blocks = 1;
   KtScope kt("laswp", 0.0, 4.0 * npiv * ncol * sizeof(T));
   laswp_kernel<T, false><<<(unsigned)blocks, 256, 0, ctx()->stream>>>(
-      A, lda, c0, c1, c2, c3, map, nullptr, 0, 0, perm);
+      A, lda, c0, c1, c2, c3, map, nullptr, 0, 0, perm, cpb);
   MGB_LAUNCHED("laswp");
   return 0;
 }
@@ -1278,10 +1281,16 @@ __global__ void __launch_bounds__(256)
   constexpr int RPL = (TB + 31) / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Ls = (T *)smem_raw;  // Ls[k*(TB+1) + i] = L(i, k)
+  // L11 staged by asynchronous copies: every element's load in flight at
+  // once instead of a load-store round trip per element
   for (int e = threadIdx.x; e < TB * TB; e += 256) {
     const int i = e % TB, k = e / TB;
-    Ls[k * (TB + 1) + i] = L[i + (int64_t)k * ldl];
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&Ls[k * (TB + 1) + i]);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst),
+                 "l"(&L[i + (int64_t)k * ldl]), "n"(sizeof(T))
+                 : "memory");
   }
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t col = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
