@@ -41,6 +41,18 @@ __device__ __forceinline__ int ld_acquire(const int *p) {
 __device__ __forceinline__ void st_release(int *p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Float solutions are published as 64-bit words (launch epoch << 32 | value
+// bits): an aligned 64-bit access is single-copy atomic, so a word that
+// carries this launch's epoch carries this launch's value -- no flag and no
+// fence between the value and its readiness.
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 
 template <typename T, int RB>
 struct TvSmem {
@@ -61,7 +73,10 @@ template <typename T, int RB, bool EL, bool TR, bool UNIT, bool INV>
 __global__ void __launch_bounds__(4 * RB)
     trsv_kernel(int64_t n, const T *__restrict__ Tm, int64_t ldt,
                 T *__restrict__ x, int *__restrict__ flags,
-                TvState *__restrict__ stt, int epoch) {
+                TvState *__restrict__ stt, int epoch,
+                unsigned long long *__restrict__ xp) {
+  // float: x blocks travel as epoch-tagged words in xp (no flags)
+  constexpr bool PK = sizeof(T) == 4;
   constexpr int NT = 4 * RB;
   constexpr int NW = NT / 32;
   constexpr int CPT = RB / 4;      // tile entries per thread
@@ -159,7 +174,76 @@ __global__ void __launch_bounds__(4 * RB)
   for (int a = 0; a < (TR ? RPW : 1); a++) acc[a] = T(0);
   if (need > 0) load_tile(0, cur);
 
-  int done = 0, par = 0;
+  if constexpr (PK) {
+    // every warp folds the tiles in order, polling its own entries of x_k
+    // until they carry this launch's epoch (bounded)
+    const uint32_t ep = (uint32_t)epoch;
+    for (int k = 0; k < need; k++) {
+      if (k + 1 < need) load_tile(k + 1, nxt);
+      const int64_t c0 = tile_col0(k);
+      bool fail = false;
+      if (!TR) {
+        const int g = tid / RB;
+        const int64_t cl = c0 + g * CPT + (lane % CPT);
+        const bool in = cl < n;
+        unsigned long long v = in ? ld_relaxed_u64(&xp[cl]) : 0ull;
+        uint32_t spins = 0;
+        while (!__all_sync(0xffffffffu, !in || (uint32_t)(v >> 32) == ep)) {
+          if (++spins > kTvSpinLimit) {
+            fail = true;
+            break;
+          }
+          if (in && (uint32_t)(v >> 32) != ep) v = ld_relaxed_u64(&xp[cl]);
+        }
+        if (fail) {
+          s_fail = 1;
+          break;
+        }
+        const T xl = in ? (T)__uint_as_float((uint32_t)v) : T(0);
+#pragma unroll
+        for (int qq = 0; qq < CPT; qq++)
+          acc[0] = fma(cur[qq], __shfl_sync(0xffffffffu, xl, qq), acc[0]);
+      } else {
+        unsigned long long v[LPC];
+        bool in[LPC];
+#pragma unroll
+        for (int m = 0; m < LPC; m++) {
+          const int64_t c = c0 + lane + 32 * m;
+          in[m] = c < n;
+          v[m] = in[m] ? ld_relaxed_u64(&xp[c]) : 0ull;
+        }
+        uint32_t spins = 0;
+        for (;;) {
+          bool ok = true;
+#pragma unroll
+          for (int m = 0; m < LPC; m++) ok = ok && (!in[m] || (uint32_t)(v[m] >> 32) == ep);
+          if (__all_sync(0xffffffffu, ok)) break;
+          if (++spins > kTvSpinLimit) {
+            fail = true;
+            break;
+          }
+#pragma unroll
+          for (int m = 0; m < LPC; m++)
+            if (in[m] && (uint32_t)(v[m] >> 32) != ep) v[m] = ld_relaxed_u64(&xp[c0 + lane + 32 * m]);
+        }
+        if (fail) {
+          s_fail = 1;
+          break;
+        }
+        T xv[LPC];
+#pragma unroll
+        for (int m = 0; m < LPC; m++) xv[m] = in[m] ? (T)__uint_as_float((uint32_t)v[m]) : T(0);
+#pragma unroll
+        for (int a = 0; a < RPW; a++)
+#pragma unroll
+          for (int m = 0; m < LPC; m++) acc[a] = fma(cur[a * LPC + m], xv[m], acc[a]);
+      }
+#pragma unroll
+      for (int qq = 0; qq < CPT; qq++) cur[qq] = nxt[qq];
+    }
+    __syncthreads();
+  }
+  int done = PK ? need : 0, par = 0;
   while (done < need) {
     // wait for tile `done`, then count the ready tiles after it
     if (tid == 0) {
@@ -305,10 +389,19 @@ __global__ void __launch_bounds__(4 * RB)
 #pragma unroll
     for (int m = 0; m < YR; m++)
       if (lane + 32 * m < rows) x[r0 + lane + 32 * m] = y[m];
-    __syncwarp();
-    if (lane == 0) {
-      __threadfence();
-      st_release(&flags[b], epoch);
+    if constexpr (PK) {
+#pragma unroll
+      for (int m = 0; m < YR; m++)
+        if (lane + 32 * m < rows)
+          st_relaxed_u64(&xp[r0 + lane + 32 * m],
+                         ((unsigned long long)(uint32_t)epoch << 32) |
+                             __float_as_uint((float)y[m]));
+    } else {
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence();
+        st_release(&flags[b], epoch);
+      }
     }
   }
 }
@@ -318,6 +411,8 @@ struct TvBufs {
   TvState *st = nullptr;
   int64_t cap = 0;
   int epoch = 0;
+  unsigned long long *xp = nullptr;  // epoch-tagged float solutions
+  int64_t xcap = 0;
 };
 static TvBufs g_tv;
 
@@ -336,6 +431,24 @@ static int launch_trsv(int64_t n, const T *Tm, int64_t ldt, T *x) {
     g_tv.cap = cap;
     g_tv.epoch = 0;
   }
+  unsigned long long *xp = nullptr;
+  if constexpr (sizeof(T) == 4) {
+    const int64_t need = (int64_t)nb * RB;
+    if (g_tv.xcap < need) {
+      if (g_tv.xp) {
+        cudaStreamSynchronize(ctx()->stream);
+        cudaFree(g_tv.xp);
+        g_tv.xp = nullptr;
+        g_tv.xcap = 0;
+      }
+      const int64_t cap = need < 65536 ? 65536 : need;
+      MGB_CUDA(cudaMalloc(&g_tv.xp, cap * sizeof(unsigned long long)));
+      // epoch 0 is never a launch's epoch
+      MGB_CUDA(cudaMemset(g_tv.xp, 0, cap * sizeof(unsigned long long)));
+      g_tv.xcap = cap;
+    }
+    xp = g_tv.xp;
+  }
   g_tv.epoch++;
   auto k = trsv_kernel<T, RB, EL, TR, UNIT, INV>;
   const size_t smem = sizeof(TvSmem<T, RB>);
@@ -344,7 +457,7 @@ static int launch_trsv(int64_t n, const T *Tm, int64_t ldt, T *x) {
   MGB_CUDA(cudaMemsetAsync(&g_tv.st->ticket, 0, sizeof(int), ctx()->stream));
   KtScope kt(INV ? "trsv_inv" : "trsv", (double)n * n, (double)sizeof(T) * n * n / 2.0);
   k<<<nb, 4 * RB, smem, ctx()->stream>>>(n, Tm, ldt, x, g_tv.flags, g_tv.st,
-                                         g_tv.epoch);
+                                         g_tv.epoch, xp);
   return launch_check((const void *)k, "trsv", smem);
 }
 
