@@ -330,6 +330,79 @@ __device__ int solve_one(const T *__restrict__ A, int n,
   return 0;
 }
 
+// General systems, diagonal pivots first (KIND 2): the same Gauss-Jordan
+// steps with logical row K as the pivot of step K, so a step needs no pivot
+// search -- the row's owner stages it, one barrier, every row eliminates.
+// Each row below K checks that partial pivoting would have kept row K (its
+// key no larger than row K's; equal keys go to the smaller row, K), and if
+// any row of the system ever would have won, the system is solved again by
+// solve_one with the search.  Otherwise the pivot sequence is partial
+// pivoting's and every operation is the one solve_one performs, so x is
+// the same either way.  Diagonally dominant systems never fall back.
+template <typename T>
+__device__ __forceinline__ auto spec_key(T v, bool first) {
+  if constexpr (sizeof(T) == 4)
+    return fkey(v, first);
+  else
+    return bkey(v, first);
+}
+
+// The fallback as a call of its own, so its register frame does not add to
+// the diagonal-first loop's.
+template <typename T, int NB>
+__device__ __noinline__ int solve_pivoted(const T *__restrict__ A, int n,
+                                          const T *__restrict__ b, T *__restrict__ x,
+                                          BatchSmem<T, NB> &sm, int i, T eps) {
+  return solve_one<T, NB, 0>(A, n, b, x, sm, i, eps);
+}
+
+template <typename T, int NB>
+__device__ int solve_diag_first(const T *__restrict__ A, int n,
+                                const T *__restrict__ b, T *__restrict__ x,
+                                BatchSmem<T, NB> &sm, int i, T eps) {
+  const bool act = i < n;
+  T a[NB];
+  T rb = act ? b[i] : T(0);
+#pragma unroll
+  for (int j = 0; j < NB; j++) a[j] = (act && j < n) ? A[i + (int64_t)j * n] : T(0);
+  T dg = T(1);
+  bool beaten = false;
+  for (int K = 0; K < n; K++) {
+    const int par = K & 1;
+    const int live = n - K;
+    if (act && i == K) put_row<T, NB>(sm.slot[par][0], a, rb, live);
+    gsync<NB>();
+    const T *u = sm.slot[par][0];
+    const T piv = u[3];
+    // the last column is not searched (mat_plu)
+    if (act && i > K && K < n - 1 && spec_key(a[0], false) > spec_key(piv, true))
+      beaten = true;
+    const bool is_piv = act && i == K;
+    if (is_piv) dg = a[0];
+    const bool elim = !(fabs(piv) < eps);
+    const T l = (act && elim && !is_piv) ? a[0] * (T(1) / piv) : T(0);
+    shift_update<T, NB>(a, rb, u, l, live - 1);
+  }
+  // did partial pivoting pick another row anywhere?
+  bool any;
+  if constexpr (Warps<NB>::v == 1) {
+    any = __any_sync(group_mask<NB>(), beaten);
+  } else {
+    const bool wany = __any_sync(0xffffffffu, beaten);
+    if ((i & 31) == 0) sm.widx[0][i >> 5] = wany ? 1 : 0;
+    gsync<NB>();
+    any = false;
+#pragma unroll
+    for (int w = 0; w < Warps<NB>::v; w++) any = any || sm.widx[0][w] != 0;
+    gsync<NB>();  // the flags are read before the next system reuses them
+  }
+  if (!any) {
+    if (act) x[i] = rb / dg;
+    return 0;
+  }
+  return solve_pivoted<T, NB>(A, n, b, x, sm, i, eps);
+}
+
 // ---------------------------------------------------------------------------
 // SPD systems: LDL^T elimination on the lower triangle (all that mat_chol
 // reads), thread i owning row i, no exchanges.  Before step K row i >= K
@@ -464,6 +537,9 @@ __global__ void __launch_bounds__(Tpg<NB>::v *GROUPS, MinCtas<NB>::v)
     int st;
     if constexpr (KIND == 1)
       st = solve_spd<T, NB>(A + offA[s], n, b + offv[s], x + offv[s], smem[g], i);
+    else if constexpr (KIND == 2)
+      st = solve_diag_first<T, NB>(A + offA[s], n, b + offv[s], x + offv[s],
+                                   smem[g], i, eps);
     else
       st = solve_one<T, NB, KIND>(A + offA[s], n, b + offv[s], x + offv[s],
                                   smem[g], i, eps);
@@ -494,7 +570,7 @@ int launch_batched_queue(int queue, const int32_t *list, BatchQueues *q,
   static const char *names[2][5] = {
       {"batched_lu_16", "batched_lu_32", "batched_lu_64", "batched_lu_96", "batched_lu_128"},
       {"batched_spd_16", "batched_spd_32", "batched_spd_64", "batched_spd_96", "batched_spd_128"}};
-  KtScope kt(names[KIND][NB <= 16 ? 0 : NB <= 32 ? 1 : NB <= 64 ? 2 : NB <= 96 ? 3 : 4], 0.0, 0.0);
+  KtScope kt(names[KIND == 1][NB <= 16 ? 0 : NB <= 32 ? 1 : NB <= 64 ? 2 : NB <= 96 ? 3 : 4], 0.0, 0.0);
   k<<<grid, threads, smem, ctx()->stream>>>(queue, list, q, n, offA, A, offv, b,
                                             x, status, eps);
   MGB_LAUNCHED("batched_solve");

@@ -7,7 +7,7 @@ int batched_bucket_64_lu(int queue, const int32_t *list, BatchQueues *q,
                        const int32_t *n, const int64_t *offA,
                        const elem_t *A, const int64_t *offv,
                        const elem_t *b, elem_t *x, int32_t *status) {
-  return launch_batched_queue<elem_t, 64, 1, 0>(queue, list, q, n, offA, A,
+  return launch_batched_queue<elem_t, 64, 1, 2>(queue, list, q, n, offA, A,
                                                    offv, b, x, status, kPivotEps);
 }
 

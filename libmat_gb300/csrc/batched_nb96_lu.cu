@@ -14,7 +14,7 @@ int batched_bucket_96_lu(int queue, const int32_t *list, BatchQueues *q,
   (void)b; (void)x; (void)status;
   return 0;
 #else
-  return launch_batched_queue<elem_t, 96, 1, 0>(queue, list, q, n, offA, A,
+  return launch_batched_queue<elem_t, 96, 1, 2>(queue, list, q, n, offA, A,
                                                    offv, b, x, status, kPivotEps);
 #endif
 }
