@@ -370,7 +370,10 @@ __device__ int solve_diag_first(const T *__restrict__ A, int n,
   for (int K = 0; K < n; K++) {
     const int par = K & 1;
     const int live = n - K;
-    if (act && i == K) put_row<T, NB>(sm.slot[par][0], a, rb, live);
+    if (act && i == K) {
+      put_row<T, NB>(sm.slot[par][0], a, rb, live);
+      sm.slot[par][0][2] = T(1) / a[0];  // the pivot's reciprocal, divided once
+    }
     gsync<NB>();
     const T *u = sm.slot[par][0];
     const T piv = u[3];
@@ -380,7 +383,7 @@ __device__ int solve_diag_first(const T *__restrict__ A, int n,
     const bool is_piv = act && i == K;
     if (is_piv) dg = a[0];
     const bool elim = !(fabs(piv) < eps);
-    const T l = (act && elim && !is_piv) ? a[0] * (T(1) / piv) : T(0);
+    const T l = (act && elim && !is_piv) ? a[0] * u[2] : T(0);
     shift_update<T, NB>(a, rb, u, l, live - 1);
   }
   // did partial pivoting pick another row anywhere?
@@ -458,11 +461,12 @@ __device__ int solve_spd(const T *__restrict__ A, int n,
     if (i == K) {
       sm.ys[K] = rb;
       myoff = off;
+      col[2] = T(1) / a[0];  // the pivot's reciprocal, divided once
     }
     gsync<NB>();
     const T d = col[3];
     if (d <= T(0)) return -1;  // NaN passes, as in mat_chol
-    const T rd = T(1) / d;
+    const T rd = col[2];
     if (i == K) rdg = rd;
     const int n_out = wlast - K;  // the warp's longest remaining row
     if (n_out > 0) {
