@@ -1211,14 +1211,14 @@ __global__ void __launch_bounds__(NT, 1)
       if (lane < kW) colp[lane] = x;
     }
     cluster.sync();
-    // rank-24 update of the rows below the panel, right columns, four
-    // columns at a time with the next four columns' L2 loads in flight
+    // rank-24 update of the rows below the panel, right columns, a group of
+    // columns at a time with the next group's L2 loads in flight
     for (int e = tid; e < kW * nright; e += NT) {
       const int i = e % kW, j = e / kW;
       sm.U12t[j][i] = __ldcg(&A[(k0 + i) + (k0 + kW + j) * lda]);
     }
     __syncthreads();
-    constexpr int JB = 4;
+    constexpr int JB = R == 1 ? 8 : 4;  // columns per group (registers allow 8 at one row)
     T *base = A + (k0 + kW) * lda + k0;
     auto load_cols = [&](T (&v)[R][JB], int j0) {
 #pragma unroll
