@@ -206,6 +206,18 @@ int matgb_potrf_lp_dev(size_t n, float *A, size_t lda, int32_t *info,
  * ipiv/perm as matgb_getrf_dev.  Pivots are never skipped (threshold 0). */
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
                        int32_t *perm, int lp_format);
+/* R -= A X (double build only; A n x n, X and R n x nrhs, column-major) with
+ * FP64-level accuracy from exact FP16 digit products on the tensor cores:
+ * rows of A and columns of X are cut into 8 signed 7-bit digits under a
+ * power-of-two scale, digit pairs multiplied over 1024-term chunks (exact
+ * in FP32) and accumulated in FP64.  The multi-RHS refinement residual of
+ * matgb_gesv_ir_multi_dev / matgb_posv_ir_dev (the step of mat.h:4820-4837
+ * and 4862-4865 repeated per correction) uses it from n = 1024 up. */
+int matgb_resid64_dev(size_t n, size_t nrhs, const mat_elem_t *A, size_t lda,
+                      const mat_elem_t *X, size_t ldx, mat_elem_t *R, size_t ldr);
+/* 0: the multi-RHS refinement forms residuals with the FP64 GEMM instead
+ * (for measurement); 1 (default): digit slices on the tensor cores. */
+int matgb_resid64_mode(int on);
 /* C (fp32, column-major, M x N) = beta*C + alpha * A * B^T with A (M x K) and
  * B (N x K) K-contiguous BF16 (bf16 != 0) or FP16, K a multiple of 64 and at
  * most 128, lda/ldb multiples of 8: the tensor-core rank-K update

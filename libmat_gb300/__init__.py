@@ -166,6 +166,8 @@ class Lib:
             "mat_solve_spd_ir": (_I, [MP, MP, MP, C.POINTER(MatIROpts),
                                       C.POINTER(MatIRReport)]),
             "matgb_potrf_lp_dev": (_I, [_S, _P, _S, _P, _I]),
+            "matgb_resid64_dev": (_I, [_S, _S, _P, _S, _P, _S, _P, _S]),
+            "matgb_resid64_mode": (_I, [_I]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(c, name)

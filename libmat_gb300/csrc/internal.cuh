@@ -51,6 +51,7 @@ struct KtScope {
 enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
   WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_SWM, WS_SWG,
+  WS_RZA, WS_RZB, WS_RZC, WS_RZE,
   WS_NSLOTS
 };
 void *ws(int slot, size_t bytes);
@@ -138,6 +139,11 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
             int lower, const int32_t *skip, const void *Alo = nullptr,
             const void *Blo = nullptr);
+// FP64 residual R -= A X (X n x nrhs) on the tensor cores from exact FP16
+// digit products (resid64.cu); resid64_prepare slices A once per solve.
+int resid64_prepare(int64_t n, const double *A, int64_t lda);
+int resid64(int64_t n, int64_t nrhs, const double *A, const double *X, int64_t ldx,
+            double *R, int64_t ldr);
 // Cholesky trailing update C22 -= L21 L21^T on the tensor cores (mixed.cu).
 int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
                    float *C22, int64_t ldc, int lp, const int32_t *info);

@@ -395,6 +395,11 @@ static IrEvents g_ir;
 // with a low-precision LU (spd = false) or Cholesky (spd = true) and
 // refinement in the element type.  Returns 0, or sets *not_spd when even the
 // FP32 Cholesky meets a non-positive pivot.
+// Residuals by digit slices on the tensor cores from this order up (below
+// it the FP64 GEMM is cheap); matgb_resid64_mode switches them off.
+constexpr int64_t kResid64MinN = 1024;
+static int g_resid64_on = 1;
+
 int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
              const elem_t *B, int64_t ldb, elem_t *X, int64_t ldx,
              const MatIROpts &o, MatIRReport *rep, int *not_spd) {
@@ -547,6 +552,15 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
         prev = eta;
       }
     }
+    // FP64 residuals of many right-hand sides on the tensor cores (digit
+    // slices of A made once per solve); see resid64.cu
+    bool rz = false;
+#ifdef MAT_DOUBLE_PRECISION
+    if (!use_krylov && nrhs > 1 && n >= kResid64MinN && g_resid64_on) {
+      MGB_TRY(resid64_prepare(n, A, lda));
+      rz = true;
+    }
+#endif
     while (!use_krylov && it < maxit) {
       // correction D = (LU)^{-1} R in FP32, column-scaled (first pass: plain)
       MGB_CUDA(cudaMemsetAsync(rs, 0, (size_t)2 * nrhs * sizeof(unsigned long long), st));
@@ -570,6 +584,10 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
       MGB_LAUNCHED("copy_cols");
       if (nrhs == 1 && ldx >= n)
         MGB_TRY(gemv_t<elem_t>(n, n, elem_t(-1), A, lda, X, elem_t(1), R));
+#ifdef MAT_DOUBLE_PRECISION
+      else if (rz)
+        MGB_TRY(resid64(n, nrhs, A, X, ldx, R, n));
+#endif
       else
         MGB_TRY(gemm_skip_t<elem_t>(false, false, n, nrhs, n, elem_t(-1), A,
                                     lda, X, ldx, elem_t(1), R, n, 0, nullptr));
@@ -649,6 +667,24 @@ void matgb_ir_default_opts(MatIROpts *o) {
   o->fp32_fallback = 1;
   o->krylov = 1;
   o->krylov_dim = 50;
+}
+
+int matgb_resid64_mode(int on) {
+  mgb::g_resid64_on = on ? 1 : 0;
+  return 0;
+}
+
+int matgb_resid64_dev(size_t n, size_t nrhs, const mat_elem_t *A, size_t lda,
+                      const mat_elem_t *X, size_t ldx, mat_elem_t *R, size_t ldr) {
+#ifdef MAT_DOUBLE_PRECISION
+  if (lda < n || ldx < n || ldr < n) return set_error(MATGB_ERR_ARG, "resid64: leading dimension");
+  if (n == 0 || nrhs == 0) return 0;
+  MGB_TRY(resid64_prepare((int64_t)n, A, (int64_t)lda));
+  return resid64((int64_t)n, (int64_t)nrhs, A, X, (int64_t)ldx, R, (int64_t)ldr);
+#else
+  (void)n; (void)nrhs; (void)A; (void)lda; (void)X; (void)ldx; (void)R; (void)ldr;
+  return set_error(MATGB_ERR_ARG, "resid64: double precision only");
+#endif
 }
 
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,

@@ -341,3 +341,57 @@ def test_lp_cholesky_reconstructs(gpu):
         Lf = np.tril(F.astype(np.float64))
         err = np.abs(Lf @ Lf.T - A).max() / np.abs(A).max()
         assert err <= tol, (lp, err)
+
+
+@pytest.mark.parametrize("n", [100, 1030, 2100])
+@pytest.mark.parametrize("nrhs", [1, 7, 64, 65])
+def test_resid64_matches_fp64(gpu, n, nrhs):
+    """R -= A X from FP16 digit slices on the tensor cores agrees with the FP64
+    product within the FP64 GEMM's own error bound (n u |A||X|), with rows
+    and columns of very different scales, a zero row and a zero column."""
+    L = gpu["f64"]
+    rs = np.random.default_rng(900 + n + nrhs)
+    A = rs.standard_normal((n, n)) * 10.0 ** rs.uniform(-6, 6, (n, 1))
+    A[n // 3, :] = 0.0
+    X = rs.standard_normal((n, nrhs)) * 10.0 ** rs.uniform(-6, 6, (1, nrhs))
+    X[:, nrhs // 2] = 0.0
+    B = rs.standard_normal((n, nrhs))
+    A, X, B = (np.asfortranarray(v) for v in (A, X, B))
+    bufs = [L.dalloc(v.nbytes) for v in (A, X, B)]
+    try:
+        for d, v in zip(bufs, (A, X, B)):
+            L.h2d(d, v)
+        L.check(L.c.matgb_resid64_dev(n, nrhs, bufs[0], n, bufs[1], n, bufs[2], n),
+                "resid64")
+        R = np.empty((n, nrhs), np.float64, order="F")
+        L.d2h(R, bufs[2])
+        L.check(L.c.matgb_tc_status(), "tc_status")
+    finally:
+        for d in bufs:
+            L.dfree(d)
+    ref = B - A @ X
+    bound = n * 2.0 ** -53 * (np.abs(A) @ np.abs(X)) + 2.0 ** -52 * np.abs(B)
+    assert np.all(np.abs(R - ref) <= 2 * bound + 1e-300)
+
+
+def test_resid64_propagates_nan(gpu):
+    L = gpu["f64"]
+    n, nrhs = 300, 3
+    rs = np.random.default_rng(7)
+    A = np.asfortranarray(rs.standard_normal((n, n)))
+    A[5, 7] = np.nan
+    X = np.asfortranarray(rs.standard_normal((n, nrhs)))
+    B = np.asfortranarray(np.zeros((n, nrhs)))
+    bufs = [L.dalloc(v.nbytes) for v in (A, X, B)]
+    try:
+        for d, v in zip(bufs, (A, X, B)):
+            L.h2d(d, v)
+        L.check(L.c.matgb_resid64_dev(n, nrhs, bufs[0], n, bufs[1], n, bufs[2], n),
+                "resid64")
+        R = np.empty((n, nrhs), np.float64, order="F")
+        L.d2h(R, bufs[2])
+    finally:
+        for d in bufs:
+            L.dfree(d)
+    assert np.all(np.isnan(R[5]))
+    assert np.all(np.isfinite(np.delete(R, 5, axis=0)))
