@@ -181,9 +181,10 @@ __global__ void rz_accum_kernel(int64_t n, int nr, const float *__restrict__ C,
   if (k >= nr) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    // products of equal weight (l + m = s) summed exactly as integers
-    // (each below 2^24), then one FP64 term per weight
-    long long is[kRzSlices];
+    // products of equal weight (l + m = s) summed exactly as integers (each
+    // below 2^24, at most 8 of them: below 2^27), then one FP64 term per
+    // weight
+    int is[kRzSlices];
 #pragma unroll
     for (int w = 0; w < kRzSlices; w++) is[w] = 0;
     bool nan = false;
@@ -194,12 +195,15 @@ __global__ void rz_accum_kernel(int64_t n, int nr, const float *__restrict__ C,
       for (int m = 0; m + l < kRzSlices; m++) {
         const float c = Cl[i + (int64_t)(m * kRzN + k) * ldc];
         nan = nan || c != c;
-        is[l + m] += (long long)c;
+        is[l + m] += (int)c;
       }
     }
+    // weights 2^(-7(w+2)) are exact doubles: a multiply, not ldexp (FP64
+    // runs at a low rate on this part)
     double acc = 0;
 #pragma unroll
-    for (int w = kRzSlices - 1; w >= 0; w--) acc += ldexp((double)is[w], -kRzBits * (w + 2));
+    for (int w = kRzSlices - 1; w >= 0; w--)
+      acc = fma((double)is[w], __longlong_as_double((long long)(1023 - kRzBits * (w + 2)) << 52), acc);
     if (nan) acc = NAN;
     const int ei = e[i], fk = f[k];
     double v;
@@ -207,8 +211,11 @@ __global__ void rz_accum_kernel(int64_t n, int nr, const float *__restrict__ C,
       v = NAN;
     else if (ei <= kRzNone || fk <= kRzNone)
       v = acc;  // zero: every digit of the row (column) is zero
-    else
-      v = ldexp(acc, ei + fk);
+    else {
+      const int E = ei + fk;  // 2^E exactly, by its bit pattern where normal
+      v = (E >= -1022 && E <= 1023) ? acc * __longlong_as_double((long long)(E + 1023) << 52)
+                                    : ldexp(acc, E);
+    }
     R[i + (int64_t)k * ldr] -= v;
   }
 }
