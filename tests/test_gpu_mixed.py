@@ -395,3 +395,29 @@ def test_resid64_propagates_nan(gpu):
             L.dfree(d)
     assert np.all(np.isnan(R[5]))
     assert np.all(np.isfinite(np.delete(R, 5, axis=0)))
+
+
+@pytest.mark.parametrize("lam,nrhs", [(1e3, 8), (1e6, 70)])
+def test_spd_ir_tensor_core_residual(gpu, lam, nrhs):
+    """From n = 1024 up the multi-RHS refinement forms its FP64 residuals from
+    FP16 digit products on the tensor cores: the solve still reaches the FP64
+    backward-error target (checked here in numpy), and agrees with the same
+    solve whose residuals come from the FP64 GEMM."""
+    L = gpu["f64"]
+    n = 1100
+    A = spd_conditioned(n, lam, 77)
+    B = np.random.default_rng(nrhs).standard_normal((n, nrhs))
+    try:
+        X1, ret1, rep1 = L.mat_solve_spd_ir(A, B, lp_format=2)
+        L.check(L.c.matgb_resid64_mode(0), "resid64_mode")
+        X0, ret0, rep0 = L.mat_solve_spd_ir(A, B, lp_format=2)
+    finally:
+        L.c.matgb_resid64_mode(1)
+    assert ret1 == 0 and rep1["converged"] == 1, rep1
+    assert ret0 == 0 and rep0["converged"] == 1, rep0
+    for c in range(nrhs):
+        x, b = X1[:, c], B[:, c]
+        eta = np.abs(b - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
+                                         + np.abs(b).max())
+        assert eta <= n * 2.0 ** -53, (c, eta)
+    assert np.abs(X1 - X0).max() <= 1e-9 * np.abs(X0).max() * lam
