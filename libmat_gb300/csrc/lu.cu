@@ -228,6 +228,19 @@ __device__ __forceinline__ int first_max_lane(unsigned uk, int idx, int split) {
 // Best (key, index) of cnt <= 32 candidates in shared memory, reduced across
 // the warp (every lane gets the result and the winner's slot).  Ties between
 // real candidates cannot happen (their indices are distinct).
+// The best of cnt <= 32 float candidates given as (index << 32 | key bits)
+// words, whose indices increase with the slot.
+__device__ __forceinline__ void pick_first_ki(const unsigned long long *ki, int cnt, float &bk,
+                                              int &bi, int &bw) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long w = lane < cnt ? ki[lane] : 0ull;
+  const float k = lane < cnt ? __uint_as_float((unsigned)w) : -3.f;
+  const int i = lane < cnt ? (int)(unsigned)(w >> 32) : INT_MAX;
+  bw = first_max_lane(ukey(k), i, INT_MAX);
+  bi = __shfl_sync(0xffffffffu, i, bw);
+  bk = __shfl_sync(0xffffffffu, k, bw);
+}
+
 // The same for float candidates whose indices increase with the slot within
 // [.., split) and within [split, ..).
 __device__ __forceinline__ void pick_first(const float *keys, const int *idxs, int cnt,
@@ -292,6 +305,8 @@ struct RegPanelSmem {
   __align__(16) T xval[2][16][kW];
   __align__(8) T xkey[2][16];
   int xidx[2][16];
+  // float: key bits and index in one 8-byte word (one message, not two)
+  __align__(8) unsigned long long xki[2][16];
   __align__(16) T kval[2][kW];
   // exchange barriers by step parity: the arm (with the step's expected
   // bytes from the other CTAs), one arrival per local warp once its share of
@@ -483,7 +498,7 @@ __device__ __forceinline__ void reg_panel_columns(
   // every thread below CS*PER sends one fixed piece to one fixed receiver
   // every column, so its destinations (both parities) are mapped once here.
   constexpr int NV = kW * (int)sizeof(T) / 16;
-  constexpr int PER = 2 * NV + 2;
+  constexpr int PER = 2 * NV + 1;  // float: row, key+index, row kk
   constexpr bool kFixed = sizeof(T) == 4 && NT >= 16 * PER;
   const int sq = tid / PER, se = tid % PER;
   const bool sender = kFixed && sq < CS;
@@ -491,9 +506,8 @@ __device__ __forceinline__ void reg_panel_columns(
   if (sender && sq != c) {
     auto dst_of = [&](int b) -> uint32_t {
       if (se < NV) return xch::mapa(xch::saddr(&sm.xval[b][c][0]), sq) + 16 * se;
-      if (se == NV) return xch::mapa(xch::saddr(&sm.xkey[b][c]), sq);
-      if (se == NV + 1) return xch::mapa(xch::saddr(&sm.xidx[b][c]), sq);
-      return xch::mapa(xch::saddr(&sm.kval[b][0]), sq) + 16 * (se - NV - 2);
+      if (se == NV) return xch::mapa(xch::saddr(&sm.xki[b][c]), sq);
+      return xch::mapa(xch::saddr(&sm.kval[b][0]), sq) + 16 * (se - NV - 1);
     };
     sdst0 = dst_of(0);
     sdst1 = dst_of(1);
@@ -566,18 +580,18 @@ __device__ __forceinline__ void reg_panel_columns(
     // local sender has read its staging row
     const T *srow = ci != INT_MAX ? &sm.wrow[cw][0] : nullptr;
     if constexpr (kFixed) {
-      if (sender && (se < NV + 2 || own_k)) {
+      const unsigned long long kiw =
+          ((unsigned long long)(unsigned)ci << 32) | __float_as_uint((float)ck);
+      if (sender && (se < NV + 1 || own_k)) {
         if (sq == c) {
           if (se < NV) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (srow) v = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(srow) + 16 * se);
             *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.xval[buf][c][0]) + 16 * se) = v;
           } else if (se == NV) {
-            sm.xkey[buf][c] = ck;
-          } else if (se == NV + 1) {
-            sm.xidx[buf][c] = ci;
+            sm.xki[buf][c] = kiw;
           } else {
-            const int o = 16 * (se - NV - 2);
+            const int o = 16 * (se - NV - 1);
             *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(&sm.kval[buf][0]) + o) =
                 *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(&sm.krow[0]) + o);
           }
@@ -591,11 +605,9 @@ __device__ __forceinline__ void reg_panel_columns(
               xch::put16(dst, &z, rbar);
             }
           } else if (se == NV) {
-            xch::put4(dst, __float_as_uint((float)ck), rbar);
-          } else if (se == NV + 1) {
-            xch::put4(dst, (uint32_t)ci, rbar);
+            xch::put8(dst, kiw, rbar);
           } else {
-            xch::put16(dst, reinterpret_cast<const char *>(&sm.krow[0]) + 16 * (se - NV - 2), rbar);
+            xch::put16(dst, reinterpret_cast<const char *>(&sm.krow[0]) + 16 * (se - NV - 1), rbar);
           }
         }
       }
@@ -656,10 +668,15 @@ __device__ __forceinline__ void reg_panel_columns(
     T gk;
     int p, wc;
     // CTA q's candidate lies in [q*rpc, (q+1)*rpc): indices grow with q
-    if constexpr (sizeof(T) == 4)
+    if constexpr (kFixed) {
+      float gkf;
+      pick_first_ki(sm.xki[buf], CS, gkf, p, wc);
+      gk = (T)gkf;
+    } else if constexpr (sizeof(T) == 4) {
       pick_first(sm.xkey[buf], sm.xidx[buf], CS, INT_MAX, gk, p, wc);
-    else
+    } else {
       pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
+    }
     if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
     if (spiv && tid == 0) spiv[kk] = (int32_t)(k0 + p);
     pprev = (int32_t)(k0 + p);
