@@ -115,6 +115,22 @@ class Oracle:
                             p.ctypes.data_as(C.c_void_p))
         return L, U, p.astype(np.int64), int(s)
 
+    def lu(self, A):
+        """Returns (L, U, p, q, swaps) exactly as mat_lu (full pivoting) fills
+        them."""
+        A, pa = self._arr(A)
+        n = A.shape[0]
+        L = np.zeros((n, n), self.dtype, order="F")
+        U = np.zeros((n, n), self.dtype, order="F")
+        p = np.zeros(n, np.uint64)
+        q = np.zeros(n, np.uint64)
+        self._fn("lu").restype = C.c_int
+        s = self._fn("lu")(pa, C.c_size_t(n), L.ctypes.data_as(C.c_void_p),
+                           U.ctypes.data_as(C.c_void_p),
+                           p.ctypes.data_as(C.c_void_p),
+                           q.ctypes.data_as(C.c_void_p))
+        return L, U, p.astype(np.int64), q.astype(np.int64), int(s)
+
     def plu_inplace(self, A):
         """Port only: packed LU, perm, per-step pivot rows and swap count."""
         assert self.kind == "port"

@@ -185,6 +185,71 @@ int orc_plu(const T *A, size_t n, T *L, T *U, size_t *perm) {
   return swaps;
 }
 
+/* mat_lu, mat.h:4476-4574 (the scalar branch, 4502-4555): full pivoting.
+ * Per step the pivot is the first entry, scanning rows i = k.. and within a
+ * row columns j = k.., whose |a| is strictly larger than the best so far
+ * (starting from a_kk); below MAT_DEFAULT_EPSILON the step is skipped.  Whole
+ * rows then whole columns are exchanged (p, q record them), column k is
+ * scaled by 1.0f / a_kk and the trailing block takes the rank-1 update.
+ * L unit-lower and U upper as mat_lu writes them; returns the swap count. */
+int orc_lu(const T *A, size_t n, T *L, T *U, size_t *p, size_t *q) {
+  T *data = (T *)malloc(n * n * sizeof(T));
+  memcpy(data, A, n * n * sizeof(T));
+  for (size_t i = 0; i < n; i++) p[i] = q[i] = i;
+  int swaps = 0;
+  for (size_t k = 0; k + 1 < n; k++) {
+    size_t pr = k, pc = k;
+    T mx = ORC_FABS(data[k * n + k]);
+    for (size_t i = k; i < n; i++)
+      for (size_t j = k; j < n; j++) {
+        const T v = ORC_FABS(data[j * n + i]);
+        if (v > mx) {
+          mx = v;
+          pr = i;
+          pc = j;
+        }
+      }
+    if (mx < ORC_EPS) continue;
+    if (pr != k) {
+      for (size_t j = 0; j < n; j++) {
+        const T t = data[j * n + k];
+        data[j * n + k] = data[j * n + pr];
+        data[j * n + pr] = t;
+      }
+      const size_t t = p[k];
+      p[k] = p[pr];
+      p[pr] = t;
+      swaps++;
+    }
+    if (pc != k) {
+      for (size_t i = 0; i < n; i++) {
+        const T t = data[k * n + i];
+        data[k * n + i] = data[pc * n + i];
+        data[pc * n + i] = t;
+      }
+      const size_t t = q[k];
+      q[k] = q[pc];
+      q[pc] = t;
+      swaps++;
+    }
+    const T inv = ORC_ONE_F / data[k * n + k];
+    for (size_t i = k + 1; i < n; i++) {
+      const T l = data[k * n + i] * inv;
+      data[k * n + i] = l;
+      for (size_t j = k + 1; j < n; j++) data[j * n + i] -= l * data[j * n + k];
+    }
+  }
+  memset(L, 0, n * n * sizeof(T));
+  memset(U, 0, n * n * sizeof(T));
+  for (size_t j = 0; j < n; j++) {
+    L[j * n + j] = 1;
+    for (size_t i = j + 1; i < n; i++) L[j * n + i] = data[j * n + i];
+    for (size_t i = 0; i <= j; i++) U[j * n + i] = data[j * n + i];
+  }
+  free(data);
+  return swaps;
+}
+
 /* Lx = b, non-unit -- mat__solve_tril_scalar, mat.h:4584-4598 */
 void orc_solve_tril(T *x, const T *L, const T *b, size_t n) {
   for (size_t i = 0; i < n; i++) {

@@ -50,6 +50,17 @@ int ref_plu(const mat_elem_t *A, size_t n, mat_elem_t *L, mat_elem_t *U,
   return mat_plu(&a, &l, &u, &p);
 }
 
+int ref_lu(const mat_elem_t *A, size_t n, mat_elem_t *L, mat_elem_t *U,
+           size_t *p, size_t *q) {
+  Mat a = wrap(n, n, A), l = wrap(n, n, L), u = wrap(n, n, U);
+  Perm pp, qq;
+  pp.data = p;
+  pp.size = n;
+  qq.data = q;
+  qq.size = n;
+  return mat_lu(&a, &l, &u, &pp, &qq);
+}
+
 int ref_chol(const mat_elem_t *A, size_t n, mat_elem_t *L) {
   Mat a = wrap(n, n, A), l = wrap(n, n, L);
   return mat_chol(&a, &l);

@@ -10,6 +10,10 @@ Fixtures:
                      with the reference's outputs.
   rand_<prec>.npz -- the reference tests' srand(42) random inputs, regenerated
                      with the same glibc rand() call sequence, plus outputs.
+  lu_<prec>.npz   -- mat_lu (full pivoting): the known-answer matrices of
+                     tests/test_mat_lu.c and test_mat_plu.c's determinant
+                     test, and test_mat_lu.c's random inputs (glibc rand()
+                     from its default seed, values in steps of 0.1).
   c1_<prec>.npz   -- the 256x256 plain config: A ~ U[-1,1] (seed 1000),
                      b ~ N(0,1) (seed 2000); mat_mul(A, A), mat_plu(A),
                      mat_solve(A, b).
@@ -176,6 +180,29 @@ def rand_fixtures(R, dt):
     return out
 
 
+def lu_fixtures(R, dt):
+    out = {}
+    # tests/test_mat_lu.c:7-80 and tests/test_mat_plu.c:125-130
+    kats = {
+        "lu_3x3": rm(3, 3, [2, -1, -2, -4, 6, 3, -4, -2, 8], dt),
+        "lu_4x4": rm(4, 4, [4, 3, 2, 1, 3, 4, 3, 2, 2, 3, 4, 3, 1, 2, 3, 4], dt),
+        "lu_det3": rm(3, 3, [6, 1, 1, 4, -2, 5, 2, 8, 7], dt),
+    }
+    # tests/test_mat_lu.c:82-90, 115-117: no srand, (rand() % 200 - 100) / 10.0f
+    R.srand(1)
+    for n in (10, 50, 100):
+        A = np.zeros((n, n), dt, order="F")
+        for i in range(n):
+            for j in range(n):
+                A[i, j] = dt(dt(R.rand() % 200 - 100) / dt(10.0))
+        kats[f"lu_random{n}"] = A
+    for name, A in kats.items():
+        L, U, p, q, s = R.lu(A)
+        out.update({name + "_A": A, name + "_L": L, name + "_U": U,
+                    name + "_p": p, name + "_q": q, name + "_s": np.int64(s)})
+    return out
+
+
 def c1(R, dt):
     n = 256
     A = rng.uniform(1000, (n, n), -1.0, 1.0, dt)
@@ -195,6 +222,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"rand_{prec}.npz"),
                             **rand_fixtures(R, dt))
         np.savez_compressed(os.path.join(HERE, f"c1_{prec}.npz"), **c1(R, dt))
+        np.savez_compressed(os.path.join(HERE, f"lu_{prec}.npz"), **lu_fixtures(R, dt))
         print(prec, "ok")
 
 

@@ -132,3 +132,55 @@ def test_port_pivot_rules(prec, dt):
     A = np.array([[1, 2, 3], [2, 4, 6], [3, 6, 10]], dt)  # singular minor
     M, p, ipiv, s = O.plu_inplace(A)
     assert list(ipiv) == [2, 2, 2] or ipiv[0] == 2
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_full_pivot_lu_matches_reference_live(prec, dt):
+    """mat_lu (full pivoting, mat.h:4476-4574) bit-exact against the reference
+    compiled in place: the reference tests' matrices, tie-heavy inputs in
+    steps of 0.1 (test_mat_lu.c's generator), Gaussian inputs, a zero matrix
+    (every step below eps) and a NaN entry."""
+    if not available(prec, "ref"):
+        pytest.skip("reference source tree not present")
+    P, R = Oracle(prec, "port"), Oracle(prec, "ref")
+    rs = np.random.default_rng(11)
+    cases = [np.array([[2, -1, -2], [-4, 6, 3], [-4, -2, 8]], dt),
+             np.array([[4, 3, 2, 1], [3, 4, 3, 2], [2, 3, 4, 3], [1, 2, 3, 4]], dt),
+             np.zeros((5, 5), dt), np.ones((1, 1), dt)]
+    for n in (2, 10, 37, 50, 100):
+        cases.append((rs.integers(0, 200, (n, n)) - 100).astype(dt) / dt(10))
+        cases.append(rs.standard_normal((n, n)).astype(dt))
+    nan = rs.standard_normal((6, 6)).astype(dt)
+    nan[3, 2] = np.nan
+    cases.append(nan)
+    for A in cases:
+        a1, a2 = P.lu(A), R.lu(A)
+        for u, v in zip(a1[:4], a2[:4]):
+            assert np.array_equal(u, v, equal_nan=True), A.shape
+        assert a1[4] == a2[4]
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_full_pivot_lu_matches_golden(prec, dt):
+    """The port against the committed mat_lu fixtures (made from the reference
+    compiled in place): test_mat_lu.c's known-answer and random matrices and
+    test_mat_plu.c's determinant matrix.  Also the reference tests' own
+    checks: P A Q = L U within their tolerance and unit-diagonal L."""
+    g = golden(f"lu_{prec}.npz")
+    P = Oracle(prec, "port")
+    names = sorted({k[:-2] for k in g if k.endswith("_A")})
+    assert len(names) == 6
+    for name in names:
+        A = g[name + "_A"]
+        L, U, p, q, s = P.lu(A)
+        assert np.array_equal(L, g[name + "_L"]), name
+        assert np.array_equal(U, g[name + "_U"]), name
+        assert np.array_equal(p, g[name + "_p"]), name
+        assert np.array_equal(q, g[name + "_q"]), name
+        assert s == int(g[name + "_s"]), name
+        n = A.shape[0]
+        PAQ = A.astype(np.float64)[p][:, q]
+        LU = L.astype(np.float64) @ U.astype(np.float64)
+        tol = 1e-3 if prec == "f32" else 1e-9
+        assert np.max(np.abs(PAQ - LU)) <= tol * max(1.0, np.abs(A).max()) * n
+        assert np.all(np.diag(L) == 1)
