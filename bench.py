@@ -531,6 +531,53 @@ def run_spd(mg, n=16384, nrhs=64):
     return {"workload": f"spd_ir_{n}_{nrhs}rhs_f64", **out}
 
 
+def run_lu_full(mg, steps=3, warmup=3):
+    """mat_lu (full pivoting) on the device at n = 512 and 2048 (float) and
+    2048 (double), beside the oracle port of the reference's scalar
+    elimination on one core at n = 512 (float)."""
+    from oracle.loader import Oracle
+    from libmat_gb300 import rng
+    out = {}
+    for prec, n in (("f32", 512), ("f32", 2048), ("f64", 2048)):
+        L = mg.load(prec)
+        c = L.c
+        es = 4 if prec == "f32" else 8
+        nA = n * n * es
+        dA0, dA, dp = L.dalloc(nA), L.dalloc(nA), L.dalloc(8 * n)
+        L.check(c.matgb_fill_normal_dev(dA0, n * n, 3001), "fill")
+        for _ in range(warmup):
+            L.check(c.matgb_memcpy_d2d(dA, dA0, nA), "d2d")
+            L.check(c.matgb_getrf_full_dev(n, dA, n, dp, dp + 4 * n), "getrf_full")
+        tot = 0.0
+        for _ in range(steps):
+            L.check(c.matgb_memcpy_d2d(dA, dA0, nA), "d2d")
+            L.sync()
+            L.check(c.matgb_event_record(0), "ev")
+            L.check(c.matgb_getrf_full_dev(n, dA, n, dp, dp + 4 * n), "getrf_full")
+            L.check(c.matgb_event_record(1), "ev")
+            L.sync()
+            tot += c.matgb_event_elapsed_ms(0, 1)
+        for d in (dA0, dA, dp):
+            L.dfree(d)
+        ms = tot / steps
+        # each step reads and writes its trailing block once; the first
+        # launch only reads the whole matrix
+        byts = es * (n * n + 2 * (n - 1) * n * (2 * n - 1) / 6)
+        out[f"{prec}_n{n}"] = {"ms": ms, "us_per_step": ms * 1e3 / n,
+                               "launches": n + 1,
+                               "algorithmic_GBs": byts / (ms * 1e-3) / 1e9}
+    n = 512
+    A = rng.normal(3001, (n, n), np.float32)
+    O = Oracle("f32", "port")
+    reps, t0 = 0, time.perf_counter()
+    while reps < 3:
+        O.lu(A)
+        reps += 1
+    out["cpu_port_f32_n512_ms"] = (time.perf_counter() - t0) / reps * 1e3
+    out["cpu_cores"] = 1
+    return out
+
+
 def run_batched(mg, count=100000, steps=5, warmup=3):
     L = mg.load("f32")
     rs = np.random.default_rng(1005)
@@ -701,7 +748,7 @@ def main():
                     help="2 FP16 split (3 products), 0 FP16, 1 BF16, -1 FP32")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--only", choices=["plain_f32", "spd", "batched"],
+    ap.add_argument("--only", choices=["plain_f32", "spd", "batched", "lu_full"],
                     help="run one secondary workload alone and print its JSON "
                          "(small cases for profiling)")
     ap.add_argument("--count", type=int, default=100000,
@@ -718,6 +765,8 @@ def main():
             out = run_plain_f32(mg, steps=args.steps, warmup=args.warmup)
         elif args.only == "spd":
             out = run_spd(mg, n=args.n)
+        elif args.only == "lu_full":
+            out = run_lu_full(mg, steps=args.steps, warmup=args.warmup)
         else:
             out = run_batched(mg, count=args.count, steps=args.steps,
                               warmup=args.warmup)
@@ -749,7 +798,7 @@ def main():
     secondary = None
     if not args.no_secondary:
         secondary = {"plain_f32": run_plain_f32(mg), "spd": run_spd(mg),
-                     "batched": run_batched(mg)}
+                     "batched": run_batched(mg), "lu_full": run_lu_full(mg)}
     cpu = None
     if not args.no_cpu:
         v, per = cpu_sample()

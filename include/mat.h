@@ -234,6 +234,15 @@ MATGB_API void mat_syrk_t(Mat *C, const Mat *A, mat_elem_t alpha,
  * A pivot with |value| < MAT_DEFAULT_EPSILON is swapped in but not divided by
  * (mat.h:4235-4236).  Replaces mat_plu, mat.h:776 (4436-4474). */
 MATGB_API int mat_plu(const Mat *A, Mat *L, Mat *U, Perm *p);
+/* P*A*Q = L*U, full pivoting: at step k the first entry (row-major from
+ * (k,k)) of largest |value| in the trailing block is swapped into (k,k) --
+ * rows first, then columns; a step whose largest |value| is below
+ * MAT_DEFAULT_EPSILON is skipped.  L unit lower, U upper, both n x n;
+ * p->data[i] / q->data[i] = source row / column of row / column i.
+ * Returns the number of row plus column swaps; results are bit-identical to
+ * the reference's scalar elimination.  Replaces mat_lu, mat.h:771
+ * (4476-4574). */
+MATGB_API int mat_lu(const Mat *A, Mat *L, Mat *U, Perm *p, Perm *q);
 /* A = L*L^T from the lower triangle of A.  Returns 0, or -1 when a diagonal
  * is <= 0 (L then holds a partial factor).  Replaces mat_chol, mat.h:780
  * (6062-6092). */

@@ -106,6 +106,13 @@ int matgb_syrk_dev(char uplo, char trans, size_t n, size_t k,
  * of row i (mat.h:4227-4229). */
 int matgb_getrf_dev(size_t n, mat_elem_t *A, size_t lda, int32_t *ipiv,
                     int32_t *perm);
+/* In-place full-pivoting elimination with mat_lu's pivot rule (mat.h:
+ * 4476-4574): rowpiv[k] / colpiv[k] (device, n int32) receive the row and
+ * the column swapped into position k at step k (k itself for none, and for
+ * a skipped step).  A holds the unit-lower L below its diagonal and U on and
+ * above it.  n must be below 2^31. */
+int matgb_getrf_full_dev(size_t n, mat_elem_t *A, size_t lda, int32_t *rowpiv,
+                         int32_t *colpiv);
 /* X (n x nrhs) = A^{-1} B from getrf output: X = B[perm] then unit-lower and
  * upper triangular solves (mat_solve's steps, mat.h:4825-4830, for many
  * columns).  B is not modified; X must not alias B. */

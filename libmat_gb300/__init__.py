@@ -116,6 +116,7 @@ class Lib:
             "matgb_syrk_dev": (_I, [C.c_char, C.c_char, _S, _S, E, _P, _S, E,
                                     _P, _S]),
             "matgb_getrf_dev": (_I, [_S, _P, _S, _P, _P]),
+            "matgb_getrf_full_dev": (_I, [_S, _P, _S, _P, _P]),
             "matgb_getrs_dev": (_I, [_S, _S, _P, _S, _P, _P, _S, _P, _S]),
             "matgb_potrf_dev": (_I, [_S, _P, _S, _P]),
             "matgb_potrs_dev": (_I, [_S, _S, _P, _S, _P, _S, _P]),
@@ -131,6 +132,7 @@ class Lib:
             "mat_syrk": (None, [MP, MP, E, E, C.c_char]),
             "mat_syrk_t": (None, [MP, MP, E, E, C.c_char]),
             "mat_plu": (_I, [MP, MP, MP, PP]),
+            "mat_lu": (_I, [MP, MP, MP, PP, PP]),
             "mat_chol": (_I, [MP, MP]),
             "mat_det": (E, [MP]),
             "mat_inv": (None, [MP, MP]),
@@ -250,6 +252,21 @@ class Lib:
                            C.byref(self.mat(U)), C.byref(p))
         self.check(0, "mat_plu")
         return L, U, pd.astype(np.int64), int(s)
+
+    def mat_lu(self, A):
+        """mat_lu (full pivoting): (L, U, p, q, swaps)."""
+        A = self.arr(A)
+        n = A.shape[0]
+        L = np.zeros((n, n), self.dtype, order="F")
+        U = np.zeros((n, n), self.dtype, order="F")
+        pd = np.zeros(n, np.uint64)
+        qd = np.zeros(n, np.uint64)
+        p = PermStruct(pd.ctypes.data, n)
+        q = PermStruct(qd.ctypes.data, n)
+        s = self.c.mat_lu(C.byref(self.mat(A)), C.byref(self.mat(L)),
+                          C.byref(self.mat(U)), C.byref(p), C.byref(q))
+        self.check(0, "mat_lu")
+        return L, U, pd.astype(np.int64), qd.astype(np.int64), int(s)
 
     def mat_chol(self, A):
         A = self.arr(A)

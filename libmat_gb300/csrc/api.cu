@@ -7,6 +7,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <utility>
 #include <vector>
 
 #include "internal.cuh"
@@ -159,6 +160,42 @@ int do_plu(const Mat *A, Mat *L, Mat *U, Perm *p, int *swaps) {
   MGB_TRY(sync());
   for (int64_t i = 0; i < n; i++) p->data[i] = (size_t)hp[n + i];
   *swaps = count_swaps(hp, n);
+  return 0;
+}
+
+// Full pivoting (mat_lu): eliminate on the device, split L and U there, and
+// replay the recorded swaps on the host into p, q and the swap count, in the
+// reference's order (rows, then columns; mat.h:4476-4574).
+int do_lu(const Mat *A, Mat *L, Mat *U, Perm *p, Perm *q, int *swaps) {
+  if (!ctx()) return MATGB_ERR_NO_DEVICE;
+  const int64_t n = A->rows;
+  for (int64_t i = 0; i < n; i++) p->data[i] = q->data[i] = (size_t)i;
+  *swaps = 0;
+  if (n == 0) return 0;
+  WS(W, elem_t, WS_A, n * n);
+  WS(piv, int32_t, WS_PIV, 2 * n);
+  WS(dL, elem_t, WS_L, n * n);
+  WS(dU, elem_t, WS_U, n * n);
+  MGB_TRY(h2d(W, A->data, n * n * ES));
+  MGB_TRY(getrf_full_t<elem_t>(n, W, n, piv, piv + n, kPivotEps));
+  split_lu_kernel<<<grid_elems(n * n), 256, 0, ctx()->stream>>>(n, W, dL, dU);
+  MGB_LAUNCHED("split_lu");
+  std::vector<int32_t> hp(2 * n);
+  MGB_TRY(d2h(L->data, dL, n * n * ES));
+  MGB_TRY(d2h(U->data, dU, n * n * ES));
+  MGB_TRY(d2h(hp.data(), piv, 2 * n * sizeof(int32_t)));
+  MGB_TRY(sync());
+  for (int64_t k = 0; k + 1 < n; k++) {
+    const int64_t pr = hp[k], pc = hp[n + k];
+    if (pr != k) {
+      std::swap(p->data[k], p->data[pr]);
+      ++*swaps;
+    }
+    if (pc != k) {
+      std::swap(q->data[k], q->data[pc]);
+      ++*swaps;
+    }
+  }
   return 0;
 }
 
@@ -360,6 +397,24 @@ int mat_chol(const Mat *A, Mat *L) {  // mat.h:6062-6092
     return -1;
   }
   return ret;
+}
+
+int mat_lu(const Mat *A, Mat *L, Mat *U, Perm *p, Perm *q) {  // mat.h:4476
+  MAT_ASSERT_MAT(A);
+  MAT_ASSERT_MAT(L);
+  MAT_ASSERT_MAT(U);
+  MAT_ASSERT(p != NULL && q != NULL);
+  MAT_ASSERT_SQUARE(A);
+  size_t n = A->rows;
+  MAT_ASSERT(L->rows == n && L->cols == n);
+  MAT_ASSERT(U->rows == n && U->cols == n);
+  MAT_ASSERT(p->size == n && q->size == n);
+  int swaps = 0;
+  if (do_lu(A, L, U, p, q, &swaps)) {
+    fail_void("mat_lu");
+    return -1;
+  }
+  return swaps;
 }
 
 mat_elem_t mat_det(const Mat *A) {  // mat.h:6227-6249

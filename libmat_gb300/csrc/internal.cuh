@@ -127,6 +127,11 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
                        int64_t ke, int64_t c0, int64_t c1, int lp, bool first,
                        unsigned *amax3 = nullptr, bool l21_ready = false,
                        bool u12_ready = false);
+// Full-pivoting elimination (lu_full.cu); rowpiv/colpiv (device, n int32):
+// the row and column swapped into position k at step k.
+template <typename T>
+int getrf_full_t(int64_t n, T *A, int64_t lda, int32_t *rowpiv,
+                 int32_t *colpiv, T eps);
 template <typename T>
 int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
             const int32_t *perm, const T *B, int64_t ldb, T *X, int64_t ldx);

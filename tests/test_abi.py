@@ -33,9 +33,10 @@ def declared_functions():
 def test_headers_declare_the_hot_path():
     names = declared_functions()
     for f in ("mat_mul", "mat_rmul", "mat_gemm", "mat_syrk", "mat_syrk_t",
-              "mat_plu", "mat_chol", "mat_solve", "mat_solve_spd",
+              "mat_plu", "mat_lu", "mat_chol", "mat_solve", "mat_solve_spd",
               "mat_solve_tril", "mat_solve_tril_unit", "mat_solve_triu",
-              "mat_solve_trilt", "matgb_getrf_dev", "matgb_potrf_dev"):
+              "mat_solve_trilt", "matgb_getrf_dev", "matgb_getrf_full_dev",
+              "matgb_potrf_dev"):
         assert f in names, f
 
 

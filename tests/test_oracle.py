@@ -184,3 +184,33 @@ def test_port_full_pivot_lu_matches_golden(prec, dt):
         tol = 1e-3 if prec == "f32" else 1e-9
         assert np.max(np.abs(PAQ - LU)) <= tol * max(1.0, np.abs(A).max()) * n
         assert np.all(np.diag(L) == 1)
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_vectorised_full_pivot_lu_matches_port(prec, dt):
+    """The vectorised restatement used at large sizes by the GPU tests
+    (tests/lu_full_np.py) is bit-identical to the scalar port: tie-heavy,
+    Gaussian, zero (every step skipped), NaN and infinity inputs."""
+    from lu_full_np import lu_full_np, perms
+    P = Oracle(prec, "port")
+    eps = dt(1e-6) if prec == "f32" else 1e-9
+    rs = np.random.default_rng(5)
+    cases = [np.zeros((4, 4), dt), np.ones((1, 1), dt)]
+    for n in (2, 3, 17, 64, 65, 130):
+        cases.append((rs.integers(0, 200, (n, n)) - 100).astype(dt) / dt(10))
+        cases.append(rs.standard_normal((n, n)).astype(dt))
+    odd = rs.standard_normal((9, 9)).astype(dt)
+    odd[0, 0], odd[4, 7], odd[2, 2] = np.nan, np.inf, dt(1e-7)
+    cases.append(odd)
+    odd2 = odd.copy()
+    odd2[0, 0] = 0
+    cases.append(odd2)
+    for A in cases:
+        n = A.shape[0]
+        L, U, p, q, s = P.lu(A)
+        M, rp, cp, s2 = lu_full_np(A, eps)
+        p2, q2 = perms(rp, cp)
+        assert np.array_equal(L, np.tril(M, -1) + np.eye(n, dtype=dt),
+                              equal_nan=True), n
+        assert np.array_equal(U, np.triu(M), equal_nan=True), n
+        assert np.array_equal(p, p2) and np.array_equal(q, q2) and s == s2
