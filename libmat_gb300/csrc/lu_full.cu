@@ -15,7 +15,7 @@
 // is bound by the memory traffic of the trailing block (read and written
 // once per step) and by the chain's per-step latency.
 //
-// GPU form: one launch per step, over the trailing block in 64 x 64 tiles.
+// GPU form: one launch per step, over the trailing block in 64 x 32 tiles.
 // Launch k applies step k's update (the multipliers and pivot row were left
 // in place by launch k-1) and, over the values it has just written, finds
 // each CTA's best candidate for step k+1.  The last CTA to finish (a ticket
@@ -34,10 +34,12 @@
 namespace mgb {
 namespace {
 
-constexpr int kFullTile = 64;      // tile edge (rows and columns)
+constexpr int kFullRows = 64;      // tile rows (one per thread)
+constexpr int kFullTileCols = 32;  // tile columns
 constexpr int kFullThreads = 256;  // 64 rows x 4 column groups
-constexpr int kFullGroups = kFullThreads / kFullTile;  // column groups
-constexpr int kFullCols = kFullTile / kFullGroups;     // columns per thread
+constexpr int kFullGroups = kFullThreads / kFullRows;      // column groups
+constexpr int kFullCols = kFullTileCols / kFullGroups;     // columns per thread
+constexpr int kFullBatch = 4;      // swap entries per thread in flight
 
 // Candidate: magnitude (-1 for NaN / none) and row-major index.
 template <typename T>
@@ -104,25 +106,31 @@ struct FullPivState {
 // Launch for step k (k = -1: search only).  m = n - k - 1 is the order of
 // the trailing block T that this launch updates and then searches.
 template <typename T>
-__global__ void __launch_bounds__(kFullThreads, 2)
+__global__ void __launch_bounds__(kFullThreads, 3)
     lu_full_step_kernel(T *__restrict__ A, int64_t n, int64_t lda, int64_t k,
                         FullPivState *st, T *part_v,
                         unsigned long long *part_r, int32_t *rowpiv,
                         int32_t *colpiv, int32_t *skip, T eps) {
   __shared__ Cand<T> sm[kFullThreads / 32];
   __shared__ unsigned s_last;
+  // Launched as a programmatic dependent of the previous step: wait for it
+  // to complete (its writes visible), then let the next step's CTAs be
+  // scheduled; they wait in turn, on slots this grid no longer needs.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;");
   const int64_t b = k + 1;  // first row and column of T
   const int64_t m = n - b;
   const bool update = k >= 0 && skip[k] == 0;
   const bool search = b + 1 < n;  // step b exists (steps run to n - 2)
-  const int64_t nt = (m + kFullTile - 1) / kFullTile;
-  const int ti = threadIdx.x % kFullTile, tg = threadIdx.x / kFullTile;
+  const int64_t ntr = (m + kFullRows - 1) / kFullRows;
+  const int64_t ntc = (m + kFullTileCols - 1) / kFullTileCols;
+  const int ti = threadIdx.x % kFullRows, tg = threadIdx.x / kFullRows;
 
   T bv = T(-1);
   unsigned long long br = ~0ull;
-  for (int64_t t = blockIdx.x; t < nt * nt; t += gridDim.x) {
-    const int64_t i = b + (t % nt) * kFullTile + ti;
-    const int64_t j0 = b + (t / nt) * kFullTile + tg;
+  for (int64_t t = blockIdx.x; t < ntr * ntc; t += gridDim.x) {
+    const int64_t i = b + (t % ntr) * kFullRows + ti;
+    const int64_t j0 = b + (t / ntr) * kFullTileCols + tg;
     if (i >= n || j0 >= n) continue;
     // columns j0, j0 + 4, ... below n
     const int64_t left = (n - j0 + kFullGroups - 1) / kFullGroups;
@@ -198,25 +206,57 @@ __global__ void __launch_bounds__(kFullThreads, 2)
     st->ticket = 0;
   }
   if (skp) return;
-  if (pr != b)
-    for (int64_t j = threadIdx.x; j < n; j += kFullThreads) {
-      const T x = __ldcg(A + b + j * lda), y = __ldcg(A + pr + j * lda);
-      A[b + j * lda] = y;
-      A[pr + j * lda] = x;
-    }
+
+  // Step b's swaps and scaling in one pass.  Each changed entry becomes
+  // new(i, j) = old(s(i), t(j)) with s = (b pr), t = (b pc), and the column
+  // below the pivot is then multiplied by inv = 1 / new(b, b).  The four
+  // entries of rows {b, pr} x columns {b, pc} are read by every thread
+  // before any store; every other changed entry is read and written by the
+  // same thread, so no other ordering is needed.
+  const T o_bb = __ldcg(A + b + b * lda), o_bc = __ldcg(A + b + pc * lda);
+  const T o_rb = __ldcg(A + pr + b * lda), o_rc = __ldcg(A + pr + pc * lda);
   __syncthreads();
-  __threadfence_block();
-  if (pc != b)
-    for (int64_t i = threadIdx.x; i < n; i += kFullThreads) {
-      const T x = __ldcg(A + i + b * lda), y = __ldcg(A + i + pc * lda);
-      A[i + b * lda] = y;
-      A[i + pc * lda] = x;
+  const T inv = T(1) / o_rc;
+  if (threadIdx.x == 0) {
+    A[b + b * lda] = o_rc;
+    if (pc != b) A[b + pc * lda] = o_rb;
+    if (pr != b) A[pr + b * lda] = mul_rn(o_bc, inv);  // pr > b: scaled
+    if (pr != b && pc != b) A[pr + pc * lda] = o_bb;
+  }
+  for (int64_t base = threadIdx.x; base < n;
+       base += (int64_t)kFullBatch * kFullThreads) {
+    T x[kFullBatch], y[kFullBatch], cb[kFullBatch], cp[kFullBatch];
+    bool rw[kFullBatch], cl[kFullBatch];
+#pragma unroll
+    for (int u = 0; u < kFullBatch; u++) {
+      const int64_t j = base + (int64_t)u * kFullThreads;  // also a row i
+      // rows b and pr, columns other than b and pc
+      rw[u] = pr != b && j < n && j != b && j != pc;
+      // columns b and pc, rows other than b and pr: swap (pc != b) and
+      // scale (rows below b)
+      cl[u] = j < n && j != b && j != pr && (pc != b || j > b);
+      if (rw[u]) {
+        x[u] = __ldcg(A + b + j * lda);
+        y[u] = __ldcg(A + pr + j * lda);
+      }
+      if (cl[u]) {
+        cb[u] = __ldcg(A + j + b * lda);
+        cp[u] = pc != b ? __ldcg(A + j + pc * lda) : cb[u];
+      }
     }
-  __syncthreads();
-  __threadfence_block();
-  const T inv = T(1) / __ldcg(A + b + b * lda);
-  for (int64_t i = b + 1 + threadIdx.x; i < n; i += kFullThreads)
-    A[i + b * lda] = mul_rn(__ldcg(A + i + b * lda), inv);
+#pragma unroll
+    for (int u = 0; u < kFullBatch; u++) {
+      const int64_t j = base + (int64_t)u * kFullThreads;
+      if (rw[u]) {
+        A[b + j * lda] = y[u];
+        A[pr + j * lda] = x[u];
+      }
+      if (cl[u]) {
+        A[j + b * lda] = j > b ? mul_rn(cp[u], inv) : cp[u];
+        if (pc != b) A[j + pc * lda] = cb[u];
+      }
+    }
+  }
 }
 
 }  // namespace
@@ -247,11 +287,22 @@ int getrf_full_t(int64_t n, T *A, int64_t lda, int32_t *rowpiv,
   if (n == 1) return 0;
   for (int64_t k = -1; k + 1 < n; k++) {
     const int64_t m = n - k - 1;
-    const int64_t nt = (m + kFullTile - 1) / kFullTile;
-    const unsigned grid = (unsigned)std::min<int64_t>(nt * nt, gmax);
+    const int64_t tiles = ((m + kFullRows - 1) / kFullRows) *
+                          ((m + kFullTileCols - 1) / kFullTileCols);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, gmax);
     KtScope kt("lu_full_step", 2.0 * m * m, (k >= 0 ? 2.0 : 1.0) * sizeof(T) * m * m);
-    lu_full_step_kernel<T><<<grid, kFullThreads, 0, s>>>(
-        A, n, lda, k, st, part_v, part_r, rowpiv, colpiv, skip, eps);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kFullThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    MGB_CUDA(cudaLaunchKernelEx(&cfg, lu_full_step_kernel<T>, A, n, lda, k, st,
+                                part_v, part_r, rowpiv, colpiv, skip, eps));
     MGB_LAUNCHED("lu_full_step");
   }
   return 0;
