@@ -162,10 +162,9 @@ __global__ void __launch_bounds__(kFullThreads, 3)
       }
   }
   if (!search) return;
-  // every thread's updated entries are visible device-wide before the
-  // ticket, so that the last CTA's swaps read them
-  if (update) __threadfence();
 
+  // The barriers in block_best order every thread's updated entries before
+  // thread 0's device-wide fence and ticket, so the last CTA reads them.
   const Cand<T> best = block_best(bv, br, sm);
   if (threadIdx.x == 0) {
     part_v[blockIdx.x] = best.v;
@@ -270,7 +269,15 @@ int getrf_full_t(int64_t n, T *A, int64_t lda, int32_t *rowpiv,
                  int32_t *colpiv, T eps) {
   if (n <= 0) return 0;
   cudaStream_t s = ctx()->stream;
-  const int64_t gmax = (int64_t)ctx()->sms * 8;
+  // one wave: as many CTAs as are resident at once, striding over the tiles
+  static int per_sm[2] = {0, 0};
+  int &occ = per_sm[sizeof(T) == 8];
+  if (occ == 0) {
+    MGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ, lu_full_step_kernel<T>, kFullThreads, 0));
+    if (occ < 1) occ = 1;
+  }
+  const int64_t gmax = (int64_t)ctx()->sms * occ;
   const size_t part_bytes = (size_t)gmax * (sizeof(T) + 8);
   const size_t scratch = 256 + part_bytes + (size_t)n * 4;
   char *w = (char *)ws(WS_T0, scratch);

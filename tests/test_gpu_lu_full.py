@@ -15,8 +15,8 @@ Cases:
     entries;
   - the vectorised restatement (tests/lu_full_np.py, pinned to the scalar
     oracle on the CPU) at orders the scalar oracle cannot reach in seconds,
-    including n = 2304, where the first steps have more 64 x 64 tiles than
-    CTAs and each CTA covers several;
+    n = 2304 (f32) and 1100 (f64), whose early steps have more 64 x 32
+    tiles than resident CTAs, so that each CTA covers several;
   - matgb_getrf_full_dev with a leading dimension above n.
 """
 import numpy as np
@@ -76,7 +76,7 @@ def test_lu_full_oracle(gpu, prec):
         assert got[4] == ref[4], A.shape
 
 
-@pytest.mark.parametrize("prec,n", [("f32", 2304), ("f64", 700)])
+@pytest.mark.parametrize("prec,n", [("f32", 2304), ("f64", 1100)])
 def test_lu_full_large(gpu, prec, n):
     L_, dt = gpu[prec], DT[prec]
     A = np.random.default_rng(n).standard_normal((n, n)).astype(dt)
