@@ -214,6 +214,13 @@ MATGB_API Mat *mat_rmul(const Mat *a, const Mat *b);
 /* y = alpha*A*x + beta*y.  Replaces mat_gemv, mat.h:597 (2137-2146). */
 MATGB_API void mat_gemv(Vec *y, mat_elem_t alpha, const Mat *A, const Vec *x,
                         mat_elem_t beta);
+/* y = alpha*A^T*x + beta*y: y[j] = beta*y[j] + alpha*dot(A[:,j], x), y read
+ * even when beta = 0.  Replaces mat_gemv_t, mat.h:601 (2224-2248). */
+MATGB_API void mat_gemv_t(Vec *y, mat_elem_t alpha, const Mat *A, const Vec *x,
+                          mat_elem_t beta);
+/* y += alpha*x, each product rounded before the sum: bit-identical to the
+ * reference's scalar loop.  Replaces mat_axpy, mat.h:594 (2009-2015). */
+MATGB_API void mat_axpy(Vec *y, mat_elem_t alpha, const Vec *x);
 /* C = alpha*A*B + beta*C.  Replaces mat_gemm, mat.h:612 (2787-2796).  beta==0
  * does not read C (BLAS convention; the reference's NEON scal does the same,
  * its scalar path multiplies C by 0). */

@@ -135,6 +135,14 @@ int matgb_potrs_dev(size_t n, size_t nrhs, const mat_elem_t *L, size_t lda,
 int matgb_trsm_dev(char uplo, char trans, char diag, size_t n, size_t nrhs,
                    const mat_elem_t *T, size_t ldt, mat_elem_t *B, size_t ldb);
 /* y = alpha*A*x + beta*y (A m x n).  Generalises mat_gemv (mat.h:2137). */
+/* y (n) = beta*y + alpha*A^T x for A m x n (mat_gemv_t, mat.h:2224-2248);
+ * rows are split into chunks, summed in a fixed order, when n is small. */
+int matgb_gemv_t_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
+                     size_t lda, const mat_elem_t *x, mat_elem_t beta,
+                     mat_elem_t *y);
+/* y += alpha*x (mat_axpy, mat.h:2009-2015), bit-identical to the reference. */
+int matgb_axpy_dev(size_t n, mat_elem_t alpha, const mat_elem_t *x,
+                   mat_elem_t *y);
 int matgb_gemv_dev(size_t m, size_t n, mat_elem_t alpha, const mat_elem_t *A,
                    size_t lda, const mat_elem_t *x, mat_elem_t beta,
                    mat_elem_t *y);

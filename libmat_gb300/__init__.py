@@ -123,12 +123,16 @@ class Lib:
             "matgb_trsm_dev": (_I, [C.c_char, C.c_char, C.c_char, _S, _S, _P,
                                     _S, _P, _S]),
             "matgb_gemv_dev": (_I, [_S, _S, E, _P, _S, _P, E, _P]),
+            "matgb_gemv_t_dev": (_I, [_S, _S, E, _P, _S, _P, E, _P]),
+            "matgb_axpy_dev": (_I, [_S, E, _P, _P]),
             "matgb_solve_multi": (None, [MP, MP, MP]),
             "matgb_solve_spd_multi": (_I, [MP, MP, MP]),
             "mat_mul": (None, [MP, MP, MP]),
             "mat_rmul": (MP, [MP, MP]),
             "mat_gemm": (None, [MP, E, MP, MP, E]),
             "mat_gemv": (None, [MP, E, MP, MP, E]),
+            "mat_gemv_t": (None, [MP, E, MP, MP, E]),
+            "mat_axpy": (None, [MP, E, MP]),
             "mat_syrk": (None, [MP, MP, E, E, C.c_char]),
             "mat_syrk_t": (None, [MP, MP, E, E, C.c_char]),
             "mat_plu": (_I, [MP, MP, MP, PP]),
@@ -230,6 +234,23 @@ class Lib:
                         C.byref(self.mat(A)), C.byref(self.mat(x)),
                         self.ct(beta))
         self.check(0, "mat_gemv")
+        return y.reshape(-1)
+
+    def mat_gemv_t(self, y, alpha, A, x, beta):
+        A, x = self.arr(A), self.arr(x)
+        y = np.array(self.arr(y), order="F", copy=True)
+        self.c.mat_gemv_t(C.byref(self.mat(y)), self.ct(alpha),
+                          C.byref(self.mat(A)), C.byref(self.mat(x)),
+                          self.ct(beta))
+        self.check(0, "mat_gemv_t")
+        return y.reshape(-1)
+
+    def mat_axpy(self, y, alpha, x):
+        x = self.arr(x)
+        y = np.array(self.arr(y), order="F", copy=True)
+        self.c.mat_axpy(C.byref(self.mat(y)), self.ct(alpha),
+                        C.byref(self.mat(x)))
+        self.check(0, "mat_axpy")
         return y.reshape(-1)
 
     def mat_syrk(self, Cm, A, alpha, beta, uplo="L", trans=False):

@@ -124,6 +124,32 @@ int do_gemv(Vec *y, elem_t alpha, const Mat *A, const Vec *x, elem_t beta) {
   return sync();
 }
 
+int do_gemv_t(Vec *y, elem_t alpha, const Mat *A, const Vec *x, elem_t beta) {
+  if (!ctx()) return MATGB_ERR_NO_DEVICE;
+  const int64_t m = A->rows, n = A->cols;
+  WS(dA, elem_t, WS_A, m * n);
+  WS(dx, elem_t, WS_B, m);
+  WS(dy, elem_t, WS_C, n);
+  MGB_TRY(h2d(dA, A->data, m * n * ES));
+  MGB_TRY(h2d(dx, x->data, m * ES));
+  MGB_TRY(h2d(dy, y->data, n * ES));  // read even for beta = 0, as mat.h:2235
+  MGB_TRY(gemv_t_t<elem_t>(m, n, alpha, dA, m, dx, beta, dy));
+  MGB_TRY(d2h(y->data, dy, n * ES));
+  return sync();
+}
+
+int do_axpy(Vec *y, elem_t alpha, const Vec *x) {
+  if (!ctx()) return MATGB_ERR_NO_DEVICE;
+  const int64_t n = x->rows;
+  WS(dx, elem_t, WS_B, n);
+  WS(dy, elem_t, WS_C, n);
+  MGB_TRY(h2d(dx, x->data, n * ES));
+  MGB_TRY(h2d(dy, y->data, n * ES));
+  MGB_TRY(axpy_t<elem_t>(n, alpha, dx, dy));
+  MGB_TRY(d2h(y->data, dy, n * ES));
+  return sync();
+}
+
 // Factor a host matrix on the device; leaves the packed LU in WS_A and
 // ipiv|perm in WS_PIV.  Returns the device pointers.
 int factor_lu(const Mat *A, elem_t **W_out, int32_t **piv_out) {
@@ -347,6 +373,23 @@ void mat_gemv(Vec *y, mat_elem_t alpha, const Mat *A, const Vec *x,
   MAT_ASSERT(A->rows == y->rows);
   MAT_ASSERT(A->cols == x->rows);
   if (do_gemv(y, alpha, A, x, beta)) fail_void("mat_gemv");
+}
+
+void mat_gemv_t(Vec *y, mat_elem_t alpha, const Mat *A, const Vec *x,
+                mat_elem_t beta) {  // mat.h:2239-2248
+  MAT_ASSERT_MAT(y);
+  MAT_ASSERT_MAT(A);
+  MAT_ASSERT_MAT(x);
+  MAT_ASSERT(A->cols == y->rows);
+  MAT_ASSERT(A->rows == x->rows);
+  if (do_gemv_t(y, alpha, A, x, beta)) fail_void("mat_gemv_t");
+}
+
+void mat_axpy(Vec *y, mat_elem_t alpha, const Vec *x) {  // mat.h:2009-2015
+  MAT_ASSERT_MAT(y);
+  MAT_ASSERT_MAT(x);
+  MAT_ASSERT(y->rows == x->rows);
+  if (do_axpy(y, alpha, x)) fail_void("mat_axpy");
 }
 
 void mat_syrk(Mat *C, const Mat *A, mat_elem_t alpha, mat_elem_t beta,

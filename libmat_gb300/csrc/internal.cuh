@@ -127,6 +127,12 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
                        int64_t ke, int64_t c0, int64_t c1, int lp, bool first,
                        unsigned *amax3 = nullptr, bool l21_ready = false,
                        bool u12_ready = false);
+// y = beta*y + alpha*A^T x and y += alpha*x (blas_t.cu).
+template <typename T>
+int gemv_t_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda,
+             const T *x, T beta, T *y);
+template <typename T>
+int axpy_t(int64_t n, T alpha, const T *x, T *y);
 // Full-pivoting elimination (lu_full.cu); rowpiv/colpiv (device, n int32):
 // the row and column swapped into position k at step k.
 template <typename T>

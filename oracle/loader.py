@@ -83,6 +83,24 @@ class Oracle:
                          self.ct(beta), C.c_size_t(m), C.c_size_t(n))
         return y
 
+    def gemv_t(self, alpha, A, x, beta, y):
+        """y = beta*y + alpha*A^T x (mat_gemv_t)."""
+        A, pa = self._arr(A)
+        x, px = self._arr(np.asarray(x).reshape(-1))
+        y = np.array(y, dtype=self.dtype, copy=True).reshape(-1)
+        m, n = A.shape
+        self._fn("gemv_t")(y.ctypes.data_as(C.c_void_p), self.ct(alpha), pa,
+                           px, self.ct(beta), C.c_size_t(m), C.c_size_t(n))
+        return y
+
+    def axpy(self, y, alpha, x):
+        """y + alpha*x (mat_axpy)."""
+        x, px = self._arr(np.asarray(x).reshape(-1))
+        y = np.array(y, dtype=self.dtype, copy=True).reshape(-1)
+        self._fn("axpy")(y.ctypes.data_as(C.c_void_p), self.ct(alpha), px,
+                         C.c_size_t(y.size))
+        return y
+
     def syrk(self, Cm, A, alpha, beta, uplo="L"):
         A, pa = self._arr(A)
         Cm = np.array(Cm, dtype=self.dtype, order="F", copy=True)

@@ -380,6 +380,20 @@ void orc_syrk_t(T *C, const T *A, size_t n, size_t k, T alpha, T beta,
 }
 
 /* y = alpha*A*x + beta*y, A m x n -- mat__gemv_scalar, mat.h:2121-2135 */
+/* y[j] = beta*y[j] + alpha*dot(A[:,j], x) -- mat__gemv_t_scalar,
+ * mat.h:2224-2237, the dot in index order as mat__dot_scalar (1003-1010) */
+void orc_gemv_t(T *y, T alpha, const T *A, const T *x, T beta, size_t m,
+                size_t n) {
+  for (size_t j = 0; j < n; j++) {
+    T d = 0;
+    for (size_t i = 0; i < m; i++) d += A[j * m + i] * x[i];
+    y[j] = beta * y[j] + alpha * d;
+  }
+}
+
+/* y += alpha*x -- mat_axpy, mat.h:2009-2015 via mat__axpy_scalar (909-914) */
+void orc_axpy(T *y, T alpha, const T *x, size_t n) { axpy(y, alpha, x, n); }
+
 void orc_gemv(T *y, T alpha, const T *A, const T *x, T beta, size_t m,
               size_t n) {
   scal(y, beta, m);

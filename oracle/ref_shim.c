@@ -107,6 +107,17 @@ void ref_gemv(mat_elem_t *y, mat_elem_t alpha, const mat_elem_t *A,
   mat_gemv(&yv, alpha, &a, &xv, beta);
 }
 
+void ref_gemv_t(mat_elem_t *y, mat_elem_t alpha, const mat_elem_t *A,
+                const mat_elem_t *x, mat_elem_t beta, size_t m, size_t n) {
+  Mat yv = wrap(n, 1, y), a = wrap(m, n, A), xv = wrap(m, 1, x);
+  mat_gemv_t(&yv, alpha, &a, &xv, beta);
+}
+
+void ref_axpy(mat_elem_t *y, mat_elem_t alpha, const mat_elem_t *x, size_t n) {
+  Mat yv = wrap(n, 1, y), xv = wrap(n, 1, x);
+  mat_axpy(&yv, alpha, &xv);
+}
+
 /* glibc rand() stream, so the reference tests' srand(42) fixtures can be
  * regenerated bit-for-bit by the fixture script. */
 void ref_srand(unsigned s) { srand(s); }

@@ -33,6 +33,7 @@ def declared_functions():
 def test_headers_declare_the_hot_path():
     names = declared_functions()
     for f in ("mat_mul", "mat_rmul", "mat_gemm", "mat_syrk", "mat_syrk_t",
+              "mat_gemv", "mat_gemv_t", "mat_axpy",
               "mat_plu", "mat_lu", "mat_chol", "mat_solve", "mat_solve_spd",
               "mat_solve_tril", "mat_solve_tril_unit", "mat_solve_triu",
               "mat_solve_trilt", "matgb_getrf_dev", "matgb_getrf_full_dev",

@@ -214,3 +214,31 @@ def test_vectorised_full_pivot_lu_matches_port(prec, dt):
                               equal_nan=True), n
         assert np.array_equal(U, np.triu(M), equal_nan=True), n
         assert np.array_equal(p, p2) and np.array_equal(q, q2) and s == s2
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_gemv_t_axpy_match_reference_live(prec, dt):
+    """mat_gemv_t (mat.h:2224-2248) and mat_axpy (2009-2015) bit-exact
+    against the reference compiled in place, on ragged shapes, with beta 0,
+    1 and other values, and NaN / infinity entries."""
+    if not available(prec, "ref"):
+        pytest.skip("reference source tree not present")
+    P, R = Oracle(prec, "port"), Oracle(prec, "ref")
+    rs = np.random.default_rng(17)
+    for m, n in ((1, 1), (7, 3), (64, 65), (257, 31), (1000, 9)):
+        A = rs.standard_normal((m, n)).astype(dt)
+        x = rs.standard_normal(m).astype(dt)
+        y = rs.standard_normal(n).astype(dt)
+        for alpha, beta in ((1.0, 0.0), (-0.75, 1.0), (2.5, -0.5)):
+            assert np.array_equal(P.gemv_t(alpha, A, x, beta, y),
+                                  R.gemv_t(alpha, A, x, beta, y))
+        v = rs.standard_normal(m).astype(dt)
+        v[0] = np.nan if m > 1 else v[0]
+        for alpha in (0.0, 1.0, -3.25):
+            assert np.array_equal(P.axpy(v, alpha, x), R.axpy(v, alpha, x),
+                                  equal_nan=True)
+    A = rs.standard_normal((5, 4)).astype(dt)
+    A[2, 1] = np.inf
+    x = rs.standard_normal(5).astype(dt)
+    assert np.array_equal(P.gemv_t(1.0, A, x, 0.0, np.zeros(4, dt)),
+                          R.gemv_t(1.0, A, x, 0.0, np.zeros(4, dt)), equal_nan=True)
