@@ -578,6 +578,51 @@ def run_lu_full(mg, steps=3, warmup=3):
     return out
 
 
+def run_blas_t(mg, steps=5, warmup=3):
+    """mat_gemv_t's device form on a 16384 x 16384 f32 matrix (1.07 GB) and
+    on a 4M x 64 one (row chunks), and AXPY over 2^28 f32 entries: HBM-bound,
+    inputs far larger than L2.  GB/s of algorithmic bytes."""
+    L = mg.load("f32")
+    c = L.c
+    pk, src = peaks()
+    peak = float(pk["hbm_gbs"])
+    out = {"hbm_peak_source": src}
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        L.sync()
+        L.check(c.matgb_event_record(0), "ev")
+        for _ in range(steps):
+            fn()
+        L.check(c.matgb_event_record(1), "ev")
+        L.sync()
+        return c.matgb_event_elapsed_ms(0, 1) / steps
+
+    for m, n in ((16384, 16384), (1 << 22, 64)):
+        dA, dx, dy = L.dalloc(m * n * 4), L.dalloc(m * 4), L.dalloc(n * 4)
+        L.check(c.matgb_fill_normal_dev(dA, m * n, 11), "fill")
+        L.check(c.matgb_fill_normal_dev(dx, m, 12), "fill")
+        L.check(c.matgb_fill_normal_dev(dy, n, 13), "fill")
+        ms = timed(lambda: L.check(c.matgb_gemv_t_dev(m, n, 1.0, dA, m, dx, 0.5,
+                                                      dy), "gemv_t"))
+        gbs = 4 * (m * n + m + 2 * n) / (ms * 1e-3) / 1e9
+        out[f"gemv_t_{m}x{n}"] = {"ms": ms, "GBs": gbs, "hbm_frac": gbs / peak}
+        for d in (dA, dx, dy):
+            L.dfree(d)
+    n = 1 << 28
+    dx, dy = L.dalloc(n * 4), L.dalloc(n * 4)
+    L.check(c.matgb_fill_normal_dev(dx, n, 14), "fill")
+    L.check(c.matgb_fill_normal_dev(dy, n, 15), "fill")
+    ms = timed(lambda: L.check(c.matgb_axpy_dev(n, 1e-3, dx, dy), "axpy"))
+    gbs = 12 * n / (ms * 1e-3) / 1e9
+    out["axpy_2^28"] = {"ms": ms, "GBs": gbs, "hbm_frac": gbs / peak}
+    for d in (dx, dy):
+        L.dfree(d)
+    out["hbm_peak_GBs"] = peak
+    return out
+
+
 def run_batched(mg, count=100000, steps=5, warmup=3):
     L = mg.load("f32")
     rs = np.random.default_rng(1005)
@@ -748,7 +793,7 @@ def main():
                     help="2 FP16 split (3 products), 0 FP16, 1 BF16, -1 FP32")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--only", choices=["plain_f32", "spd", "batched", "lu_full"],
+    ap.add_argument("--only", choices=["plain_f32", "spd", "batched", "lu_full", "blas_t"],
                     help="run one secondary workload alone and print its JSON "
                          "(small cases for profiling)")
     ap.add_argument("--count", type=int, default=100000,
@@ -765,6 +810,8 @@ def main():
             out = run_plain_f32(mg, steps=args.steps, warmup=args.warmup)
         elif args.only == "spd":
             out = run_spd(mg, n=args.n)
+        elif args.only == "blas_t":
+            out = run_blas_t(mg, steps=args.steps, warmup=args.warmup)
         elif args.only == "lu_full":
             out = run_lu_full(mg, steps=args.steps, warmup=args.warmup)
         else:
@@ -798,7 +845,8 @@ def main():
     secondary = None
     if not args.no_secondary:
         secondary = {"plain_f32": run_plain_f32(mg), "spd": run_spd(mg),
-                     "batched": run_batched(mg), "lu_full": run_lu_full(mg)}
+                     "batched": run_batched(mg), "lu_full": run_lu_full(mg),
+                     "blas_t": run_blas_t(mg)}
     cpu = None
     if not args.no_cpu:
         v, per = cpu_sample()
