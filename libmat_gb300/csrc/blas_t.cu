@@ -20,7 +20,7 @@ namespace {
 
 constexpr int kTvWarps = 8;      // warps (columns) per CTA
 constexpr int kTvUnroll = 8;     // loads in flight per thread
-constexpr int64_t kTvChunk = 8192;  // rows per chunk when the rows are split
+constexpr int64_t kTvChunk = 8192;  // fewest rows per chunk when the rows are split
 
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
@@ -54,18 +54,20 @@ __device__ T column_dot(const T *__restrict__ col, const T *__restrict__ x,
 }
 
 // chunks == 1: y[j] = beta*y[j] + alpha*dot.  chunks > 1: part[c*n + j] =
-// the dot over chunk c (blockIdx.y).
+// the dot over rows [c*rpc, (c+1)*rpc) (chunk c = blockIdx.y), where
+// chunks * rpc >= m.
 template <typename T>
 __global__ void __launch_bounds__(kTvWarps * 32)
     gemv_t_kernel(int64_t m, int64_t n, T alpha, const T *__restrict__ A,
                   int64_t lda, const T *__restrict__ x, T beta,
-                  T *__restrict__ y, T *__restrict__ part, int chunks) {
+                  T *__restrict__ y, T *__restrict__ part, int chunks,
+                  int64_t rpc) {
   const int lane = threadIdx.x & 31;
   const int64_t j = (int64_t)blockIdx.x * kTvWarps + (threadIdx.x >> 5);
   if (j >= n) return;
   const int64_t c = blockIdx.y;
-  const int64_t i0 = chunks == 1 ? 0 : c * kTvChunk;
-  const int64_t i1 = chunks == 1 ? m : (i0 + kTvChunk < m ? i0 + kTvChunk : m);
+  const int64_t i0 = chunks == 1 ? 0 : c * rpc;
+  const int64_t i1 = chunks == 1 ? m : (i0 + rpc < m ? i0 + rpc : m);
   const T d = column_dot(A + j * lda, x, i0, i1, lane);
   if (lane != 0) return;
   if (chunks == 1)
@@ -104,10 +106,14 @@ int gemv_t_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda,
   const int64_t cols = (n + kTvWarps - 1) / kTvWarps;
   // split the rows when the columns alone give under ~4 CTAs per SM
   int chunks = 1;
+  int64_t rpc = m;  // rows per chunk
   const int64_t want = (int64_t)ctx()->sms * 4;
-  if (cols < want && m > 2 * kTvChunk)
-    chunks = (int)std::min<int64_t>((m + kTvChunk - 1) / kTvChunk,
-                                    (want + cols - 1) / cols);
+  if (cols < want && m > 2 * kTvChunk) {
+    const int64_t c0 = std::min<int64_t>((m + kTvChunk - 1) / kTvChunk,
+                                         (want + cols - 1) / cols);
+    rpc = ((m + c0 - 1) / c0 + 255) / 256 * 256;
+    chunks = (int)((m + rpc - 1) / rpc);  // every row in exactly one chunk
+  }
   T *part = nullptr;
   if (chunks > 1) {
     part = (T *)ws(WS_K, (size_t)chunks * n * sizeof(T));
@@ -115,7 +121,7 @@ int gemv_t_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda,
   }
   KtScope kt("gemv_t", 2.0 * m * n, (double)sizeof(T) * (m * n + m + 2 * n));
   gemv_t_kernel<T><<<dim3((unsigned)cols, (unsigned)chunks), kTvWarps * 32, 0,
-                     s>>>(m, n, alpha, A, lda, x, beta, y, part, chunks);
+                     s>>>(m, n, alpha, A, lda, x, beta, y, part, chunks, rpc);
   MGB_LAUNCHED("gemv_t");
   if (chunks > 1) {
     gemv_t_reduce_kernel<T><<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024),

@@ -9,7 +9,9 @@ entrywise against the oracle within
 the standard bound for two summation orders of the same dot product.
 Shapes cover one row and one column, ragged sizes around the 32-lane and
 8-column granules, and tall, skinny products whose rows are split into
-8192-row chunks, which a second launch adds in a fixed order.
+chunks, which a second launch adds in a fixed order.  At 700000 x 64 the
+chunk count is capped by the column count, so each chunk spans more than
+the 8192-row minimum.
 """
 import numpy as np
 import pytest
@@ -36,7 +38,7 @@ def test_gemv_t_against_oracle(gpu, prec):
     O = Oracle(prec, "port")
     rs = np.random.default_rng(31)
     shapes = [(1, 1), (1, 9), (33, 1), (31, 8), (257, 65), (1000, 300),
-              (40000, 3), (20000, 17)]
+              (40000, 3), (20000, 17), (700000, 64)]
     for m, n in shapes:
         A = rs.standard_normal((m, n)).astype(dt)
         x = rs.standard_normal(m).astype(dt)
