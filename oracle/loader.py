@@ -93,6 +93,17 @@ class Oracle:
                            px, self.ct(beta), C.c_size_t(m), C.c_size_t(n))
         return y
 
+    def qr(self, A):
+        """(Q, R) exactly as mat_qr fills them (the port: the reference's
+        unblocked path, used by the reference for n < 64)."""
+        A, pa = self._arr(A)
+        m, n = A.shape
+        Q = np.zeros((m, m), self.dtype, order="F")
+        R = np.zeros((m, n), self.dtype, order="F")
+        self._fn("qr")(pa, C.c_size_t(m), C.c_size_t(n),
+                       Q.ctypes.data_as(C.c_void_p), R.ctypes.data_as(C.c_void_p))
+        return Q, R
+
     def axpy(self, y, alpha, x):
         """y + alpha*x (mat_axpy)."""
         x, px = self._arr(np.asarray(x).reshape(-1))

@@ -391,6 +391,64 @@ void orc_gemv_t(T *y, T alpha, const T *A, const T *x, T beta, size_t m,
   }
 }
 
+/* Householder vector of x (n entries): v[0] = 1, H = I - tau v v^T maps x
+ * to beta e1 with beta = -sign(x0) ||x||; tau = 0 and v = 0 when ||x|| is
+ * below eps -- mat_householder, mat.h:3636-3718 (scalar branch). */
+static T householder(T *v, T *tau, const T *x, size_t n) {
+  if (n == 0) {
+    *tau = 0;
+    return 0;
+  }
+  T norm_sq = 0;
+  for (size_t i = 0; i < n; i++) norm_sq += x[i] * x[i];
+  const T norm_x = ORC_SQRT(norm_sq);
+  if (norm_x < ORC_EPS) {
+    *tau = 0;
+    for (size_t i = 0; i < n; i++) v[i] = 0;
+    return 0;
+  }
+  const T x0 = x[0];
+  const T beta = (x0 >= 0) ? -norm_x : norm_x;
+  const T v0 = x0 - beta;
+  const T v0_inv = 1 / v0;
+  v[0] = 1;
+  for (size_t i = 1; i < n; i++) v[i] = x[i] * v0_inv;
+  *tau = -v0 / beta;
+  return beta;
+}
+
+/* A (m x n, m >= n) = Q (m x m) R (m x n) by Householder reflections, one
+ * column at a time: the reference's unblocked path (n < 64), mat.h:
+ * 4016-4060.  R's entries below the diagonal are what the reflections leave
+ * there (not set to zero), as in the reference. */
+void orc_qr(const T *A, size_t m, size_t n, T *Q, T *R) {
+  memcpy(R, A, m * n * sizeof(T));
+  memset(Q, 0, m * m * sizeof(T));
+  for (size_t i = 0; i < m; i++) Q[i * m + i] = 1;
+  T *x = (T *)malloc((m + 1) * sizeof(T));
+  T *v = (T *)malloc((m + 1) * sizeof(T));
+  T *u = (T *)malloc((m + 1) * sizeof(T));
+  for (size_t j = 0; j < n; j++) {
+    const size_t len = m - j;
+    memcpy(x, &R[j * m + j], len * sizeof(T));
+    T tau;
+    (void)householder(v, &tau, x, len);
+    if (tau == 0) continue;
+    for (size_t k = j; k < n; k++) {
+      T *Rk = &R[k * m + j];
+      const T w = tau * dot(v, Rk, len);
+      axpy(Rk, -w, v, len);
+    }
+    memset(u, 0, m * sizeof(T));
+    for (size_t jj = 0; jj < len; jj++) axpy(u, v[jj], &Q[(j + jj) * m], m);
+    for (size_t jj = 0; jj < len; jj++)
+      axpy(&Q[(j + jj) * m], -tau * v[jj], u, m);
+  }
+  free(x);
+  free(v);
+  free(u);
+}
+
 /* y += alpha*x -- mat_axpy, mat.h:2009-2015 via mat__axpy_scalar (909-914) */
 void orc_axpy(T *y, T alpha, const T *x, size_t n) { axpy(y, alpha, x, n); }
 

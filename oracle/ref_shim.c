@@ -118,6 +118,12 @@ void ref_axpy(mat_elem_t *y, mat_elem_t alpha, const mat_elem_t *x, size_t n) {
   mat_axpy(&yv, alpha, &xv);
 }
 
+void ref_qr(const mat_elem_t *A, size_t m, size_t n, mat_elem_t *Q,
+            mat_elem_t *R) {
+  Mat a = wrap(m, n, A), q = wrap(m, m, Q), r = wrap(m, n, R);
+  mat_qr(&a, &q, &r);
+}
+
 /* glibc rand() stream, so the reference tests' srand(42) fixtures can be
  * regenerated bit-for-bit by the fixture script. */
 void ref_srand(unsigned s) { srand(s); }

@@ -242,3 +242,39 @@ def test_port_gemv_t_axpy_match_reference_live(prec, dt):
     x = rs.standard_normal(5).astype(dt)
     assert np.array_equal(P.gemv_t(1.0, A, x, 0.0, np.zeros(4, dt)),
                           R.gemv_t(1.0, A, x, 0.0, np.zeros(4, dt)), equal_nan=True)
+
+
+@pytest.mark.parametrize("prec,dt", PRECS)
+def test_port_qr_matches_reference_live(prec, dt):
+    """mat_qr (mat.h:3907-4064): the port restates the reference's unblocked
+    path, which the reference itself takes below 64 columns -- identical
+    there; from 64 columns the reference applies 16-column WY blocks, and the
+    two agree within 64 * n * u of max|.| (summation order only).  Also
+    test_mat_qr.c's checks on its matrices: Q orthogonal, R upper
+    triangular within m * eps, Q R = A."""
+    if not available(prec, "ref"):
+        pytest.skip("reference source tree not present")
+    P, R_ = Oracle(prec, "port"), Oracle(prec, "ref")
+    rs = np.random.default_rng(23)
+    u = np.finfo(dt).eps
+    kats = [np.array([[12, -51, 4], [6, 167, -68], [-4, 24, -41]], dt),
+            np.arange(1, 13, dtype=dt).reshape(4, 3), np.eye(3, dtype=dt),
+            np.zeros((4, 2), dt)]
+    for A in kats + [rs.standard_normal(s).astype(dt)
+                     for s in ((1, 1), (5, 3), (10, 10), (63, 40), (100, 63))]:
+        q1, r1 = P.qr(A)
+        q2, r2 = R_.qr(A)
+        assert np.array_equal(q1, q2) and np.array_equal(r1, r2), A.shape
+    for s in ((64, 64), (130, 100)):
+        A = rs.standard_normal(s).astype(dt)
+        (q1, r1), (q2, r2) = P.qr(A), R_.qr(A)
+        tol = 64 * s[1] * u
+        assert np.abs(q1 - q2).max() <= tol * np.abs(q2).max(), s
+        assert np.abs(r1 - r2).max() <= tol * np.abs(r2).max(), s
+    eps = 1e-6 if prec == "f32" else 1e-9
+    for A in kats[:3]:
+        Q, R = P.qr(A)
+        m = A.shape[0]
+        assert np.abs(Q.T.astype(np.float64) @ Q - np.eye(m)).max() <= 1e-5
+        assert np.abs(np.tril(R, -1)).max(initial=0) <= m * eps
+        assert np.abs(Q.astype(np.float64) @ R - A).max() <= 1e-4
