@@ -62,9 +62,14 @@ def peaks():
             "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+# directory for the bench's side files (the nvidia-smi clock samples);
+# --log-dir overrides it
+LOG_DIR = [os.environ.get("TMPDIR") or "/tmp"]
+
+
 def out_path(name):
-    d = os.path.join(ROOT, "gpurun_out")
-    return os.path.join(d, name) if os.path.isdir(d) else os.path.join("/tmp", name)
+    os.makedirs(LOG_DIR[0], exist_ok=True)
+    return os.path.join(LOG_DIR[0], name)
 
 
 class Clocks:
@@ -798,7 +803,12 @@ def main():
                          "(small cases for profiling)")
     ap.add_argument("--count", type=int, default=100000,
                     help="systems in the batched workload")
+    ap.add_argument("--log-dir", default=None,
+                    help="where side files (clock samples) are written "
+                         "(default $TMPDIR or /tmp)")
     args = ap.parse_args()
+    if args.log_dir:
+        LOG_DIR[0] = args.log_dir
     if args.impl == "reference":
         return run_reference(args)
     if args.only:

@@ -102,12 +102,14 @@ template <typename T>
 int gemv_t_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda,
              const T *x, T beta, T *y) {
   if (n <= 0) return 0;
-  cudaStream_t s = ctx()->stream;
+  Ctx *cx = ctx();
+  if (!cx) return MATGB_ERR_NO_DEVICE;
+  cudaStream_t s = cx->stream;
   const int64_t cols = (n + kTvWarps - 1) / kTvWarps;
   // split the rows when the columns alone give under ~4 CTAs per SM
   int chunks = 1;
   int64_t rpc = m;  // rows per chunk
-  const int64_t want = (int64_t)ctx()->sms * 4;
+  const int64_t want = (int64_t)cx->sms * 4;
   if (cols < want && m > 2 * kTvChunk) {
     const int64_t c0 = std::min<int64_t>((m + kTvChunk - 1) / kTvChunk,
                                          (want + cols - 1) / cols);
@@ -134,10 +136,12 @@ int gemv_t_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda,
 template <typename T>
 int axpy_t(int64_t n, T alpha, const T *x, T *y) {
   if (n <= 0) return 0;
+  Ctx *cx = ctx();
+  if (!cx) return MATGB_ERR_NO_DEVICE;
   const unsigned grid =
-      (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)ctx()->sms * 16);
+      (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)cx->sms * 16);
   KtScope kt("axpy", 2.0 * n, 3.0 * sizeof(T) * n);
-  axpy_kernel<T><<<grid, 256, 0, ctx()->stream>>>(n, alpha, x, y);
+  axpy_kernel<T><<<grid, 256, 0, cx->stream>>>(n, alpha, x, y);
   MGB_LAUNCHED("axpy");
   return 0;
 }

@@ -479,8 +479,9 @@ struct MapSink {
 template <typename T, int R, int NT>
 __device__ __forceinline__ void reg_panel_columns(
     T (&a)[R][kW], const int (&prow)[R], RegPanelSmem<T, NT> &sm,
-    cg::cluster_group &cluster, int c, int CS, int rbase, int rpc, int64_t k0,
-    int32_t *__restrict__ ipiv, int32_t *spiv, T eps, int &step, int nsteps,
+    cg::cluster_group &cluster, int c, int CS, int rbase, int rpc, int mrows,
+    int64_t k0, int32_t *__restrict__ ipiv, int32_t *spiv, T eps, int &step,
+    int nsteps,
     const MapSink *maps = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = NT / 32;
@@ -664,7 +665,8 @@ __device__ __forceinline__ void reg_panel_columns(
     __syncwarp();
     if (lane == 0) xch::arrive(&sm.xbar[buf]);
     if (mapper && kk > 0) map_pivot(kk - 1);
-    if (!xch::wait(&sm.xbar[buf], (uint32_t)(step >> 1) & 1u)) g_lu_wait_err = 1;
+    const bool got = xch::wait(&sm.xbar[buf], (uint32_t)(step >> 1) & 1u);
+    if (!got) g_lu_wait_err = 1;
     T gk;
     int p, wc;
     // CTA q's candidate lies in [q*rpc, (q+1)*rpc): indices grow with q
@@ -676,6 +678,15 @@ __device__ __forceinline__ void reg_panel_columns(
       pick_first(sm.xkey[buf], sm.xidx[buf], CS, INT_MAX, gk, p, wc);
     } else {
       pick_best<T>(sm.xkey[buf], sm.xidx[buf], CS, gk, p, wc);
+    }
+    // A wait that gave up leaves the exchange slots stale (or never written):
+    // take no pivot from them.  The step then keeps row kk in place and
+    // eliminates nothing, so every index written below stays in [k0, n) and
+    // the kernels queued behind this one see a valid (if meaningless) swap
+    // sequence; the host reports MATGB_ERR_TIMEOUT after its next sync.
+    if (!got || p < kk || p >= mrows) {
+      p = kk;
+      wc = c;
     }
     if (c == 0 && tid == 0) ipiv[k0 + kk] = (int32_t)(k0 + p);
     if (spiv && tid == 0) spiv[kk] = (int32_t)(k0 + p);
@@ -695,7 +706,7 @@ __device__ __forceinline__ void reg_panel_columns(
       }
     }
     const T piv = u[0];
-    const bool elim = !(fabs(piv) < eps);
+    const bool elim = got && !(fabs(piv) < eps);
     const T inv = elim ? T(1) / piv : T(0);
     const int live = kW - 1 - kk;  // columns right of kk
     T uj[kW];
@@ -736,7 +747,7 @@ __global__ void __launch_bounds__(NT, 1)
   }
   xch_setup<T, NT>(sm, cluster, CS, c, 0, 1 / rpc);
   int step = 0;
-  reg_panel_columns<T, R, NT>(a, prow, sm, cluster, c, CS, rbase, rpc, k0,
+  reg_panel_columns<T, R, NT>(a, prow, sm, cluster, c, CS, rbase, rpc, m, k0,
                               ipiv, nullptr, eps, step, kW);
 #pragma unroll
   for (int r = 0; r < R; r++)
@@ -774,7 +785,7 @@ __device__ void build_swap_map(SwapMap &sm, const int32_t *__restrict__ ipiv,
   for (int i = 0; i < nk; i++) {
     const int32_t k = (int32_t)(k1 + i);
     const int32_t p = sm.piv[i];
-    if (p == k) continue;
+    if (p <= k) continue;  // p < k: never written by a factorisation; no swap
     int slot;
     if (p < k2) {
       slot = p - (int32_t)k1;
@@ -823,7 +834,10 @@ __device__ __forceinline__ void swap_map_reset(SwapMap &map, int64_t k0, int nk)
 __device__ __forceinline__ void swap_map_step(SwapMap &map, int64_t k0, int nk, int i,
                                               int32_t P) {
   const int lane = threadIdx.x & 31;
-  if (P == (int32_t)(k0 + i)) return;
+  // P < k0 + i never comes from a completed exchange (the pick is over rows
+  // at or below the step); it is treated as no swap rather than indexing
+  // the map with a negative slot
+  if (P <= (int32_t)(k0 + i)) return;
   int slot;
   if (P < (int32_t)(k0 + nk)) {
     slot = P - (int32_t)k0;
@@ -1163,7 +1177,7 @@ __global__ void __launch_bounds__(NT, 1)
       for (int j = 0; j < kW; j++)
         a[r][j] = prow[r] >= 0 ? __ldcg(&A[(k0 + prow[r]) + (k0 + j) * lda]) : T(0);
     }
-    reg_panel_columns<T, R, NT>(a, prow, sm.ps, cluster, c, CS, rbase, rpc, k0,
+    reg_panel_columns<T, R, NT>(a, prow, sm.ps, cluster, c, CS, rbase, rpc, m, k0,
                                 ipiv, sm.spiv, eps, step, np * kW, &sink);
 #pragma unroll
     for (int r = 0; r < R; r++)

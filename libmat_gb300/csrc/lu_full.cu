@@ -268,16 +268,17 @@ template <typename T>
 int getrf_full_t(int64_t n, T *A, int64_t lda, int32_t *rowpiv,
                  int32_t *colpiv, T eps) {
   if (n <= 0) return 0;
-  cudaStream_t s = ctx()->stream;
-  // one wave: as many CTAs as are resident at once, striding over the tiles
-  static int per_sm[2] = {0, 0};
-  int &occ = per_sm[sizeof(T) == 8];
-  if (occ == 0) {
-    MGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &occ, lu_full_step_kernel<T>, kFullThreads, 0));
-    if (occ < 1) occ = 1;
-  }
-  const int64_t gmax = (int64_t)ctx()->sms * occ;
+  Ctx *cx = ctx();
+  if (!cx) return MATGB_ERR_NO_DEVICE;
+  cudaStream_t s = cx->stream;
+  // one wave: as many CTAs as are resident at once on the current device,
+  // striding over the tiles (queried per call: a cheap host query, and the
+  // answer belongs to the device that is current now)
+  int occ = 0;
+  MGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &occ, lu_full_step_kernel<T>, kFullThreads, 0));
+  if (occ < 1) occ = 1;
+  const int64_t gmax = (int64_t)cx->sms * occ;
   const size_t part_bytes = (size_t)gmax * (sizeof(T) + 8);
   const size_t scratch = 256 + part_bytes + (size_t)n * 4;
   char *w = (char *)ws(WS_T0, scratch);

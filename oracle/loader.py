@@ -18,12 +18,26 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
+# Where the reference source tree (mat.h and its tests/) is read from when it
+# exists on this host: $LIBMAT_REF_DIR, else the checker's default location.
+# On hosts without it (the GPU machines) every reference-backed check skips.
+REF_ENV = "LIBMAT_REF_DIR"
+_REF_DEFAULT = "/root/reference"
 
-def build(ref_dir=None):
-    """Run oracle/Makefile (the port always; the reference shim if present)."""
+
+def ref_dir():
+    """The reference source tree, or None when it is not present here."""
+    d = os.environ.get(REF_ENV) or _REF_DEFAULT
+    return d if os.path.isfile(os.path.join(d, "mat.h")) else None
+
+
+def build(ref=None):
+    """Run oracle/Makefile: the port always, the reference shim when a
+    reference tree is given (or found by ref_dir())."""
+    ref = ref or ref_dir()
     cmd = ["make", "-s", "-C", HERE]
-    if ref_dir:
-        cmd.append("REF_DIR=" + ref_dir)
+    if ref:
+        cmd.append("REF_DIR=" + ref)
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
 
 

@@ -214,8 +214,11 @@ def c1(R, dt):
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    loader.build(ref_dir)
+    ref = sys.argv[1] if len(sys.argv) > 1 else loader.ref_dir()
+    if not ref:
+        raise SystemExit("reference source tree not found: pass it as the "
+                         f"first argument or set ${loader.REF_ENV}")
+    loader.build(ref)
     for prec, dt in (("f32", np.float32), ("f64", np.float64)):
         R = loader.Oracle(prec, "ref")
         np.savez_compressed(os.path.join(HERE, f"kat_{prec}.npz"), **kat(R, dt))

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
+from oracle import loader
 
 INCLUDE = os.path.join(ROOT, "include")
 
@@ -107,10 +108,12 @@ def test_headers_compile_as_c_and_cpp(tmp_path):
 
 
 REF_TESTS = ["test_mat_solve.c", "test_mat_chol.c", "test_mat_solve_spd.c",
-             "test_mat_solve_tri.c", "test_mat_mul.c"]
+             "test_mat_solve_tri.c", "test_mat_mul.c", "test_mat_plu.c"]
+_REF = loader.ref_dir()
+_REF_TESTS_DIR = os.path.join(_REF, "tests") if _REF else None
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/tests"),
+@pytest.mark.skipif(not (_REF_TESTS_DIR and os.path.isdir(_REF_TESTS_DIR)),
                     reason="reference source tree not present on this host")
 @pytest.mark.parametrize("name", REF_TESTS)
 def test_reference_unit_tests_link_against_libmatgb(libs, tmp_path, name):
@@ -120,8 +123,8 @@ def test_reference_unit_tests_link_against_libmatgb(libs, tmp_path, name):
     import libmat_gb300 as mg
     out = tmp_path / name.replace(".c", "")
     r = subprocess.run(
-        ["gcc", "-std=gnu99", "-I", INCLUDE, "-I", "/root/reference/tests",
-         os.path.join("/root/reference/tests", name), "-o", str(out),
+        ["gcc", "-std=gnu99", "-I", INCLUDE, "-I", _REF_TESTS_DIR,
+         os.path.join(_REF_TESTS_DIR, name), "-o", str(out),
          os.path.join(mg.LIBDIR, "libmatgb_f32.so"), "-lm",
          "-Wl,-rpath," + mg.LIBDIR], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

@@ -62,3 +62,41 @@ def test_noalloc_gemv_rejects_rows_beyond_scratch(gpu, prec):
     msg = L.c.matgb_last_error().decode()
     L.c.matgb_clear_error()
     assert "static scratch" in msg
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("which", ["caller", "null"])
+def test_noalloc_gemv_on_callers_stream(gpu, prec, which):
+    """The allocation-free GEMV runs on the stream the caller passes -- one it
+    created, or NULL (the legacy default stream) -- and leaves the library
+    stream alone: the caller synchronises its own stream before reading y."""
+    torch = pytest.importorskip("torch")
+    L = gpu[prec]
+    dt = L.dtype
+    m, n = 2500, 1500
+    A = rng.normal(930, (m, n), dt)
+    x = rng.normal(931, (n,), dt)
+    y0 = rng.normal(932, (m,), dt)
+    dA, dx, dy = L.dalloc(A.nbytes), L.dalloc(x.nbytes), L.dalloc(y0.nbytes)
+    s = torch.cuda.Stream() if which == "caller" else None
+    try:
+        L.h2d(dA, A)
+        L.h2d(dx, x)
+        ref = run(L, "ws", m, n, 0.75, dA, dx, 2.0, y0, dy, L.c.matgb_stream())
+        for _ in range(2):
+            L.h2d(dy, y0)
+            L.sync()
+            rc = L.c.matgb_gemv_noalloc_dev(m, n, 0.75, dA, m, dx, 2.0, dy,
+                                            s.cuda_stream if s else None)
+            L.check(rc, "noalloc")
+            if s is not None:
+                s.synchronize()
+            else:
+                torch.cuda.synchronize()
+            got = np.empty(m, dt)
+            L.d2h(got, dy)
+            err = np.abs(got.astype(np.float64) - ref).max() / np.abs(ref).max()
+            assert err <= TOL[prec] * max(1.0, n / 256), err
+    finally:
+        for p in (dA, dx, dy):
+            L.dfree(p)
