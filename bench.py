@@ -254,13 +254,44 @@ def run_headline(args, mg):
         d["ms_refine"] = r["ms_refine"]
     for d in per_kappa.values():
         d["ms"] = float(np.mean(d["ms"]))
-    # independent check of the last solve of each condition number
+    # FP64 oracle solutions: the plain FP64 GPU LU solve of each system
+    # (matgb_getrf_dev + matgb_getrs_dev, pinned to the reference's double
+    # mat_solve by the parity tests); each one timed for the speed-up
+    Aw = torch.empty_like(mats[KAPPAS[0]])
+    piv = torch.empty(2 * n, device="cuda", dtype=torch.int32)
+    small = torch.randn(512, 512, device="cuda", dtype=torch.float64)
+    L.check(L.c.matgb_getrf_dev(512, small.data_ptr(), 512, piv.data_ptr(),
+                                piv.data_ptr() + 4 * n), "getrf warm")
+    del small
+    xref, plain_ms = {}, {}
+    for k in KAPPAS:
+        xp = torch.empty_like(b)
+        Aw.copy_(mats[k])
+        torch.cuda.synchronize()
+        L.sync()
+        L.check(L.c.matgb_event_record(2), "ev")
+        L.check(L.c.matgb_getrf_dev(n, Aw.data_ptr(), n, piv.data_ptr(),
+                                    piv.data_ptr() + 4 * n), "getrf")
+        L.check(L.c.matgb_getrs_dev(n, 1, Aw.data_ptr(), n,
+                                    piv.data_ptr() + 4 * n, b.data_ptr(), n,
+                                    xp.data_ptr(), n), "getrs")
+        L.check(L.c.matgb_event_record(3), "ev")
+        L.sync()
+        plain_ms["%g" % k] = L.c.matgb_event_elapsed_ms(2, 3)
+        xref[k] = xp
+    del Aw
+    # independent check of the last solve of each condition number: backward
+    # error, and forward error against the FP64 oracle solution
     for k in KAPPAS:
         if "%g" % k not in per_kappa:
             continue
-        solve(k)
+        r = solve(k)
         L.sync()
-        per_kappa["%g" % k]["bwd_err_check"] = bwd_err_T(mats[k], x, b)
+        d = per_kappa["%g" % k]
+        d["bwd_err_check"] = bwd_err_T(mats[k], x, b)
+        d["fwd_err"] = ((x - xref[k]).abs().max() / xref[k].abs().max()).item()
+        d["fwd_err_est"] = r["forward_error_est"]
+        d["plain_fp64_bwd_err"] = bwd_err_T(mats[k], xref[k], b)
     all_ok = all(d["converged"] == 1 and d["bwd_err_max"] <= tol
                  for d in per_kappa.values())
 
@@ -278,30 +309,16 @@ def run_headline(args, mg):
     A = mats[1e4]
     e2e = e2e_mixed(L, mg, A, b, flops, opts, max(3, min(args.steps, 5)))
 
-    # plain FP64 GPU LU + solve of the kappa = 1e4 system (same API family)
-    Aw = torch.empty_like(A)
-    piv = torch.empty(2 * n, device="cuda", dtype=torch.int32)
-    xp = torch.empty_like(b)
-    small = torch.randn(512, 512, device="cuda", dtype=torch.float64)
-    L.check(L.c.matgb_getrf_dev(512, small.data_ptr(), 512, piv.data_ptr(),
-                                piv.data_ptr() + 4 * n), "getrf warm")
-    Aw.copy_(A)
-    torch.cuda.synchronize()
-    L.sync()
-    L.check(L.c.matgb_event_record(2), "ev")
-    L.check(L.c.matgb_getrf_dev(n, Aw.data_ptr(), n, piv.data_ptr(),
-                                piv.data_ptr() + 4 * n), "getrf")
-    L.check(L.c.matgb_getrs_dev(n, 1, Aw.data_ptr(), n, piv.data_ptr() + 4 * n,
-                                b.data_ptr(), n, xp.data_ptr(), n), "getrs")
-    L.check(L.c.matgb_event_record(3), "ev")
-    L.sync()
-    ms_plain = L.c.matgb_event_elapsed_ms(2, 3)
-    plain = {"ms": ms_plain, "tflops": flops / (ms_plain * 1e-3) / 1e12,
-             "bwd_err": bwd_err_T(A, xp, b), "kappa": 1e4,
+    # plain FP64 GPU LU + solve (same API family), timed above per system
+    ms_plain = plain_ms["%g" % 1e4]
+    plain = {"ms": ms_plain, "ms_per_kappa": plain_ms,
+             "tflops": flops / (ms_plain * 1e-3) / 1e12,
+             "bwd_err": per_kappa.get("%g" % 1e4, {}).get("plain_fp64_bwd_err"),
+             "kappa": 1e4,
              "api": "matgb_getrf_dev + matgb_getrs_dev (f64)",
-             "speedup_of_mixed": {kk: ms_plain / d["ms"]
+             "speedup_of_mixed": {kk: plain_ms[kk] / d["ms"]
                                   for kk, d in per_kappa.items()}}
-    del Aw, xp
+    del xref
 
     for k in list(mats):
         del mats[k]
@@ -424,19 +441,37 @@ def e2e_mixed(L, mg, A, b, flops, opts, ke):
 
 
 # ----------------------------------------------------------------- secondary
+def c2_golden():
+    """The reference's outputs on the 8192 plain config (tests/golden), or
+    None when the fixture is absent."""
+    p = os.path.join(ROOT, "tests", "golden", "c2_8192.npz")
+    if not os.path.exists(p):
+        return None
+    with np.load(p) as z:
+        return {k: z[k] for k in z.files}
+
+
 def run_plain_f32(mg, steps=3, warmup=3):
-    """Plain float32 PLU + 16-RHS solve at 8192 and the 8192^3 GEMM."""
+    """Plain float32 PLU + 16-RHS solve at 8192 and the 8192^3 GEMM.  The
+    PLU inputs are the 8192 plain config's (A ~ N(0,1) seed 1002, B seed
+    2002, generated on the host and copied in), so the permutation and the
+    forward error are checked against the reference's own outputs."""
+    from libmat_gb300 import rng
     L = mg.load("f32")
     c = L.c
     n, nrhs, es = 8192, 16, 4
     nA = n * n * es
+    g = c2_golden()
+    Ah = rng.normal(1002, (n, n), np.float32)
+    Bh = rng.normal(2002, (n, nrhs), np.float32)
     dA0 = L.dalloc(nA)
     dAs = [L.dalloc(nA) for _ in range(steps)]
     dB = L.dalloc(n * nrhs * es)
     dX = L.dalloc(n * nrhs * es)
     dpiv = L.dalloc(2 * n * 4)
-    L.check(c.matgb_fill_normal_dev(dA0, n * n, 1001), "fill")
-    L.check(c.matgb_fill_normal_dev(dB, n * nrhs, 2001), "fill")
+    L.h2d(dA0, Ah)
+    L.h2d(dB, Bh)
+    L.sync()
 
     def step(dA):
         L.check(c.matgb_getrf_dev(n, dA, n, dpiv, dpiv + n * 4), "getrf")
@@ -466,6 +501,21 @@ def run_plain_f32(mg, steps=3, warmup=3):
     R = B - A64 @ X
     eta = float((np.abs(R).max(0) / (np.abs(A64).sum(1).max() * np.abs(X).max(0)
                                      + np.abs(B).max(0))).max())
+    piv = np.empty(2 * n, np.int32)
+    L.d2h(piv, dpiv)
+    parity = {"golden": g is not None}
+    if g is not None:
+        xt = g["x_f64"]
+        fe = np.abs(X.astype(np.float64) - xt).max(0) / np.abs(xt).max(0)
+        fe_ref = np.abs(g["x_f32"].astype(np.float64) - xt).max(0) / np.abs(xt).max(0)
+        parity.update({
+            "perm_equals_reference": bool(np.array_equal(piv[n:], g["p_f32"])),
+            "swaps": int(np.sum(piv[:n] != np.arange(n))),
+            "swaps_reference": int(g["s_f32"]),
+            "fwd_err": float(fe.max()),
+            "fwd_err_reference_f32": float(fe_ref.max()),
+            "fwd_err_oracle": "reference double mat_solve of the same system",
+            "kappa_inf_est": float(g["kappa_inf_est"])})
     # GEMM 8192^3 (C = A A, fresh output each time; inputs larger than L2)
     dC = dAs[0]
     for _ in range(warmup):
@@ -482,21 +532,24 @@ def run_plain_f32(mg, steps=3, warmup=3):
     for d in [dA0, dB, dX, dpiv] + dAs:
         L.dfree(d)
     return {"plu_solve_8192_f32": {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12,
-                                   "nrhs": nrhs, "bwd_err_max": eta},
+                                   "nrhs": nrhs, "bwd_err_max": eta, **parity},
             "gemm_8192_f32": {"ms": ms_g, "tflops": 2 * n ** 3 / (ms_g * 1e-3) / 1e12}}
 
 
 def run_spd(mg, n=16384, nrhs=64):
     """SPD solve with 64 right-hand sides: mixed Cholesky (FP16 split
     tensor-core SYRK updates) + refinement for lambda log-uniform in [1,1e3]
-    and [1,1e6], and the plain FP64 Cholesky."""
+    and [1,1e6], and the plain FP64 Cholesky solve of each system, which is
+    also the FP64 oracle of the mixed solutions' forward error."""
     import torch
     L = mg.load("f64")
     mats, B = spd_set(n, (1e3, 1e6), nrhs, 77)
     X = torch.empty_like(B)
     flops = n ** 3 / 3 + 2 * nrhs * 2 * n * n
     out = {}
+    info = torch.zeros(4, device="cuda", dtype=torch.int32)
     for lm, lp in ((1e3, 2), (1e6, 2)):
+        key = "lam_1e%d" % int(round(np.log10(lm)))
         opts = L.ir_opts(lp_format=lp)
         rep = mg.MatIRReport()
         for rnd in range(2):
@@ -509,31 +562,36 @@ def run_spd(mg, n=16384, nrhs=64):
             ms = (time.perf_counter() - t0) * 1e3
         L.check(rc if rc != -1 else 0, "posv_ir")
         r = rep.as_dict()
-        out["lam_1e%d" % int(round(np.log10(lm)))] = {
+        # plain FP64 Cholesky + 64-RHS solve of the same system
+        A = mats[lm]
+        Aw = A.clone()
+        Xp = B.clone()
+        torch.cuda.synchronize()
+        L.sync()
+        t0 = time.perf_counter()
+        L.check(L.c.matgb_potrf_dev(n, Aw.data_ptr(), n, info.data_ptr()), "potrf")
+        L.check(L.c.matgb_potrs_dev(n, nrhs, Aw.data_ptr(), n, Xp.data_ptr(), n,
+                                    info.data_ptr()), "potrs")
+        L.sync()
+        ms_p = (time.perf_counter() - t0) * 1e3
+        # B, X are row-major nrhs x n: row j is right-hand side j
+        fe = ((X - Xp).abs().amax(1) / Xp.abs().amax(1)).max().item()
+        out[key] = {
             "ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "ret": rc,
             "converged": r["converged"], "bwd_err": r["backward_error"],
+            "fwd_err": fe, "fwd_err_est": r["forward_error_est"],
             "lp_format": r["lp_format"], "refinements": r["refinements"],
-            "ms_factor": r["ms_factor"], "ms_refine": r["ms_refine"]}
-    # plain FP64 Cholesky + 64-RHS solve
-    A = mats[1e3]
-    Aw = A.clone()
-    info = torch.zeros(4, device="cuda", dtype=torch.int32)
-    Xp = B.clone()
-    torch.cuda.synchronize()
-    L.sync()
-    t0 = time.perf_counter()
-    L.check(L.c.matgb_potrf_dev(n, Aw.data_ptr(), n, info.data_ptr()), "potrf")
-    L.check(L.c.matgb_potrs_dev(n, nrhs, Aw.data_ptr(), n, Xp.data_ptr(), n,
-                                info.data_ptr()), "potrs")
-    L.sync()
-    ms_p = (time.perf_counter() - t0) * 1e3
-    out["plain_fp64"] = {"ms": ms_p, "tflops": flops / (ms_p * 1e-3) / 1e12}
-    for k in out:
-        if k.startswith("lam"):
-            out[k]["speedup_vs_plain"] = ms_p / out[k]["ms"]
-    del mats, Aw, Xp, X, B
+            "ms_factor": r["ms_factor"], "ms_refine": r["ms_refine"],
+            "plain_fp64_ms": ms_p, "speedup_vs_plain": ms_p / ms}
+        del Aw, Xp
+    out["plain_fp64"] = {"ms": out["lam_1e3"]["plain_fp64_ms"],
+                         "tflops": flops / (out["lam_1e3"]["plain_fp64_ms"] * 1e-3) / 1e12,
+                         "api": "matgb_potrf_dev + matgb_potrs_dev (f64)"}
+    del mats, X, B
     torch.cuda.empty_cache()
-    return {"workload": f"spd_ir_{n}_{nrhs}rhs_f64", **out}
+    return {"workload": f"spd_ir_{n}_{nrhs}rhs_f64",
+            "fwd_err_oracle": "plain FP64 GPU Cholesky solve of the same system",
+            **out}
 
 
 def run_lu_full(mg, steps=3, warmup=3):
@@ -688,7 +746,11 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
     L.d2h(status, st)
     x = np.empty(totv, np.float32)
     L.d2h(x, dx)
-    worst = 0.0
+    # a sample of 100 systems: backward error, and forward error against the
+    # FP64 oracle (the reference's mat_solve / mat_solve_spd in double)
+    from oracle.loader import Oracle
+    O64 = Oracle("f64", "port")
+    worst, worst_fe = 0.0, 0.0
     for s in rs.integers(0, count, 100):
         n = ns[s]
         M = A[offA[s]:offA[s] + n * n].reshape(n, n, order="F").astype(np.float64)
@@ -696,6 +758,8 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
         bs = b[offv[s]:offv[s] + n]
         worst = max(worst, np.abs(M @ xs - bs).max() /
                     (np.abs(M).sum(1).max() * np.abs(xs).max() + np.abs(bs).max()))
+        xt = O64.solve(M, bs) if kinds[s] == 0 else O64.solve_spd(M, bs)[0]
+        worst_fe = max(worst_fe, np.abs(xs - xt).max() / np.abs(xt).max())
     for v in list(d.values()) + [dx, st]:
         L.dfree(v)
     pk, src = peaks()
@@ -715,7 +779,9 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
             "fp32_peak_tflops": fp32_peak,
             "fp32_frac": tfl / fp32_peak if fp32_peak else None,
             "status_nonzero": int((status != 0).sum()),
-            "bwd_err_sample_max": worst,
+            "bwd_err_sample_max": worst, "fwd_err_sample_max": worst_fe,
+            "fwd_err_oracle": "reference mat_solve / mat_solve_spd in double "
+                              "(oracle port), 100 sampled systems",
             "kernels": [{"name": r[0], "ms": round(r[2], 4)} for r in kt]}
 
 

@@ -184,6 +184,12 @@ typedef struct {
   double ms_refine;      /* GPU time of solves, residuals and updates         */
   int refinements;       /* residuals computed in the element type            */
   int krylov_steps;      /* FGMRES steps over all cycles (0: classic)         */
+  double forward_error_est; /* |d|_inf / |x|_inf of the last correction d
+                        applied (largest over the columns): the refinement's
+                        own estimate of the forward error |x - x*|/|x*| of the
+                        iterate before that correction (the final iterate's
+                        error is smaller when refinement converged); the
+                        library has no exact solution to compare with      */
 } MatIRReport;
 
 void matgb_ir_default_opts(MatIROpts *o);

@@ -40,7 +40,7 @@ class MatIRReport(C.Structure):
                 ("a_inf", C.c_double), ("b_inf", C.c_double),
                 ("tol", C.c_double), ("ms_factor", C.c_double),
                 ("ms_refine", C.c_double), ("refinements", C.c_int),
-                ("krylov_steps", C.c_int)]
+                ("krylov_steps", C.c_int), ("forward_error_est", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -346,17 +346,35 @@ __global__ void scale_to_float_kernel(int64_t n, const S *__restrict__ R,
     RF[i + c * n] = (float)((double)R[i + c * ldr] * s);
 }
 
-// X(:,c) += rn_c * D(:,c)
+// max |v| over the block's threads into *out (double bits; NaN wins)
+__device__ __forceinline__ void amax_into(double v, unsigned long long *out) {
+  for (int off = 16; off; off >>= 1) {
+    const double o = __shfl_xor_sync(~0u, v, off);
+    v = (o > v || o != o) ? o : v;
+  }
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(out, (unsigned long long)__double_as_longlong(v));
+}
+
+// X(:,c) += rn_c * D(:,c); dn[c] = max |rn_c * D(:,c)| (the applied
+// correction's size, the refinement's forward-error estimate)
 template <typename S>
 __global__ void update_x_kernel(int64_t n, S *__restrict__ X, int64_t ldx,
                                 const float *__restrict__ D,
-                                const unsigned long long *__restrict__ rn) {
+                                const unsigned long long *__restrict__ rn,
+                                unsigned long long *__restrict__ dn) {
   const int64_t c = blockIdx.y;
   double s = __longlong_as_double((long long)rn[2 * c]);
   if (!(s > 0 && s < INFINITY)) s = 1.0;
+  double md = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    X[i + c * ldx] = (S)((double)X[i + c * ldx] + s * (double)D[i + c * n]);
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = s * (double)D[i + c * n];
+    X[i + c * ldx] = (S)((double)X[i + c * ldx] + d);
+    const double a = fabs(d);
+    md = (a > md || a != a) ? a : md;
+  }
+  amax_into(md, dn + c);
 }
 
 template <typename S>
@@ -368,13 +386,19 @@ __global__ void copy_cols_kernel(int64_t n, int64_t nrhs, const S *__restrict__ 
     R[(e % n) + (e / n) * ldr] = B[(e % n) + (e / n) * ldb];
 }
 
-// X += D (element type)
+// X += D (element type); *dn = max |D|
 template <typename S>
 __global__ void add_vec_kernel(int64_t n, S *__restrict__ X,
-                               const S *__restrict__ D) {
+                               const S *__restrict__ D,
+                               unsigned long long *__restrict__ dn) {
+  double md = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
+       i += (int64_t)gridDim.x * blockDim.x) {
     X[i] = X[i] + D[i];
+    const double a = fabs((double)D[i]);
+    md = (a > md || a != a) ? a : md;
+  }
+  amax_into(md, dn);
 }
 
 // Reduced doubles (stored as bit patterns) to the host.
@@ -421,11 +445,12 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   elem_t *R = (elem_t *)ws(WS_V0, (size_t)n * nrhs * sizeof(elem_t));
   float *RF = (float *)ws(WS_V1, (size_t)2 * n * nrhs * sizeof(float));
   unsigned long long *red = (unsigned long long *)ws(
-      WS_INFO, (size_t)(2 * nrhs + 8) * sizeof(unsigned long long));
+      WS_INFO, (size_t)(3 * nrhs + 8) * sizeof(unsigned long long));
   if (!W || !piv || !R || !RF || !red) return MATGB_ERR_NOMEM;
   float *DF = RF + n * nrhs;
   int32_t *info = piv + 2 * n;
   unsigned long long *rs = red + 8;  // 2 per column
+  unsigned long long *dn = rs + 2 * nrhs;  // 1 per column: last correction
   const dim3 cg(grid_cap(n) < 64 ? grid_cap(n) : 64, (unsigned)nrhs);
   const unsigned gnn = grid_cap(n * nrhs);
 
@@ -436,7 +461,7 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   MGB_CUDA(cudaMemsetAsync(rowsum, 0, (size_t)n * sizeof(double), st));
   col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, B, ldb, B, ldb, rs);
   MGB_LAUNCHED("col_amax");
-  std::vector<double> hv(2 * nrhs + 8);
+  std::vector<double> hv(3 * nrhs + 8);
   double anorm = 0;
   std::vector<double> bn(nrhs);
   const double eps = sizeof(elem_t) == 8 ? 1.1102230246251565e-16
@@ -445,7 +470,7 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   const int maxit = o.max_iter > 0 ? o.max_iter : 100;
 
   int lp = o.lp_format;
-  double eta = INFINITY, rn = 0, xn = 0;
+  double eta = INFINITY, rn = 0, xn = 0, fwd = INFINITY;
   int it = 0, converged = 0, refinements = 0, ksteps = 0;
   const bool use_krylov = o.krylov != 0 && nrhs == 1;
   const int kdim = o.krylov_dim > 0 ? (o.krylov_dim < kKrylovMaxDim ? o.krylov_dim
@@ -527,7 +552,8 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
         it += inner;
         ksteps += inner;
         if (stalled) break;
-        add_vec_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, X, D);
+        MGB_CUDA(cudaMemsetAsync(dn, 0, sizeof(unsigned long long), st));
+        add_vec_kernel<elem_t><<<grid_cap(n), 256, 0, st>>>(n, X, D, dn);
         MGB_LAUNCHED("add_vec");
         refinements++;
         // true residual in the element type
@@ -537,10 +563,11 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
         MGB_CUDA(cudaMemsetAsync(rs, 0, 2 * sizeof(unsigned long long), st));
         col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, V, n, X, ldx, rs);
         MGB_LAUNCHED("col_amax");
-        MGB_TRY(fetch(rs, hv.data(), 2));
+        MGB_TRY(fetch(rs, hv.data(), 3));  // rs[0..1], then dn[0]
         rn = hv[0];
         xn = hv[1];
         xn_known = xn;
+        fwd = xn > 0 ? hv[2] / xn : (hv[2] == 0 ? 0.0 : INFINITY);
         const double den = anorm * xn + bn[0];
         eta = (den > 0) ? rn / den : (rn == 0 ? 0.0 : INFINITY);
         if (rn != rn || den != den) eta = NAN;
@@ -575,7 +602,8 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
       } else {
         MGB_TRY(getrs_t<float>(n, nrhs, W, n, piv + n, RF, n, DF, n));
       }
-      update_x_kernel<elem_t><<<cg, 256, 0, st>>>(n, X, ldx, DF, rs);
+      MGB_CUDA(cudaMemsetAsync(dn, 0, (size_t)nrhs * sizeof(unsigned long long), st));
+      update_x_kernel<elem_t><<<cg, 256, 0, st>>>(n, X, ldx, DF, rs, dn);
       MGB_LAUNCHED("update_x");
       it++;
       refinements++;
@@ -594,12 +622,16 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
       MGB_CUDA(cudaMemsetAsync(rs, 0, (size_t)2 * nrhs * sizeof(unsigned long long), st));
       col_amax2_kernel<elem_t><<<cg, 256, 0, st>>>(n, R, n, X, ldx, rs);
       MGB_LAUNCHED("col_amax");
-      MGB_TRY(fetch(rs, hv.data(), 2 * (int)nrhs));
+      MGB_TRY(fetch(rs, hv.data(), 3 * (int)nrhs));  // rs, then dn
       eta = 0;
       rn = 0;
       xn = 0;
+      fwd = 0;
       for (int64_t c = 0; c < nrhs; c++) {
         const double r = hv[2 * c], xv = hv[2 * c + 1];
+        const double dv = hv[2 * nrhs + c];
+        const double f = xv > 0 ? dv / xv : (dv == 0 ? 0.0 : INFINITY);
+        if (!(f <= fwd)) fwd = f;
         const double den = anorm * xv + bn[c];
         double e = (den > 0) ? r / den : (r == 0 ? 0.0 : INFINITY);
         if (r != r || den != den) e = NAN;
@@ -645,6 +677,7 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
     rep->lp_format = lp;
     rep->refinements = refinements;
     rep->krylov_steps = ksteps;
+    rep->forward_error_est = fwd;
   }
   return 0;
 }

@@ -65,6 +65,13 @@ class Oracle:
         self.ct = C.c_float if prec == "f32" else C.c_double
         self.pre = "orc_" if kind == "port" else "ref_"
 
+    def arch(self):
+        """MAT_ARCH of the reference build ("port" for the restatement)."""
+        if self.kind != "ref":
+            return "port"
+        self.lib.ref_arch.restype = C.c_char_p
+        return self.lib.ref_arch().decode()
+
     def _fn(self, name):
         return getattr(self.lib, self.pre + name)
 

@@ -17,8 +17,19 @@ Fixtures:
   c1_<prec>.npz   -- the 256x256 plain config: A ~ U[-1,1] (seed 1000),
                      b ~ N(0,1) (seed 2000); mat_mul(A, A), mat_plu(A),
                      mat_solve(A, b).
+  c2_8192.npz     -- the 8192 plain config (PLU + 16-RHS solve): A ~ N(0,1)
+                     float32 (seed 1002), B ~ N(0,1) float32 8192 x 16
+                     (seed 2002), both from libmat_gb300.rng.  Holds the
+                     reference's float mat_plu permutation and swap count,
+                     its float solutions (mat_plu once, then per column the
+                     public mat_solve_tril_unit / mat_solve_triu on B[p]) and
+                     its double solutions of the same (exactly widened)
+                     system, plus kappa_inf(A) estimated by LAPACK's dgecon
+                     (scipy).  A itself is not stored: it is regenerated from
+                     the seed.  Takes a few minutes (two scalar
+                     factorisations).  Only with --c2.
 
-Usage: python tests/golden/make_golden.py [reference_dir]
+Usage: python tests/golden/make_golden.py [reference_dir] [--c2]
 """
 import os
 import sys
@@ -213,12 +224,66 @@ def c1(R, dt):
             "s": np.int64(s), "x": R.solve(A, b)}
 
 
+C2_N, C2_NRHS, C2_SEED_A, C2_SEED_B = 8192, 16, 1002, 2002
+
+
+def c2_inputs():
+    """The 8192 plain config's inputs (regenerated the same way by the GPU
+    parity test)."""
+    A = rng.normal(C2_SEED_A, (C2_N, C2_N), np.float32)
+    B = rng.normal(C2_SEED_B, (C2_N, C2_NRHS), np.float32)
+    return A, B
+
+
+def c2():
+    import time
+    import scipy.linalg as sl
+    A, B = c2_inputs()
+    out = {"seed_A": np.int64(C2_SEED_A), "seed_B": np.int64(C2_SEED_B)}
+    for prec, dt in (("f32", np.float32), ("f64", np.float64)):
+        R = loader.Oracle(prec, "ref")
+        Ad = A.astype(dt)
+        t0 = time.time()
+        L, U, p, s = R.plu(Ad)
+        X = np.empty((C2_N, C2_NRHS), dt, order="F")
+        for j in range(C2_NRHS):
+            X[:, j] = R.solve_triu(U, R.solve_tril_unit(L, B[p, j].astype(dt)))
+        print(f"c2 {prec}: plu + {C2_NRHS} solves {time.time() - t0:.0f} s, "
+              f"MAT_ARCH {R.arch()}")
+        out[f"p_{prec}"] = p.astype(np.int32)
+        out[f"s_{prec}"] = np.int64(s)
+        out[f"x_{prec}"] = X
+        del L, U
+    A64 = A.astype(np.float64)
+    lu, piv, info = sl.lapack.dgetrf(A64)
+    anorm = np.abs(A64).sum(1).max()
+    rcond, info2 = sl.lapack.dgecon(lu, anorm, norm="I")
+    out["kappa_inf_est"] = np.float64(1.0 / rcond)
+    out["lapack_perm_matches_ref_f64"] = np.int64(
+        np.array_equal(_perm_from_ipiv(piv), out["p_f64"]))
+    return out
+
+
+def _perm_from_ipiv(ipiv):
+    """LAPACK's row interchanges as mat_plu's permutation (p[i] = source row
+    of row i)."""
+    p = np.arange(len(ipiv))
+    for k, r in enumerate(ipiv):
+        p[[k, r]] = p[[r, k]]
+    return p
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else loader.ref_dir()
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else loader.ref_dir()
     if not ref:
         raise SystemExit("reference source tree not found: pass it as the "
                          f"first argument or set ${loader.REF_ENV}")
     loader.build(ref)
+    if "--c2" in sys.argv:  # the 8192 fixture alone (minutes)
+        np.savez_compressed(os.path.join(HERE, "c2_8192.npz"), **c2())
+        print("c2 ok")
+        return
     for prec, dt in (("f32", np.float32), ("f64", np.float64)):
         R = loader.Oracle(prec, "ref")
         np.savez_compressed(os.path.join(HERE, f"kat_{prec}.npz"), **kat(R, dt))

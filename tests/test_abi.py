@@ -128,3 +128,33 @@ def test_reference_unit_tests_link_against_libmatgb(libs, tmp_path, name):
          os.path.join(mg.LIBDIR, "libmatgb_f32.so"), "-lm",
          "-Wl,-rpath," + mg.LIBDIR], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_report_struct_layout_matches_ctypes(tmp_path):
+    """MatIROpts / MatIRReport: the ctypes mirror has the C header's size and
+    field offsets (a mismatch would corrupt memory on every refinement
+    call)."""
+    import ctypes as C
+    import libmat_gb300 as mg
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    lines = []
+    for st in (mg.MatIROpts, mg.MatIRReport):
+        name = st.__name__
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f, _ in st._fields_:
+            lines.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "matgb.h"\n'
+                   "int main(void){" + "".join(lines) + "return 0;}\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-I", INCLUDE, str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = dict(l.split() for l in subprocess.run(
+        [str(exe)], capture_output=True, text=True, check=True).stdout.split("\n") if l)
+    for st in (mg.MatIROpts, mg.MatIRReport):
+        name = st.__name__
+        assert int(got[name]) == C.sizeof(st), name
+        for f, _ in st._fields_:
+            assert int(got[f"{name}.{f}"]) == getattr(st, f).offset, (name, f)
