@@ -134,6 +134,17 @@ int matgb_potrs_dev(size_t n, size_t nrhs, const mat_elem_t *L, size_t lda,
  * 'N'), mat.h:4580-4803.  Non-unit diagonals are divided by, as there. */
 int matgb_trsm_dev(char uplo, char trans, char diag, size_t n, size_t nrhs,
                    const mat_elem_t *T, size_t ldt, mat_elem_t *B, size_t ldb);
+/* Plain float products and factorisations on the tensor cores: with on = 1
+ * (the default) the float build runs mat_mul / mat_gemm / mat_syrk (and the
+ * *_dev forms) of at least 256 x 256, and the trailing updates of mat_plu /
+ * mat_chol / mat_solve* (and matgb_getrf_dev / matgb_potrf_dev) from order
+ * 1024 up, as FP32-accurate tensor-core products: each operand split into
+ * FP16 hi + remainder under power-of-two row / column scales, three products
+ * accumulated in FP32 (about 22 bits of every operand).  0: the FP32 SIMT
+ * kernels.  -1: query only.  Returns the previous setting.  No effect in
+ * libmatgb_f64.  No counterpart in the reference (its GEMM is the NEON /
+ * scalar mat_gemm, mat.h:2470-2796). */
+int matgb_plain_tensor_core(int on);
 /* y = alpha*A*x + beta*y (A m x n).  Generalises mat_gemv (mat.h:2137). */
 /* y (n) = beta*y + alpha*A^T x for A m x n (mat_gemv_t, mat.h:2224-2248);
  * rows are split into chunks, summed in a fixed order, when n is small. */
@@ -184,12 +195,15 @@ typedef struct {
   double ms_refine;      /* GPU time of solves, residuals and updates         */
   int refinements;       /* residuals computed in the element type            */
   int krylov_steps;      /* FGMRES steps over all cycles (0: classic)         */
-  double forward_error_est; /* |d|_inf / |x|_inf of the last correction d
-                        applied (largest over the columns): the refinement's
-                        own estimate of the forward error |x - x*|/|x*| of the
-                        iterate before that correction (the final iterate's
-                        error is smaller when refinement converged); the
-                        library has no exact solution to compare with      */
+  double forward_error_est; /* the solver's own estimate of the forward
+                        error |x - x*|_inf / |x*|_inf (it has no exact
+                        solution to compare with): one right-hand side
+                        (FGMRES): |M^-1 r|_inf / |x|_inf, the correction the
+                        low-precision factors M give for the final residual
+                        r; many right-hand sides (classic refinement): the
+                        largest |d|_inf / |x|_inf of the last correction d,
+                        an upper estimate (it is the error of the iterate
+                        before that correction)                            */
 } MatIRReport;
 
 void matgb_ir_default_opts(MatIROpts *o);

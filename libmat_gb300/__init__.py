@@ -97,6 +97,7 @@ class Lib:
                                      C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]),
             "matgb_measure_fma_peak": (C.c_double, [_I]),
+            "matgb_plain_tensor_core": (_I, [_I]),
             "matgb_device_alloc": (_P, [_S]),
             "matgb_device_free": (_I, [_P]),
             "matgb_host_alloc": (_P, [_S]),

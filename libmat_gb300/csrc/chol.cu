@@ -311,8 +311,12 @@ template int potrs_t<float>(int64_t, int64_t, const float *, int64_t, float *,
 template int potrs_t<double>(int64_t, int64_t, const double *, int64_t,
                              double *, int64_t, const int32_t *);
 
+// The plain Cholesky (mat_chol, mat_solve_spd, matgb_potrf_dev): float
+// orders from 1024 up take their SYRK updates on the tensor cores in the
+// FP32-accurate split form (lp 2) unless matgb_plain_tensor_core(0).
 int potrf(int64_t n, elem_t *A, int64_t lda, int32_t *info) {
-  return potrf_t<elem_t>(n, A, lda, info, -1);
+  const int lp = (sizeof(elem_t) == 4 && plain_tc_on() && n >= kPlainTcMinN) ? 2 : -1;
+  return potrf_t<elem_t>(n, A, lda, info, lp);
 }
 
 int potrs(int64_t n, int64_t nrhs, const elem_t *L, int64_t lda, elem_t *B,

@@ -1,4 +1,5 @@
 // SIMT GEMM / SYRK / GEMV in the library's element type (float or double).
+// (Large float products go to the tensor cores instead: tc_sgemm.cu.)
 //
 // This is the plain-precision path: mat_gemm / mat_mul, the LU trailing
 // update A22 -= L21*U12 (mat__gemm_strided_, mat.h:2719-2741, called from
@@ -197,9 +198,21 @@ int gemm_skip(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
                              ldc, tri, skip);
 }
 
+// The public products (mat_mul, mat_gemm, mat_syrk, matgb_gemm_dev,
+// matgb_syrk_dev): in the float build, products of at least 256 x 256 run on
+// the tensor cores in the FP32-accurate split form (tc_sgemm.cu) unless
+// matgb_plain_tensor_core(0) chose the SIMT kernel.
 int gemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, elem_t alpha,
          const elem_t *A, int64_t lda, const elem_t *B, int64_t ldb,
          elem_t beta, elem_t *C, int64_t ldc, int tri) {
+#ifndef MAT_DOUBLE_PRECISION
+  if (plain_tc_on() && m >= kPlainTcMinMN && n >= kPlainTcMinMN && k >= 16) {
+    // SYRK (op(B) = op(A)^T): one packed operand serves both sides
+    const bool same_ab = A == B && lda == ldb && ta != tb && m == n;
+    return tc_sgemm(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri,
+                    same_ab);
+  }
+#endif
   return gemm_skip(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri,
                    nullptr);
 }

@@ -51,7 +51,7 @@ struct KtScope {
 enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
   WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_SWM, WS_SWG,
-  WS_RZA, WS_RZB, WS_RZC, WS_RZE,
+  WS_RZA, WS_RZB, WS_RZC, WS_RZE, WS_TCA, WS_TCB, WS_TCS,
   WS_NSLOTS
 };
 void *ws(int slot, size_t bytes);
@@ -145,11 +145,26 @@ int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
 // lower: only tiles on/below the diagonal, elements with col <= row;
 // skip: every CTA returns at once when *skip != 0 (may be null);
 // Alo/Blo (may be null): remainders of A and B for the three-product split.
+// lower: 0 every element, 1 lower triangle, 2 upper triangle (tiles and
+// elements outside it are skipped); rinv/cinv (may be null): per-row and
+// per-column power-of-two factors applied to the product before alpha.
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
             int lower, const int32_t *skip, const void *Alo = nullptr,
-            const void *Blo = nullptr);
+            const void *Blo = nullptr, const float *rinv = nullptr,
+            const float *cinv = nullptr);
+// FP32-accurate float GEMM / SYRK on the tensor cores (tc_sgemm.cu): op(A)
+// and op(B) packed to FP16 hi + remainder under per-row / per-column
+// power-of-two scales, three products per update; tri as tc_gemm's lower.
+int tc_sgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, float alpha,
+             const float *A, int64_t lda, const float *B, int64_t ldb,
+             float beta, float *C, int64_t ldc, int tri, bool same_ab = false);
+// Whether the plain float paths (GEMM, SYRK, LU, Cholesky) use the tensor
+// cores (matgb_plain_tensor_core), and the size from which they do.
+bool plain_tc_on();
+constexpr int64_t kPlainTcMinMN = 256;
+constexpr int64_t kPlainTcMinN = 1024;  // LU / Cholesky order
 // FP64 residual R -= A X (X n x nrhs) on the tensor cores from exact FP16
 // digit products (resid64.cu); resid64_prepare slices A once per solve.
 int resid64_prepare(int64_t n, const double *A, int64_t lda);

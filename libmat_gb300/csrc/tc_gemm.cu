@@ -16,16 +16,18 @@
 //
 // One CTA computes one 128 x 256 tile (UMMA M=128, N=256, K=16, cta_group::1):
 //   warp 8  : TMA producer -- for each 64-wide K block a 128x64 A box and a
-//             256x64 B box (128-byte swizzle) into a 2-stage ring (full /
-//             empty mbarriers);
+//             256x64 B box (128-byte swizzle) into a ring of 2 stages (short
+//             K, two CTAs per SM) or 4 (long K, one CTA per SM) with full /
+//             empty mbarriers;
 //   warp 9  : TMEM allocator and single-thread MMA issuer (4 MMAs per K
 //             block, tcgen05.commit to the stage's empty barrier), then a
 //             final commit to the "accumulator ready" mbarrier;
 //   warps 0-7: epilogue -- tcgen05.ld 16 columns at a time from TMEM (warp w
 //             reads lane quarter w%4, column half w/4), then a coalesced
 //             read-modify-write of C (consecutive lanes = consecutive rows).
-// 96 KB of smem, so two CTAs fit per SM and one CTA's epilogue overlaps the
-// other's loads and MMAs.  Every wait is bounded; on a timeout the CTA records
+// The 2-stage form takes 96 KB of smem, so two CTAs fit per SM and one CTA's
+// epilogue overlaps the other's loads and MMAs; the 4-stage form (192 KB)
+// serves long K sums, where the epilogue is a few percent of a tile.  Every wait is bounded; on a timeout the CTA records
 // an error flag, stops issuing work, waits (bounded) for its copies in
 // flight, still frees its TMEM and returns.
 #include <cudaTypedefs.h>
@@ -36,17 +38,23 @@
 namespace mgb {
 
 constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 64;
-constexpr int kTcStages = 2;
-constexpr int kTcMaxKB = 64;  // K blocks per launch (all segments)
 constexpr int kTcThreads = 320;
 constexpr uint32_t kTcWaitLimit = 1u << 24;  // ~1.5 s of polling
+// K blocks per launch (all segments): bounds one CTA's main loop (3 x 16384
+// columns of K, ~0.3 ms on one SM), far inside the wait limit; longer sums
+// are split by the caller
+constexpr int kTcMaxKB = 3 * 16384 / kTcBK;
 
+// Two ring depths: 2 stages with two CTAs per SM (short K, the LU and
+// Cholesky updates: one CTA's epilogue overlaps the other's main loop), and
+// 4 stages with one CTA per SM (long K, the plain GEMM: deeper prefetch).
+template <int ST>
 struct TcSmem {
   // 1024-byte aligned swizzle atoms
-  uint16_t a[kTcStages][kTcBM * kTcBK];
-  uint16_t b[kTcStages][kTcBN * kTcBK];
-  uint64_t full[kTcStages];
-  uint64_t empty[kTcStages];
+  uint16_t a[ST][kTcBM * kTcBK];
+  uint16_t b[ST][kTcBN * kTcBK];
+  uint64_t full[ST];
+  uint64_t empty[ST];
   uint64_t done;
   uint32_t tmem_base;
   volatile int timeout;
@@ -54,7 +62,12 @@ struct TcSmem {
 
 // Segment s of the K axis (kps K blocks each) reads A from tmA1 when bit s of
 // amask is set (else tmA0), B likewise with bmask.
-__global__ void __launch_bounds__(kTcThreads, 2)
+// tri: 0 every tile; 1 lower (tiles on/below the diagonal, elements with
+// col <= row); 2 upper (col >= row).  rinv / cinv (may be null): per-row and
+// per-column power-of-two factors applied to the accumulator before alpha
+// (the inverses of the operands' packing scales; exact).
+template <int ST, int MINB>
+__global__ void __launch_bounds__(kTcThreads, MINB)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0,
                    const __grid_constant__ CUtensorMap tmA1,
                    const __grid_constant__ CUtensorMap tmB0,
@@ -62,20 +75,22 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                    int kps, int nseg, unsigned amask, unsigned bmask,
                    float alpha, const float *__restrict__ alpha_scale,
                    float beta, float *__restrict__ C, int64_t ldc,
-                   uint32_t idesc, int lower, const int32_t *__restrict__ skip,
-                   int *__restrict__ err) {
+                   uint32_t idesc, int tri, const int32_t *__restrict__ skip,
+                   const float *__restrict__ rinv,
+                   const float *__restrict__ cinv, int *__restrict__ err) {
+  constexpr int kTcStages = ST;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // align the carve-out to 1024 B (the swizzle atom)
-  TcSmem &s = *reinterpret_cast<TcSmem *>(
+  TcSmem<ST> &s = *reinterpret_cast<TcSmem<ST> *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
   const int nkb = kps * nseg;
   // whole-CTA exits before any barrier or TMEM allocation: a failed earlier
-  // step (skip flag) or, for a lower-triangular update, a tile strictly above
-  // the diagonal
+  // step (skip flag) or a tile strictly outside the triangle
   if (skip && *skip != 0) return;
-  if (lower && n0 >= m0 + kTcBM) return;
+  if (tri == 1 && n0 >= m0 + kTcBM) return;
+  if (tri == 2 && m0 >= n0 + kTcBN) return;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < kTcStages; i++) {
@@ -164,6 +179,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     };
     float cur[CH];
     load(cur, 0);
+    const float rs = (rinv && rok) ? __ldg(&rinv[row]) : 1.f;
     const bool ready = tc::mbar_wait(&s.done, 0, kTcWaitLimit);
     tc::tc_fence_after();
     if (ready && !s.timeout) {
@@ -172,6 +188,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       for (int ch = 0; ch < NCH; ch++) {
         float nxt[CH];
         if (ch + 1 < NCH) load(nxt, ch + 1);
+        float cs[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+          const int col = cbase + ch * CH + j;
+          cs[j] = (cinv && col < N) ? __ldg(&cinv[col]) : 1.f;
+        }
         float v[CH];
         tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) +
                           (uint32_t)(half * (kTcBN / 2) + ch * CH),
@@ -180,8 +202,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 #pragma unroll
           for (int j = 0; j < CH; j++) {
             const int col = ch * CH + j;
-            if (cbase + col < N && (!lower || cbase + col <= row))
-              cp[(int64_t)col * ldc] = fmaf(al, v[j], beta * cur[j]);
+            const bool in = tri == 0 || (tri == 1 ? cbase + col <= row
+                                                   : cbase + col >= row);
+            if (cbase + col < N && in)
+              cp[(int64_t)col * ldc] = fmaf(al, (v[j] * rs) * cs[j], beta * cur[j]);
           }
         }
         if (ch + 1 < NCH) {
@@ -207,6 +231,11 @@ static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 static int *g_tc_err = nullptr;
 static bool g_tc_ready = false;
 
+template <int ST, int MINB>
+static constexpr size_t tc_smem_bytes() {
+  return sizeof(TcSmem<ST>) + 1024;
+}
+
 static int tc_setup() {
   if (g_tc_ready) return 0;
   void *fn = nullptr;
@@ -218,9 +247,12 @@ static int tc_setup() {
   g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
   MGB_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
   MGB_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
-  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel,
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<2, 2>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sizeof(TcSmem) + 1024));
+                                (int)tc_smem_bytes<2, 2>()));
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<4, 1>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tc_smem_bytes<4, 1>()));
   g_tc_ready = true;
   return 0;
 }
@@ -248,7 +280,8 @@ static int make_map(CUtensorMap *m, const void *ptr, int bf16, int64_t rows,
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
-            int lower, const int32_t *skip, const void *Alo, const void *Blo) {
+            int lower, const int32_t *skip, const void *Alo, const void *Blo,
+            const float *rinv, const float *cinv) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (M <= 0 || N <= 0) return 0;
@@ -275,12 +308,23 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
   const double frac = lower ? 0.5 : 1.0;
   // segments: [Ah|Ah|Al] . [Bh|Bl|Bh]
   const unsigned amask = split ? 4u : 0u, bmask = split ? 2u : 0u;
-  KtScope kt(split ? "tc_gemm_split" : "tc_gemm", 2.0 * M * N * K * frac * nseg,
+  // long K (the plain GEMM): the deeper ring, one CTA per SM
+  const bool deep = K * nseg > 16 * kTcBK;
+  const char *nm = deep ? (split ? "tc_gemm_split_k" : "tc_gemm_k")
+                        : (split ? "tc_gemm_split" : "tc_gemm");
+  KtScope kt(nm, 2.0 * M * N * K * frac * nseg,
              4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N * frac +
                  2.0 * (M + N) * K * (split ? 2 : 1));
-  tc_gemm_kernel<<<grid, kTcThreads, sizeof(TcSmem) + 1024, cx->stream>>>(
-      ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,
-      alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, g_tc_err);
+  if (deep)
+    tc_gemm_kernel<4, 1><<<grid, kTcThreads, tc_smem_bytes<4, 1>(), cx->stream>>>(
+        ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,
+        alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv,
+        g_tc_err);
+  else
+    tc_gemm_kernel<2, 2><<<grid, kTcThreads, tc_smem_bytes<2, 2>(), cx->stream>>>(
+        ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,
+        alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv,
+        g_tc_err);
   MGB_LAUNCHED("tc_gemm");
   return 0;
 }
