@@ -261,6 +261,16 @@ MATGB_API mat_elem_t mat_det(const Mat *A);
  * Replaces mat_inv, mat.h:789 (6166-6225). */
 MATGB_API void mat_inv(Mat *out, const Mat *A);
 
+/* A (m x n, m >= n) = Q (m x m) * R (m x n) by Householder reflections with
+ * the reference's reflector (beta = -sign(a_jj) |x|, v[0] = 1, no reflection
+ * when |x| < MAT_DEFAULT_EPSILON), blocked in the WY form; R's entries below
+ * the diagonal are the reflections' rounding residue, as in the reference.
+ * Replaces mat_qr, mat.h:744 (3907-4064). */
+MATGB_API void mat_qr(const Mat *A, Mat *Q, Mat *R);
+/* The R factor alone (no Q accumulation).  Replaces mat_qr_r, mat.h:749
+ * (4066-4192). */
+MATGB_API void mat_qr_r(const Mat *A, Mat *R);
+
 /* ---- Solvers (GPU; mat.h:821-838) --------------------------------------- */
 /* Ax = b by PLU; only column 0 of b is read, as in the reference.  Replaces
  * mat_solve, mat.h:823 (4807-4837). */

@@ -145,6 +145,12 @@ int matgb_trsm_dev(char uplo, char trans, char diag, size_t n, size_t nrhs,
  * libmatgb_f64.  No counterpart in the reference (its GEMM is the NEON /
  * scalar mat_gemm, mat.h:2470-2796). */
 int matgb_plain_tensor_core(int on);
+/* Householder QR in place: R (m x n, m >= n, leading dimension ldr) holds A
+ * on entry and R on return; Q (m x m, leading dimension ldq) receives the
+ * orthogonal factor, or is not formed when NULL (mat_qr_r).  Device form of
+ * mat_qr / mat_qr_r (mat.h:3907-4192). */
+int matgb_qr_dev(size_t m, size_t n, mat_elem_t *R, size_t ldr, mat_elem_t *Q,
+                 size_t ldq);
 /* y = alpha*A*x + beta*y (A m x n).  Generalises mat_gemv (mat.h:2137). */
 /* y (n) = beta*y + alpha*A^T x for A m x n (mat_gemv_t, mat.h:2224-2248);
  * rows are split into chunks, summed in a fixed order, when n is small. */

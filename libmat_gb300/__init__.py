@@ -141,6 +141,9 @@ class Lib:
             "mat_chol": (_I, [MP, MP]),
             "mat_det": (E, [MP]),
             "mat_inv": (None, [MP, MP]),
+            "mat_qr": (None, [MP, MP, MP]),
+            "mat_qr_r": (None, [MP, MP]),
+            "matgb_qr_dev": (_I, [_S, _S, _P, _S, _P, _S]),
             "mat_solve": (None, [MP, MP, MP]),
             "mat_solve_spd": (_I, [MP, MP, MP]),
             "mat_solve_tril": (None, [MP, MP, MP]),
@@ -310,6 +313,21 @@ class Lib:
         self.c.mat_inv(C.byref(self.mat(out)), C.byref(self.mat(A)))
         self.check(0, "mat_inv")
         return out
+
+    def mat_qr(self, A, want_q=True):
+        """(Q, R) from mat_qr, or R alone from mat_qr_r."""
+        A = self.arr(A)
+        m, n = A.shape
+        R = np.zeros((m, n), self.dtype, order="F")
+        if want_q:
+            Q = np.zeros((m, m), self.dtype, order="F")
+            self.c.mat_qr(C.byref(self.mat(A)), C.byref(self.mat(Q)),
+                          C.byref(self.mat(R)))
+            self.check(0, "mat_qr")
+            return Q, R
+        self.c.mat_qr_r(C.byref(self.mat(A)), C.byref(self.mat(R)))
+        self.check(0, "mat_qr_r")
+        return R
 
     def _vec_call(self, name, A, b):
         A, b = self.arr(A), self.arr(b)

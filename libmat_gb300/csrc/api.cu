@@ -94,6 +94,22 @@ int do_gemm(Mat *C, elem_t alpha, const Mat *A, const Mat *B, elem_t beta) {
   return sync();
 }
 
+int do_qr(const Mat *A, Mat *Q, Mat *R) {
+  if (!ctx()) return MATGB_ERR_NO_DEVICE;
+  const int64_t m = A->rows, n = A->cols;
+  WS(dR, elem_t, WS_A, m * n);
+  elem_t *dQ = nullptr;
+  if (Q) {
+    dQ = (elem_t *)ws(WS_B, (size_t)(m * m) * sizeof(elem_t));
+    if (!dQ) return MATGB_ERR_NOMEM;
+  }
+  MGB_TRY(h2d(dR, A->data, m * n * ES));
+  MGB_TRY(qr(m, n, dR, m, dQ, m));
+  MGB_TRY(d2h(R->data, dR, m * n * ES));
+  if (Q) MGB_TRY(d2h(Q->data, dQ, m * m * ES));
+  return sync();
+}
+
 int do_syrk(Mat *C, const Mat *A, elem_t alpha, elem_t beta, char uplo,
             bool trans) {
   if (!ctx()) return MATGB_ERR_NO_DEVICE;
@@ -475,6 +491,26 @@ void mat_inv(Mat *out, const Mat *A) {  // mat.h:6166-6225
   size_t n = A->rows;
   MAT_ASSERT(out->rows == n && out->cols == n);
   if (do_inv(out, A)) fail_void("mat_inv");
+}
+
+void mat_qr(const Mat *A, Mat *Q, Mat *R) {  // mat.h:3907-4064
+  MAT_ASSERT_MAT(A);
+  MAT_ASSERT_MAT(Q);
+  MAT_ASSERT_MAT(R);
+  const size_t m = A->rows, n = A->cols;
+  MAT_ASSERT(m >= n && "mat_qr requires m >= n");
+  MAT_ASSERT(Q->rows == m && Q->cols == m);
+  MAT_ASSERT(R->rows == m && R->cols == n);
+  if (do_qr(A, Q, R)) fail_void("mat_qr");
+}
+
+void mat_qr_r(const Mat *A, Mat *R) {  // mat.h:4066-4192
+  MAT_ASSERT_MAT(A);
+  MAT_ASSERT_MAT(R);
+  const size_t m = A->rows, n = A->cols;
+  MAT_ASSERT(m >= n && "mat_qr_r requires m >= n");
+  MAT_ASSERT(R->rows == m && R->cols == n);
+  if (do_qr(A, nullptr, R)) fail_void("mat_qr_r");
 }
 
 void mat_solve(Vec *x, const Mat *A, const Vec *b) {  // mat.h:4807-4837

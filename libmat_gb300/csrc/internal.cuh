@@ -51,7 +51,7 @@ struct KtScope {
 enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
   WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_SWM, WS_SWG,
-  WS_RZA, WS_RZB, WS_RZC, WS_RZE, WS_TCA, WS_TCB, WS_TCS,
+  WS_RZA, WS_RZB, WS_RZC, WS_RZE, WS_TCA, WS_TCB, WS_TCS, WS_QR,
   WS_NSLOTS
 };
 void *ws(int slot, size_t bytes);
@@ -217,6 +217,9 @@ int fgmres_cycle(bool spd, int64_t n, const elem_t *A, int64_t lda,
                  double abort_ratio, const KrylovTarget *tg, elem_t *d,
                  int *inner, double *res_est, int *stalled);
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm);
+// Householder QR in place on R (m x n, m >= n); Q (m x m, may be null) gets
+// the orthogonal factor (qr.cu).
+int qr(int64_t m, int64_t n, elem_t *R, int64_t ldr, elem_t *Q, int64_t ldq);
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,
           const int32_t *perm, const elem_t *B, int64_t ldb, elem_t *X,
           int64_t ldx);
