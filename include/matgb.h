@@ -134,11 +134,11 @@ int matgb_potrs_dev(size_t n, size_t nrhs, const mat_elem_t *L, size_t lda,
  * 'N'), mat.h:4580-4803.  Non-unit diagonals are divided by, as there. */
 int matgb_trsm_dev(char uplo, char trans, char diag, size_t n, size_t nrhs,
                    const mat_elem_t *T, size_t ldt, mat_elem_t *B, size_t ldb);
-/* Plain float products and factorisations on the tensor cores: with on = 1
- * (the default) the float build runs mat_mul / mat_gemm / mat_syrk (and the
- * *_dev forms) of at least 256 x 256, and the trailing updates of mat_plu /
- * mat_chol / mat_solve* (and matgb_getrf_dev / matgb_potrf_dev) from order
- * 1024 up, as FP32-accurate tensor-core products: each operand split into
+/* Plain float products on the tensor cores: with on = 1 (the default) the
+ * float build runs mat_mul / mat_gemm / mat_syrk (and the *_dev forms) of at
+ * least 256 x 256, and the SYRK updates of mat_chol / mat_solve_spd (and
+ * matgb_potrf_dev) from order 1024 up, as FP32-accurate tensor-core
+ * products: each operand split into
  * FP16 hi + remainder under power-of-two row / column scales, three products
  * accumulated in FP32 (about 22 bits of every operand).  0: the FP32 SIMT
  * kernels.  -1: query only.  Returns the previous setting.  No effect in

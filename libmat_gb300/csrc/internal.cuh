@@ -160,11 +160,11 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
 int tc_sgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, float alpha,
              const float *A, int64_t lda, const float *B, int64_t ldb,
              float beta, float *C, int64_t ldc, int tri, bool same_ab = false);
-// Whether the plain float paths (GEMM, SYRK, LU, Cholesky) use the tensor
-// cores (matgb_plain_tensor_core), and the size from which they do.
+// Whether the plain float paths (GEMM, SYRK, Cholesky) use the tensor cores
+// (matgb_plain_tensor_core), and the size from which they do.
 bool plain_tc_on();
 constexpr int64_t kPlainTcMinMN = 256;
-constexpr int64_t kPlainTcMinN = 1024;  // LU / Cholesky order
+constexpr int64_t kPlainTcMinN = 1024;  // Cholesky order
 // FP64 residual R -= A X (X n x nrhs) on the tensor cores from exact FP16
 // digit products (resid64.cu); resid64_prepare slices A once per solve.
 int resid64_prepare(int64_t n, const double *A, int64_t lda);

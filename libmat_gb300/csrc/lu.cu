@@ -1924,13 +1924,15 @@ int laswp(elem_t *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2,
   return laswp_t<elem_t>(A, lda, c0, c1, c2, c3, ipiv, k1, k2, nullptr);
 }
 
-// The plain LU (mat_plu, mat_solve, matgb_getrf_dev): in the float build,
-// orders from 1024 up take their trailing updates on the tensor cores in the
-// FP32-accurate split form (lp 2) unless matgb_plain_tensor_core(0) chose the
-// SIMT GEMM; the pivot rule (and its MAT_DEFAULT_EPSILON skip) is the same.
+// The plain LU (mat_plu, mat_solve, matgb_getrf_dev) keeps its trailing
+// updates in the element type (SIMT GEMM): the pivot sequence must follow the
+// reference's on every data-determined step, and the three-product FP16
+// split (about 22 bits per operand) is noisier than FP32 -- on the 8192
+// N(0,1) plain config it changed a pivot at step 6370, where FP32 updates
+// follow the reference up to step 8116, the first step at which the
+// reference's own float and double pivots part.
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm) {
-  const int lp = (sizeof(elem_t) == 4 && plain_tc_on() && n >= kPlainTcMinN) ? 2 : -1;
-  return getrf_t<elem_t>(n, A, lda, ipiv, perm, kPivotEps, lp);
+  return getrf_t<elem_t>(n, A, lda, ipiv, perm, kPivotEps, -1);
 }
 
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,

@@ -1,7 +1,8 @@
 """GPU: the float build's tensor-core products (FP16 hi + remainder split under
 power-of-two row / column scales, three products, FP32 accumulation) behind
-mat_gemm / mat_mul / mat_syrk and the plain LU and Cholesky trailing updates,
-through the C ABI.
+mat_gemm / mat_mul / mat_syrk and the plain Cholesky's SYRK updates, through
+the C ABI (the plain LU keeps FP32 SIMT updates; its test here checks that
+the switch leaves its pivots with the reference's).
 
 Each case is checked against an FP64 product of the same float inputs (the
 exact answer to ~1e-16) and against the oracle where it is quick, within the
@@ -140,8 +141,9 @@ def test_tc_syrk(tc_mode, uplo, trans):
 
 @pytest.mark.parametrize("n", [1024, 1500])
 def test_tc_plain_lu_and_chol_vs_oracle(tc_mode, n):
-    """The plain float LU and Cholesky at orders that take the tensor-core
-    trailing updates: the oracle's pivots exactly, factors within 2e-4."""
+    """The plain float LU and Cholesky with the tensor cores switched on (the
+    Cholesky takes tensor-core SYRK updates at these orders): the oracle's
+    pivots exactly, factors within 2e-4."""
     L = tc_mode
     L.c.matgb_plain_tensor_core(1)
     O = Oracle("f32")
