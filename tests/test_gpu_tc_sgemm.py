@@ -117,7 +117,9 @@ def test_tc_gemm_special_values(tc_mode):
     assert np.array_equal(np.isfinite(got), np.isfinite(exp))
     ok = np.isfinite(exp)
     assert np.abs(got[ok] - exp[ok]).max() / np.abs(exp[ok]).max() <= TOL * 2
-    assert np.all(got[9] == 0.0)
+    # a zero row gives zeros except where it meets the infinite column
+    # (0 * inf = NaN, as in FP32)
+    assert np.all(got[9][np.arange(n) != 11] == 0.0) and np.isnan(got[9, 11])
 
 
 @pytest.mark.parametrize("uplo", ["L", "U"])
@@ -143,15 +145,20 @@ def test_tc_syrk(tc_mode, uplo, trans):
 def test_tc_plain_lu_and_chol_vs_oracle(tc_mode, n):
     """The plain float LU and Cholesky with the tensor cores switched on (the
     Cholesky takes tensor-core SYRK updates at these orders): the oracle's
-    pivots exactly, factors within 2e-4."""
+    pivots exactly; the LU factors reproduce P A to n u of |A| (at these
+    orders the last multipliers of two float eliminations differ by ~1e-3,
+    rounding noise, so they are not compared entry by entry); the Cholesky
+    factor of a well-conditioned matrix within 2e-4 of the oracle's."""
     L = tc_mode
     L.c.matgb_plain_tensor_core(1)
     O = Oracle("f32")
     A = rng.uniform(61 + n, (n, n), -1.0, 1.0, np.float32)
     Lg, Ug, pg, sg = L.mat_plu(A)
-    Lr, Ur, pr, sr = O.plu(A)
+    _, _, pr, sr = O.plu(A)
     assert np.array_equal(pg, pr) and sg == sr
-    assert rel(Lg, Lr) <= 2e-4 and rel(Ug, Ur) <= 2e-4
+    A64 = A.astype(np.float64)
+    res = np.abs(A64[pg] - Lg.astype(np.float64) @ Ug.astype(np.float64)).max()
+    assert res <= n * 2.0 ** -24 * np.abs(A64).max()
     Bm = rng.normal(62 + n, (n, n), np.float32)
     S = (Bm.T @ Bm / n + np.eye(n, dtype=np.float32)).astype(np.float32)
     Lc, rc = L.mat_chol(S)
