@@ -48,6 +48,8 @@ void *matgb_stream(void);
 unsigned long long matgb_launch_count(void);
 /* Number of SMs on the current device. */
 int matgb_sm_count(void);
+/* Directory of the loaded library file ("" if unknown). */
+const char *matgb_library_dir(void);
 
 /* ---- Memory helpers for device-resident callers ------------------------- */
 void *matgb_device_alloc(size_t bytes);
@@ -298,7 +300,7 @@ int matgb_gemv_noalloc_dev(size_t m, size_t n, mat_elem_t alpha,
 /* ---- Batched small systems ------------------------------------------------- */
 /* Solve `count` independent systems in one pass (mat_solve / mat_solve_spd
  * applied to each, mat.h:4807-4871).  Device pointers: system s has order
- * n[s] (1..128; 1..64 in libmatgb_f64), its matrix at A + offA[s]
+ * n[s] (1..128), its matrix at A + offA[s]
  * (column-major, leading dimension n[s]) and its right-hand side / solution at
  * b + offv[s] / x + offv[s].  kind[s] = 0: partial-pivot LU with the
  * reference's pivot rule; 1: Cholesky of the lower triangle.  status[s]: 0, or
@@ -309,6 +311,18 @@ int matgb_solve_batched_dev(int64_t count, const int32_t *n,
                             const int64_t *offv, const mat_elem_t *b,
                             mat_elem_t *x, const uint8_t *kind,
                             int32_t *status);
+/* The batched solver's schedule per (size bucket nb = 16, 32, 64, 96 or 128,
+ * kind 0 general / 1 SPD): algo 0 = one row per thread, Gauss-Jordan with one
+ * barrier per column; 1 = blocked LU in 8-column panels (nb >= 64);
+ * ctas_per_sm caps the resident systems per SM (0: as many as fit).  The
+ * library starts from compiled-in defaults, then reads the tuner's file
+ * (libmat_gb300/batched_tune.json next to the library directory, or
+ * $LIBMATGB_BATCHED_TUNE) at the first batched call; this call overrides
+ * one entry.  No counterpart in the reference. */
+int matgb_batched_tune(int nb, int kind, int algo, int ctas_per_sm);
+int matgb_batched_tune_get(int nb, int kind, int *algo, int *ctas_per_sm);
+/* Where the schedule came from: "defaults" or the file and its entry count. */
+const char *matgb_batched_tune_source(void);
 
 /* ---- Host (Mat) superset ------------------------------------------------- */
 /* AX = B for every column of B (mat_solve reads only column 0, mat.h:4825). */

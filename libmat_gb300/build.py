@@ -74,7 +74,7 @@ def build(jobs=None, verbose=False, extra=()):
     for prec in PRECS:
         lib = os.path.join(LIB, f"libmatgb_{prec}.so")
         if _stale(lib, objs[prec]):
-            cmd = [_nvcc()] + ARCH + ["-shared", "-o", lib] + objs[prec]
+            cmd = [_nvcc()] + ARCH + ["-shared", "-o", lib] + objs[prec] + ["-ldl"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError(f"link failed ({prec}):\n{r.stderr}")

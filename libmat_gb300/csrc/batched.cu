@@ -27,9 +27,83 @@
 // Scheduling: a device-side pre-pass sorts systems into (size bucket, kind)
 // queues; one persistent launch per queue pulls systems with an atomic
 // counter, largest sizes first.
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+
 #include "batched_kernels.cuh"
 
 namespace mgb {
+
+// ---- schedule table -----------------------------------------------------------
+// Compiled-in defaults: the blocked LU for the three large buckets, occupancy
+// as the kernels' resources allow.  tune_batched.py measures the
+// alternatives on the device and writes libmat_gb300/batched_tune.json (or
+// $LIBMATGB_BATCHED_TUNE), read once at the first batched call; entries it
+// does not name keep their defaults.
+static BatchTune g_tune[kNumBuckets][2] = {
+    {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}, {{1, 0}, {1, 0}}, {{1, 0}, {1, 0}},
+    {{1, 0}, {1, 0}}};
+static std::once_flag g_tune_once;
+static char g_tune_source[512] = "defaults";
+
+// Reads {"entries": [{"nb": 128, "kind": 0, "algo": 1, "ctas_per_sm": 2},
+// ...]} -- a flat list; every object needs all four keys.
+static int int_after(const char *p, const char *key, const char *end, int *out) {
+  const char *k = strstr(p, key);
+  if (!k || k >= end) return 0;
+  k = strchr(k + strlen(key), ':');
+  if (!k || k >= end) return 0;
+  return sscanf(k + 1, "%d", out) == 1;
+}
+
+static void load_tune_file() {
+  const char *env = getenv("LIBMATGB_BATCHED_TUNE");
+  std::string path;
+  if (env && *env) {
+    path = env;
+  } else {
+    // next to the package: <lib dir>/../batched_tune.json
+    const char *libdir = matgb_library_dir();
+    if (!libdir || !*libdir) return;
+    path = std::string(libdir) + "/../batched_tune.json";
+  }
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return;
+  std::string text;
+  char buf[4096];
+  size_t got;
+  while ((got = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
+  fclose(f);
+  int used = 0;
+  for (const char *p = strchr(text.c_str(), '{'); p; ) {
+    p = strchr(p + 1, '{');
+    if (!p) break;
+    const char *e = strchr(p, '}');
+    if (!e) break;
+    int nb, kind, algo, ctas;
+    if (int_after(p, "\"nb\"", e, &nb) && int_after(p, "\"kind\"", e, &kind) &&
+        int_after(p, "\"algo\"", e, &algo) &&
+        int_after(p, "\"ctas_per_sm\"", e, &ctas) && (kind == 0 || kind == 1) &&
+        (algo == 0 || algo == 1) && ctas >= 0 && ctas <= 64) {
+      for (int bk = 0; bk < kNumBuckets; bk++)
+        if (bucket_nb(bk) == nb && (algo == 0 || nb >= 64)) {
+          g_tune[bk][kind] = BatchTune{algo, ctas};
+          used++;
+        }
+    }
+    p = e;
+  }
+  snprintf(g_tune_source, sizeof g_tune_source, "%s (%d entries)", path.c_str(), used);
+}
+
+const BatchTune &batched_tune(int bucket, int kind) {
+  std::call_once(g_tune_once, load_tune_file);
+  return g_tune[bucket][kind ? 1 : 0];
+}
 
 // queue = 2*bucket + kind; counts per queue, then the list is grouped by queue
 __global__ void bucket_count_kernel(int64_t count, const int32_t *__restrict__ n,
@@ -82,11 +156,8 @@ int solve_batched(int64_t count, const int32_t *n, const int64_t *offA,
   cudaStream_t st = cx->stream;
   MGB_CUDA(cudaMemsetAsync(q, 0, sizeof(BatchQueues) + sizeof(int), st));
   const unsigned g = (unsigned)((count + 255) / 256 < 1024 ? (count + 255) / 256 : 1024);
-#ifdef MAT_DOUBLE_PRECISION
-  constexpr int nmax = 64;
-#else
   constexpr int nmax = 128;
-#endif
+  (void)batched_tune(0, 0);  // the schedule table, loaded once
   bucket_count_kernel<<<g, 256, 0, st>>>(count, n, kind, q);
   MGB_LAUNCHED("bucket_count");
   bucket_scatter_kernel<<<g, 256, 0, st>>>(count, n, kind, q, list);
@@ -114,6 +185,37 @@ int solve_batched(int64_t count, const int32_t *n, const int64_t *offA,
 }  // namespace mgb
 
 using namespace mgb;
+
+extern "C" int matgb_batched_tune(int nb, int kind, int algo, int ctas_per_sm) {
+  (void)batched_tune(0, 0);  // the file (if any) is read first, then overridden
+  if ((kind != 0 && kind != 1) || (algo != 0 && algo != 1) || ctas_per_sm < 0 ||
+      ctas_per_sm > 64)
+    return set_error(MATGB_ERR_ARG, "batched_tune: bad kind/algo/ctas_per_sm");
+  for (int bk = 0; bk < kNumBuckets; bk++)
+    if (bucket_nb(bk) == nb) {
+      if (algo == 1 && nb < 64)
+        return set_error(MATGB_ERR_ARG, "batched_tune: blocked form needs nb >= 64");
+      g_tune[bk][kind] = BatchTune{algo, ctas_per_sm};
+      return 0;
+    }
+  return set_error(MATGB_ERR_ARG, "batched_tune: nb must be 16, 32, 64, 96 or 128");
+}
+
+extern "C" int matgb_batched_tune_get(int nb, int kind, int *algo, int *ctas_per_sm) {
+  for (int bk = 0; bk < kNumBuckets; bk++)
+    if (bucket_nb(bk) == nb && (kind == 0 || kind == 1)) {
+      const BatchTune &t = batched_tune(bk, kind);
+      if (algo) *algo = t.algo;
+      if (ctas_per_sm) *ctas_per_sm = t.ctas_per_sm;
+      return 0;
+    }
+  return set_error(MATGB_ERR_ARG, "batched_tune_get: bad nb/kind");
+}
+
+extern "C" const char *matgb_batched_tune_source(void) {
+  (void)batched_tune(0, 0);
+  return g_tune_source;
+}
 
 extern "C" int matgb_solve_batched_dev(int64_t count, const int32_t *n,
                                        const int64_t *offA, const mat_elem_t *A,

@@ -27,6 +27,16 @@ struct BatchQueues {
   int fill[kNumQueues];   // scatter cursors
 };
 
+// Per (size bucket, kind) schedule, chosen by the tuner (tune_batched.py
+// writes batched_tune.json, which the library reads at the first batched
+// call; compiled-in defaults otherwise): algo 0 = register Gauss-Jordan,
+// 1 = blocked LU (buckets 64..128); ctas_per_sm 0 = as many as fit.
+struct BatchTune {
+  int algo;
+  int ctas_per_sm;
+};
+const BatchTune &batched_tune(int bucket, int kind);
+
 // |v| as a pivot key; NaN loses to every number except in the first row of
 // the search, where it wins (mat__iamax keeps its starting element when
 // nothing compares greater).
@@ -556,7 +566,7 @@ template <typename T, int NB, int GROUPS, int KIND>
 int launch_batched_queue(int queue, const int32_t *list, BatchQueues *q,
                          const int32_t *n, const int64_t *offA, const T *A,
                          const int64_t *offv, const T *b, T *x,
-                         int32_t *status, T eps) {
+                         int32_t *status, T eps, int ctas_per_sm = 0) {
   auto k = batched_kernel<T, NB, GROUPS, KIND>;
   constexpr int threads = Tpg<NB>::v * GROUPS;
   using Smem = typename std::conditional<KIND == 1, SpdSmem<T, NB>, BatchSmem<T, NB>>::type;
@@ -569,6 +579,7 @@ int launch_batched_queue(int queue, const int32_t *list, BatchQueues *q,
   }
   int per_sm = 0;
   MGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
+  if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
   if (per_sm < 1) per_sm = 1;
   const int grid = ctx()->sms * per_sm;
   static const char *names[2][5] = {

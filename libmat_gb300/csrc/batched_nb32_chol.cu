@@ -8,7 +8,8 @@ int batched_bucket_32_chol(int queue, const int32_t *list, BatchQueues *q,
                          const elem_t *A, const int64_t *offv,
                          const elem_t *b, elem_t *x, int32_t *status) {
   return launch_batched_queue<elem_t, 32, 4, 1>(queue, list, q, n, offA, A,
-                                                   offv, b, x, status, kPivotEps);
+                                                   offv, b, x, status, kPivotEps,
+                                                   batched_tune(1, 1).ctas_per_sm);
 }
 
 }  // namespace mgb

@@ -1,21 +1,28 @@
-// Batched Cholesky solves of systems of order <= 96 (see batched.cu).
-#include "batched_kernels.cuh"
+// Batched Cholesky solves of systems of order <= 96 (see batched.cu): the
+// blocked LU kernel (batched_blk.cuh) or the register Gauss-Jordan kernel
+// (batched_kernels.cuh), as the tuning table picks.
+#include "batched_smem.cuh"
 
 namespace mgb {
 
 int batched_bucket_96_chol(int queue, const int32_t *list, BatchQueues *q,
-                         const int32_t *n, const int64_t *offA,
-                         const elem_t *A, const int64_t *offv,
-                         const elem_t *b, elem_t *x, int32_t *status) {
+                           const int32_t *n, const int64_t *offA,
+                           const elem_t *A, const int64_t *offv,
+                           const elem_t *b, elem_t *x, int32_t *status) {
+  const BatchTune &t = batched_tune(3, 1);
 #ifdef MAT_DOUBLE_PRECISION
-  // A row of this order does not fit in registers in double precision; the
-  // driver has marked these systems with status -2.
-  (void)queue; (void)list; (void)q; (void)n; (void)offA; (void)A; (void)offv;
-  (void)b; (void)x; (void)status;
-  return 0;
+  // a row of this order does not fit in registers in double precision: the
+  // rows live in shared memory (batched_smem.cuh)
+  (void)t;
+  return launch_smem_queue<elem_t, 96, 1>(queue, list, q, n, offA, A, offv, b, x,
+                                              status, kPivotEps);
 #else
+  if (t.algo == 1)
+    return launch_blk_queue<elem_t, 96, 1, 3>(queue, list, q, n, offA, A, offv,
+                                                   b, x, status, kPivotEps, t.ctas_per_sm);
   return launch_batched_queue<elem_t, 96, 1, 1>(queue, list, q, n, offA, A,
-                                                   offv, b, x, status, kPivotEps);
+                                                   offv, b, x, status, kPivotEps,
+                                                   t.ctas_per_sm);
 #endif
 }
 

@@ -1,5 +1,6 @@
 // Runtime: device context, library stream, error channel, grow-only device
 // workspace, events, memory helpers and seeded device-side input generation.
+#include <dlfcn.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -211,6 +212,25 @@ unsigned long long matgb_launch_count(void) { return g_launches.load(); }
 int matgb_sm_count(void) {
   Ctx *c = ctx();
   return c ? c->sms : 0;
+}
+
+const char *matgb_library_dir(void) {
+  static char dir[1024];
+  static std::once_flag once;
+  std::call_once(once, [] {
+    Dl_info info;
+    dir[0] = 0;
+    if (dladdr(reinterpret_cast<void *>(&matgb_library_dir), &info) && info.dli_fname) {
+      strncpy(dir, info.dli_fname, sizeof dir - 1);
+      dir[sizeof dir - 1] = 0;
+      char *slash = strrchr(dir, '/');
+      if (slash)
+        *slash = 0;
+      else
+        strcpy(dir, ".");
+    }
+  });
+  return dir;
 }
 
 void *matgb_device_alloc(size_t bytes) {

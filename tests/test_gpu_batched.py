@@ -3,7 +3,14 @@ each system checked against the oracle's mat_solve / mat_solve_spd.
 
 Systems are well conditioned by construction (U[-1,1] + n*I for LU,
 B^T B + n*I for Cholesky), so the tolerance is the parity suite's factor
-bound: max|x - x_ref| <= 2e-4 * max|x_ref| (f32) / 1e-11 (f64)."""
+bound: max|x - x_ref| <= 2e-4 * max|x_ref| (f32) / 1e-11 (f64).  Systems
+that pivot (U[-1,1], no shift) are held to the parity suite's conditioning
+bound: |x - x_ref| <= 10 * cond(A) * u * |x_ref| (the oracle solves with the
+same pivots; two backward-stable float solves differ by ~cond * u).  Both
+schedules of the large buckets -- the blocked LU and the register
+Gauss-Jordan kernel -- are run (matgb_batched_tune)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -11,6 +18,25 @@ from oracle.loader import Oracle
 
 pytestmark = pytest.mark.gpu
 TOL = {"f32": 2e-4, "f64": 1e-11}
+U = {"f32": 2.0 ** -24, "f64": 2.0 ** -53}
+
+
+@pytest.fixture(params=[1, 0], ids=["blocked", "gauss_jordan"])
+def algo(request, gpu):
+    """Every large bucket on one algorithm for the test, defaults restored."""
+    saved = {}
+    for prec in ("f32", "f64"):
+        L = gpu[prec]
+        for nb in (64, 96, 128):
+            for kind in (0, 1):
+                a, c = C.c_int(), C.c_int()
+                L.check(L.c.matgb_batched_tune_get(nb, kind, C.byref(a), C.byref(c)))
+                saved[prec, nb, kind] = (a.value, c.value)
+                # the double build's 96 and 128 buckets have one form only
+                L.check(L.c.matgb_batched_tune(nb, kind, request.param, c.value))
+    yield request.param
+    for (prec, nb, kind), (a, c) in saved.items():
+        gpu[prec].c.matgb_batched_tune(nb, kind, a, c)
 
 
 def make_batch(count, nmax, dt, seed):
@@ -31,8 +57,8 @@ def make_batch(count, nmax, dt, seed):
 
 
 @pytest.mark.parametrize("prec,nmax,count", [("f32", 128, 600), ("f32", 20, 300),
-                                             ("f64", 64, 300)])
-def test_batched_matches_oracle(gpu, prec, nmax, count):
+                                             ("f64", 128, 300)])
+def test_batched_matches_oracle(gpu, algo, prec, nmax, count):
     L = gpu[prec]
     O = Oracle(prec)
     mats, rhs, kinds = make_batch(count, nmax, L.dtype, 11 + nmax)
@@ -44,39 +70,49 @@ def test_batched_matches_oracle(gpu, prec, nmax, count):
         assert err <= TOL[prec], (A.shape[0], k, err)
 
 
-def test_batched_pivoting_and_not_spd(gpu):
-    """Row exchanges are exercised (no diagonal shift), and a non-SPD system
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_batched_pivoting_and_not_spd(gpu, algo, prec):
+    """Row exchanges on every step (U[-1,1], no diagonal shift) in every
+    bucket: x within 10 * cond * u of the oracle's mat_solve; a non-SPD
+    system (a negative Schur diagonal at step 3, and one at the last step)
     reports -1 and leaves its x untouched while its neighbours solve."""
-    L = gpu["f32"]
-    O = Oracle("f32")
+    L = gpu[prec]
+    O = Oracle(prec)
+    dt = L.dtype
     rs = np.random.default_rng(5)
     mats, rhs, kinds = [], [], []
-    for n in (3, 17, 40, 77, 128):
-        mats.append(np.asfortranarray(rs.uniform(-1, 1, (n, n)).astype(np.float32)))
-        rhs.append(rs.standard_normal(n).astype(np.float32))
+    sizes = (1, 2, 3, 8, 9, 16, 17, 31, 33, 40, 64, 65, 77, 96, 97, 120, 128)
+    for n in sizes:
+        mats.append(np.asfortranarray(rs.uniform(-1, 1, (n, n)).astype(dt)))
+        rhs.append(rs.standard_normal(n).astype(dt))
         kinds.append(0)
-    bad = np.eye(5, dtype=np.float32)
-    bad[3, 3] = -2.0
-    mats.append(bad)
-    rhs.append(np.ones(5, np.float32))
-    kinds.append(1)
+    for n, where in ((5, 3), (100, 99)):
+        bad = np.eye(n, dtype=dt) * 2
+        bad[where, where] = -2.0
+        mats.append(bad)
+        rhs.append(np.ones(n, dt))
+        kinds.append(1)
     xs, status = L.solve_batched(mats, rhs, kinds)
-    assert list(status) == [0, 0, 0, 0, 0, -1]
-    assert np.array_equal(xs[-1], rhs[-1])  # untouched: still the input copy
-    for A, b, x in zip(mats[:-1], rhs[:-1], xs[:-1]):
-        xr = O.solve(A, b)
-        # random U[-1,1] matrices: compare through the backward error
-        r = np.abs(A.astype(np.float64) @ x - b).max()
-        eta = r / (np.abs(A).sum(1).max() * np.abs(x).max() + np.abs(b).max())
-        assert eta <= 1e-5, (A.shape[0], eta)
-        assert np.abs(x - xr).max() / np.abs(xr).max() <= 0.05
+    assert list(status) == [0] * len(sizes) + [-1, -1]
+    # untouched: the solution buffer still holds the input copy
+    assert np.array_equal(xs[-1], rhs[-1]) and np.array_equal(xs[-2], rhs[-2])
+    for A, b, x in zip(mats[:len(sizes)], rhs, xs):
+        xr = O.solve(A, b).astype(np.float64)
+        cond = np.linalg.cond(A.astype(np.float64), np.inf)
+        err = np.abs(x.astype(np.float64) - xr).max() / np.abs(xr).max()
+        assert err <= 10 * cond * U[prec], (A.shape[0], err, cond)
 
 
-def test_batched_f64_marks_unsupported_order(gpu):
-    """The double build solves orders up to 64; larger systems get status -2
-    and their neighbours are still solved."""
-    L = gpu["f64"]
-    mats = [np.eye(100) * 2, np.eye(3) * 4]
-    xs, status = L.solve_batched(mats, [np.ones(100), np.ones(3)], [0, 1])
-    assert list(status) == [-2, 0]
-    assert np.allclose(xs[1], 0.25)
+def test_batched_marks_unsupported_order(gpu):
+    """Orders above 128 (and below 1) get status -2; their neighbours are
+    still solved, in both builds (the double build's 65..128 orders keep
+    their rows in shared memory)."""
+    for prec in ("f32", "f64"):
+        L = gpu[prec]
+        dt = L.dtype
+        mats = [np.eye(130, dtype=dt) * 2, np.eye(3, dtype=dt) * 4,
+                np.eye(100, dtype=dt) * 8]
+        xs, status = L.solve_batched(mats, [np.ones(130, dt), np.ones(3, dt),
+                                            np.ones(100, dt)], [0, 1, 0])
+        assert list(status) == [-2, 0, 0]
+        assert np.allclose(xs[1], 0.25) and np.allclose(xs[2], 0.125)
