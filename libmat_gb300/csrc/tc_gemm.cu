@@ -40,6 +40,7 @@ namespace mgb {
 constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 64;
 constexpr int kTcThreads = 320;
 constexpr uint32_t kTcWaitLimit = 1u << 24;  // ~1.5 s of polling
+constexpr uint32_t kTcSpin = 256;  // producer / MMA polls before sleeping
 // K blocks per launch (all segments): bounds one CTA's main loop (3 x 16384
 // columns of K, ~0.3 ms on one SM), far inside the wait limit; longer sums
 // are split by the caller
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
     int issued = 0;
     for (int kb = 0; kb < nkb; kb++) {
       const int st = kb % kTcStages, use = kb / kTcStages;
-      if (use > 0 && !tc::mbar_wait(&s.empty[st], (use - 1) & 1, kTcWaitLimit)) {
+      if (use > 0 && !tc::mbar_wait(&s.empty[st], (use - 1) & 1, kTcWaitLimit, kTcSpin)) {
         s.timeout = 1;
         break;
       }
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
     bool ok = true;
     for (int kb = 0; kb < nkb; kb++) {
       const int st = kb % kTcStages, use = kb / kTcStages;
-      if (s.timeout || !tc::mbar_wait(&s.full[st], use & 1, kTcWaitLimit)) {
+      if (s.timeout || !tc::mbar_wait(&s.full[st], use & 1, kTcWaitLimit, kTcSpin)) {
         ok = false;
         break;
       }

@@ -46,15 +46,17 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait: the first 256 polls spin (a pipeline wait is usually over
-// within a few hundred cycles), later ones sleep briefly between polls; false
-// after `limit` polls (at most about limit * 100 ns), so a lost arrival never
-// hangs the GPU.
+// Bounded wait: the first `spin` polls spin (the pipeline waits of the
+// producer and MMA threads are usually over within a few hundred cycles),
+// later ones sleep briefly between polls (waiters that would otherwise take
+// issue slots from those threads, like the epilogue's); false after `limit`
+// polls (at most about limit * 100 ns), so a lost arrival never hangs the
+// GPU.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
-                                          uint32_t limit) {
+                                          uint32_t limit, uint32_t spin = 0) {
   for (uint32_t i = 0; i < limit; i++) {
     if (mbar_test(bar, parity)) return true;
-    if (i >= 256) __nanosleep(64);
+    if (i >= spin) __nanosleep(64);
   }
   return false;
 }
