@@ -687,33 +687,12 @@ def run_blas_t(mg, steps=5, warmup=3):
 
 
 def run_batched(mg, count=100000, steps=5, warmup=3):
+    from libmat_gb300 import batched_data
     L = mg.load("f32")
-    rs = np.random.default_rng(1005)
-    ns = rs.integers(4, 129, count).astype(np.int32)
-    kinds = (np.arange(count) % 2).astype(np.uint8)
-    offA = np.zeros(count, np.int64)
-    offA[1:] = np.cumsum(ns.astype(np.int64) ** 2)[:-1]
-    offv = np.zeros(count, np.int64)
-    offv[1:] = np.cumsum(ns.astype(np.int64))[:-1]
-    totA = int(offA[-1] + ns[-1] ** 2)
-    totv = int(offv[-1] + ns[-1])
-    A = np.empty(totA, np.float32)
-    for n in range(4, 129):
-        idx = np.nonzero(ns == n)[0]
-        lu = idx[kinds[idx] == 0]
-        sp = idx[kinds[idx] == 1]
-        if len(lu):
-            M = rs.uniform(-1, 1, (len(lu), n, n)).astype(np.float32) + \
-                n * np.eye(n, dtype=np.float32)
-            A[(offA[lu][:, None] + np.arange(n * n)).ravel()] = \
-                M.transpose(0, 2, 1).reshape(len(lu), -1).ravel()
-        if len(sp):
-            Bm = rs.standard_normal((len(sp), n, n)).astype(np.float32)
-            M = np.matmul(Bm.transpose(0, 2, 1), Bm) + n * np.eye(n, dtype=np.float32)
-            A[(offA[sp][:, None] + np.arange(n * n)).ravel()] = \
-                M.transpose(0, 2, 1).reshape(len(sp), -1).ravel()
-    b = rs.standard_normal(totv).astype(np.float32)
-    arrs = {"n": ns, "oA": offA, "ov": offv, "A": A, "b": b, "k": kinds}
+    rs = np.random.default_rng(7)  # the sample of systems checked below
+    arrs = batched_data.make(count)
+    ns, offA, offv, A, b, kinds = (arrs[k] for k in ("n", "oA", "ov", "A", "b", "k"))
+    totA, totv = A.size, b.size
     d = {k: L.dalloc(v.nbytes) for k, v in arrs.items()}
     dx = L.dalloc(b.nbytes)
     st = L.dalloc(4 * count)
@@ -772,7 +751,12 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
     flops = float(np.sum(np.where(kinds == 0, 2 * nn ** 3 / 3, nn ** 3 / 3) + 2 * nn ** 2))
     fp32_peak = pk.get("fp32_tflops") or L.c.matgb_measure_fma_peak(0)
     tfl = flops / (ms * 1e-3) / 1e12
+    fused = L.c.matgb_batched_schedule(-1, -1, -1)
     return {"workload": "batched_100k_uneven_f32", "ms": ms,
+            "schedule": ("one persistent cooperative launch, replayed as a "
+                         "CUDA graph" if fused else "one launch per (bucket, "
+                         "kind) queue"),
+            "tune_source": L.c.matgb_batched_tune_source().decode(),
             "solves_per_s": count / (ms * 1e-3), "bytes": byt,
             "hbm_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"],
             "hbm_peak_source": src, "flops": flops, "tflops": tfl,

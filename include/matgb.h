@@ -299,7 +299,10 @@ int matgb_gemv_noalloc_dev(size_t m, size_t n, mat_elem_t alpha,
 
 /* ---- Batched small systems ------------------------------------------------- */
 /* Solve `count` independent systems in one pass (mat_solve / mat_solve_spd
- * applied to each, mat.h:4807-4871).  Device pointers: system s has order
+ * applied to each, mat.h:4807-4871).  status[s] = -2 marks an order outside
+ * 1..128 (not solved); with the fused schedule, -4 marks a system left
+ * unsolved because the launch's bounded grid barrier gave up (never expected:
+ * the launch is cooperative).  Device pointers: system s has order
  * n[s] (1..128), its matrix at A + offA[s]
  * (column-major, leading dimension n[s]) and its right-hand side / solution at
  * b + offv[s] / x + offv[s].  kind[s] = 0: partial-pivot LU with the
@@ -321,6 +324,15 @@ int matgb_solve_batched_dev(int64_t count, const int32_t *n,
  * one entry.  No counterpart in the reference. */
 int matgb_batched_tune(int nb, int kind, int algo, int ctas_per_sm);
 int matgb_batched_tune_get(int nb, int kind, int *algo, int *ctas_per_sm);
+/* The batched solver's launch schedule: fused = 1 (the default) files and
+ * solves every system in ONE persistent cooperative launch (orders 65..128
+ * one per CTA, 33..64 two, 17..32 four, 1..16 eight; largest first), 0 = one
+ * launch per (bucket, kind) queue with the per-bucket algorithms above;
+ * ctas_per_sm caps the fused launch's resident CTAs per SM (0: as many as
+ * fit); graphs = 1 (the default) captures the fused launch sequence in a CUDA
+ * graph and replays it while the same buffers are passed.  -1 leaves a
+ * setting unchanged.  Returns the previous fused setting. */
+int matgb_batched_schedule(int fused, int ctas_per_sm, int graphs);
 /* Where the schedule came from: "defaults" or the file and its entry count. */
 const char *matgb_batched_tune_source(void);
 

@@ -39,19 +39,28 @@
 namespace mgb {
 
 // ---- schedule table -----------------------------------------------------------
-// Compiled-in defaults: the blocked LU for the three large buckets, occupancy
-// as the kernels' resources allow.  tune_batched.py measures the
-// alternatives on the device and writes libmat_gb300/batched_tune.json (or
+// Compiled-in defaults: the register Gauss-Jordan kernels everywhere (the
+// blocked LU measured 2.5-3x slower on the 100k-system workload: its panel,
+// one warp's serial chain of 8 columns, idles the CTA), occupancy as the
+// kernels' resources allow.  tune_batched.py measures the alternatives on the
+// device and writes libmat_gb300/batched_tune.json (or
 // $LIBMATGB_BATCHED_TUNE), read once at the first batched call; entries it
 // does not name keep their defaults.
 static BatchTune g_tune[kNumBuckets][2] = {
-    {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}, {{1, 0}, {1, 0}}, {{1, 0}, {1, 0}},
-    {{1, 0}, {1, 0}}};
+    {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}},
+    {{0, 0}, {0, 0}}};
+static int g_fused = 1;       // 1: one persistent launch; 0: a launch per queue
+static int g_fused_ctas = 0;  // resident CTAs per SM for it (0: as many as fit)
+static int g_graphs = 1;      // replay the launch sequence as a CUDA graph
+static bool g_graphs_broken = false;
 static std::once_flag g_tune_once;
 static char g_tune_source[512] = "defaults";
 
-// Reads {"entries": [{"nb": 128, "kind": 0, "algo": 1, "ctas_per_sm": 2},
-// ...]} -- a flat list; every object needs all four keys.
+// Reads {"entries": [{"prec": "f32", "nb": 128, "kind": 0, "algo": 1,
+// "ctas_per_sm": 2}, ...]} -- a flat list of objects; each needs nb, kind,
+// algo and ctas_per_sm, and one whose "prec" names the other build is
+// skipped.  (Other keys, and other objects without those keys, are
+// ignored.)
 static int int_after(const char *p, const char *key, const char *end, int *out) {
   const char *k = strstr(p, key);
   if (!k || k >= end) return 0;
@@ -79,11 +88,31 @@ static void load_tune_file() {
   while ((got = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
   fclose(f);
   int used = 0;
+  {
+    // top-level schedule keys (before the entries list)
+    const char *t = text.c_str();
+    const char *lst = strstr(t, "\"entries\"");
+    const char *end = lst ? lst : t + text.size();
+    int v;
+    if (int_after(t, "\"fused\"", end, &v) && (v == 0 || v == 1)) g_fused = v;
+    if (int_after(t, "\"fused_ctas_per_sm\"", end, &v) && v >= 0 && v <= 64)
+      g_fused_ctas = v;
+  }
   for (const char *p = strchr(text.c_str(), '{'); p; ) {
     p = strchr(p + 1, '{');
     if (!p) break;
     const char *e = strchr(p, '}');
     if (!e) break;
+    // entries for the other precision's library are skipped
+    const char *pk = strstr(p, "\"prec\"");
+    if (pk && pk < e) {
+      const char *want = sizeof(elem_t) == 8 ? "f64" : "f32";
+      const char *v = strchr(pk + 6, '"');
+      if (!v || v >= e || strncmp(v + 1, want, 3) != 0) {
+        p = e;
+        continue;
+      }
+    }
     int nb, kind, algo, ctas;
     if (int_after(p, "\"nb\"", e, &nb) && int_after(p, "\"kind\"", e, &kind) &&
         int_after(p, "\"algo\"", e, &algo) &&
@@ -142,13 +171,84 @@ __global__ void check_sizes_kernel(int64_t count, const int32_t *__restrict__ n,
     if (n[s] < 1 || n[s] > nmax) status[s] = -2;
 }
 
+// ---- the one-launch schedule (batched_fused.cu), replayed as a CUDA graph -----
+int launch_fused(int64_t count, const int32_t *n, const int64_t *offA,
+                 const elem_t *A, const int64_t *offv, const elem_t *b, elem_t *x,
+                 const uint8_t *kind, int32_t *status, int32_t *list, void *state,
+                 int ctas_per_sm);
+int fused_prepare(int ctas_per_sm);
+size_t fused_state_bytes();
+
+
+// The graph of the last call's arguments: the memset of the queue state and
+// the cooperative launch, captured once and replayed while the caller passes
+// the same buffers (the usual case: a solver called again on new data in the
+// same buffers).
+struct GraphKey {
+  int64_t count;
+  const void *p[11];
+  int ctas;
+  bool operator==(const GraphKey &o) const {
+    if (count != o.count || ctas != o.ctas) return false;
+    for (int i = 0; i < 11; i++)
+      if (p[i] != o.p[i]) return false;
+    return true;
+  }
+};
+static GraphKey g_gkey{};
+static cudaGraphExec_t g_gexec = nullptr;
+
+static int solve_fused(int64_t count, const int32_t *n, const int64_t *offA,
+                       const elem_t *A, const int64_t *offv, const elem_t *b,
+                       elem_t *x, const uint8_t *kind, int32_t *status) {
+  cudaStream_t st = ctx()->stream;
+  int32_t *list = (int32_t *)ws(WS_V1, (size_t)kNumQueues * count * sizeof(int32_t));
+  void *state = ws(WS_T2, fused_state_bytes() + 256);
+  if (!list || !state) return MATGB_ERR_NOMEM;
+  MGB_TRY(fused_prepare(g_fused_ctas));  // attributes, occupancy (not capturable)
+  if (!g_graphs || g_graphs_broken || ktime_on())
+    return launch_fused(count, n, offA, A, offv, b, x, kind, status, list, state,
+                        g_fused_ctas);
+  const GraphKey key{count, {n, offA, A, offv, b, x, kind, status, list, state, st},
+                     g_fused_ctas};
+  if (!(g_gexec && key == g_gkey)) {
+    if (g_gexec) {
+      cudaGraphExecDestroy(g_gexec);
+      g_gexec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    MGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int r = launch_fused(count, n, offA, A, offv, b, x, kind, status, list,
+                               state, g_fused_ctas);
+    const cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (r != 0 || e != cudaSuccess || !graph ||
+        cudaGraphInstantiate(&g_gexec, graph, 0) != cudaSuccess) {
+      // capture of this launch is not supported here: launch directly from
+      // now on
+      if (graph) cudaGraphDestroy(graph);
+      g_gexec = nullptr;
+      cudaGetLastError();
+      matgb_clear_error();
+      g_graphs_broken = true;
+      return launch_fused(count, n, offA, A, offv, b, x, kind, status, list, state,
+                          g_fused_ctas);
+    }
+    cudaGraphDestroy(graph);
+    g_gkey = key;
+  }
+  MGB_CUDA(cudaGraphLaunch(g_gexec, st));
+  return launched("batched_fused");
+}
+
 int solve_batched(int64_t count, const int32_t *n, const int64_t *offA,
                   const elem_t *A, const int64_t *offv, const elem_t *b,
                   elem_t *x, const uint8_t *kind, int32_t *status) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (count <= 0) return 0;
-  if (count > INT32_MAX) return set_error(MATGB_ERR_ARG, "batch too large");
+  if (count > INT32_MAX / kNumQueues) return set_error(MATGB_ERR_ARG, "batch too large");
+  (void)batched_tune(0, 0);  // the schedule table, loaded once
+  if (g_fused) return solve_fused(count, n, offA, A, offv, b, x, kind, status);
   BatchQueues *q = (BatchQueues *)ws(WS_T2, sizeof(BatchQueues) + 256);
   int32_t *list = (int32_t *)ws(WS_V1, (size_t)count * sizeof(int32_t));
   if (!q || !list) return MATGB_ERR_NOMEM;
@@ -157,7 +257,6 @@ int solve_batched(int64_t count, const int32_t *n, const int64_t *offA,
   MGB_CUDA(cudaMemsetAsync(q, 0, sizeof(BatchQueues) + sizeof(int), st));
   const unsigned g = (unsigned)((count + 255) / 256 < 1024 ? (count + 255) / 256 : 1024);
   constexpr int nmax = 128;
-  (void)batched_tune(0, 0);  // the schedule table, loaded once
   bucket_count_kernel<<<g, 256, 0, st>>>(count, n, kind, q);
   MGB_LAUNCHED("bucket_count");
   bucket_scatter_kernel<<<g, 256, 0, st>>>(count, n, kind, q, list);
@@ -210,6 +309,15 @@ extern "C" int matgb_batched_tune_get(int nb, int kind, int *algo, int *ctas_per
       return 0;
     }
   return set_error(MATGB_ERR_ARG, "batched_tune_get: bad nb/kind");
+}
+
+extern "C" int matgb_batched_schedule(int fused, int ctas_per_sm, int graphs) {
+  (void)batched_tune(0, 0);
+  const int prev = g_fused;
+  if (fused >= 0) g_fused = fused ? 1 : 0;
+  if (ctas_per_sm >= 0) g_fused_ctas = ctas_per_sm;
+  if (graphs >= 0) g_graphs = graphs ? 1 : 0;
+  return prev;
 }
 
 extern "C" const char *matgb_batched_tune_source(void) {

@@ -56,6 +56,18 @@ struct BlkSmem {
 
 __device__ __forceinline__ int ucoff(int j) { return j * (j + 1) / 2; }
 
+// The barrier of the threads solving one system: the whole CTA, or a named
+// barrier over one group of NB threads (several systems per CTA).
+struct CtaBar {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct GroupBar {
+  int id, count;  // named barrier id (1..15) and its thread count
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
+};
+
 // 8 consecutive values to / from 16-byte aligned shared memory, register
 // arrays indexed statically only (no address of a register array is taken)
 template <typename T>
@@ -210,9 +222,10 @@ __device__ __forceinline__ bool blk_panel(BlkSmem<T, NB> &sm, int K0, int pw,
 // Solve one system of order n (NB - 31 <= n <= NB in practice; any n <= NB
 // works) with the CTA's NB threads; returns the status (0, or -1: SPD
 // system not positive definite, x untouched).
-template <typename T, int NB, int KIND>
+template <typename T, int NB, int KIND, class Bar = CtaBar>
 __device__ int solve_blk(const T *__restrict__ A, int n, const T *__restrict__ b,
-                         T *__restrict__ x, BlkSmem<T, NB> &sm, int i, T eps) {
+                         T *__restrict__ x, BlkSmem<T, NB> &sm, int i, T eps,
+                         Bar bar = Bar()) {
   constexpr int W = VecOf<T>::w;
   const int warp = i >> 5, lane = i & 31;
   const bool act = i < n;
@@ -239,12 +252,12 @@ __device__ int solve_blk(const T *__restrict__ A, int n, const T *__restrict__ b
     // 1. stage the panel entries of every live row
     int mylr = sm.lr[i];
     if (mylr >= K0) st8<T>(&sm.pan[i][0], a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]);
-    __syncthreads();
+    bar();
     // 2. the panel, in warp 0
     if (warp == 0) {
       if (!blk_panel<T, NB, KIND>(sm, K0, pw, n, eps) && lane == 0) sm.fail = 1;
     }
-    __syncthreads();
+    bar();
     if (KIND == 1 && sm.fail) return -1;
     mylr = sm.lr[i];
     // 3. the panel's pivot rows stage their trailing entries and rhs
@@ -264,7 +277,7 @@ __device__ int solve_blk(const T *__restrict__ A, int n, const T *__restrict__ b
       }
       rw[tw] = rb;  // after the vector stores (one may run past tw)
     }
-    __syncthreads();
+    bar();
     // 4. U12 column by column (thread j), rhs last; U filed by columns
     if (i <= tw) {
       T u[kBPW];
@@ -297,7 +310,7 @@ __device__ int solve_blk(const T *__restrict__ A, int n, const T *__restrict__ b
       T *col = sm.ucol + ucoff(K0 + c) + K0;
       for (int c2 = 0; c2 <= c; c2++) col[c2] = sm.pan[sm.pv[c2]][c];
     }
-    __syncthreads();
+    bar();
     // 5. rank-8 update of the rows below the panel, then the frame shifts
     if (mylr >= K0 + pw) {
       T l[kBPW];
@@ -329,7 +342,7 @@ __device__ int solve_blk(const T *__restrict__ A, int n, const T *__restrict__ b
       for (int c = 0; c < kBPW; c++) rb = fma(-u[c], l[c], rb);
     }
   }
-  __syncthreads();
+  bar();
   // back substitution U x = y in warp 0: column by column, lane l holding
   // the partial sums of rows l, l + 32, ...
   if (warp == 0) {
@@ -356,7 +369,7 @@ __device__ int solve_blk(const T *__restrict__ A, int n, const T *__restrict__ b
       }
     }
   }
-  __syncthreads();
+  bar();
   if (act) x[i] = sm.xv[i];
   return 0;
 }

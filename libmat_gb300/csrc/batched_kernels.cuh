@@ -82,6 +82,21 @@ __device__ __forceinline__ void gsync() {
     __syncthreads();
 }
 
+// The group barrier as a functor, so a caller that runs several groups of
+// more than 32 threads in one CTA can pass a named barrier instead.
+template <int NB>
+struct GSync {
+  __device__ __forceinline__ void operator()() const { gsync<NB>(); }
+};
+// A named barrier over `count` threads (id 1..15); bar.sync 0 is
+// __syncthreads.
+struct NamedBar {
+  int id, count;
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
+};
+
 // Row slot: slot[3 + k] = a[k] (k < NB) and slot[NB + 3] = right-hand side,
 // so the update's u[j + 1] = slot[j + 4] starts on a 16-byte boundary for
 // every 4th (float) or 2nd (double) j and is read with vector loads.
@@ -223,10 +238,10 @@ __device__ __forceinline__ void shift_update(T (&a)[NB], T &rb, const T *slot,
 // (all that mat_chol reads), no row exchanges, and a pivot d_K <= 0 -- the
 // Schur-complement diagonal mat_chol tests -- makes the status -1 and leaves
 // x untouched.  Returns the status.
-template <typename T, int NB, int KIND>
+template <typename T, int NB, int KIND, class Bar = GSync<NB>>
 __device__ int solve_one(const T *__restrict__ A, int n,
                          const T *__restrict__ b, T *__restrict__ x,
-                         BatchSmem<T, NB> &sm, int i, T eps) {
+                         BatchSmem<T, NB> &sm, int i, T eps, Bar bar = Bar()) {
   const bool act = i < n;
   const int w = NB <= 32 ? 0 : (i >> 5);
   const unsigned gm = group_mask<NB>();
@@ -267,7 +282,7 @@ __device__ int solve_one(const T *__restrict__ A, int n,
           sm.widx[par][w] = (int)((wi << 2) | (unsigned)w);
         }
         if (cand && (unsigned)lr == wi) put_row<T, NB>(sm.slot[par][w], a, rb, live);
-        gsync<NB>();
+        bar();
         if constexpr (Warps<NB>::v == 1) {
           p = (int)wi;
         } else {
@@ -297,7 +312,7 @@ __device__ int solve_one(const T *__restrict__ A, int n,
           sm.widx[par][w] = idx;
         }
         if (cand && lr == idx) put_row<T, NB>(sm.slot[par][w], a, rb, live);
-        gsync<NB>();
+        bar();
         p = sm.widx[par][0];
         if constexpr (Warps<NB>::v > 1) {
           T bk = sm.wkey[par][0];
@@ -316,7 +331,7 @@ __device__ int solve_one(const T *__restrict__ A, int n,
     } else {
       // the pivot is logical row K itself
       if (act && lr == K) put_row<T, NB>(sm.slot[par][0], a, rb, live);
-      gsync<NB>();
+      bar();
     }
     const T *u = sm.slot[par][pw];
     const T piv = u[3];
@@ -359,17 +374,17 @@ __device__ __forceinline__ auto spec_key(T v, bool first) {
 
 // The fallback as a call of its own, so its register frame does not add to
 // the diagonal-first loop's.
-template <typename T, int NB>
+template <typename T, int NB, class Bar>
 __device__ __noinline__ int solve_pivoted(const T *__restrict__ A, int n,
                                           const T *__restrict__ b, T *__restrict__ x,
-                                          BatchSmem<T, NB> &sm, int i, T eps) {
-  return solve_one<T, NB, 0>(A, n, b, x, sm, i, eps);
+                                          BatchSmem<T, NB> &sm, int i, T eps, Bar bar) {
+  return solve_one<T, NB, 0, Bar>(A, n, b, x, sm, i, eps, bar);
 }
 
-template <typename T, int NB>
+template <typename T, int NB, class Bar = GSync<NB>>
 __device__ int solve_diag_first(const T *__restrict__ A, int n,
                                 const T *__restrict__ b, T *__restrict__ x,
-                                BatchSmem<T, NB> &sm, int i, T eps) {
+                                BatchSmem<T, NB> &sm, int i, T eps, Bar bar = Bar()) {
   const bool act = i < n;
   T a[NB];
   T rb = act ? b[i] : T(0);
@@ -384,7 +399,7 @@ __device__ int solve_diag_first(const T *__restrict__ A, int n,
       put_row<T, NB>(sm.slot[par][0], a, rb, live);
       sm.slot[par][0][2] = T(1) / a[0];  // the pivot's reciprocal, divided once
     }
-    gsync<NB>();
+    bar();
     const T *u = sm.slot[par][0];
     const T piv = u[3];
     // the last column is not searched (mat_plu)
@@ -403,17 +418,17 @@ __device__ int solve_diag_first(const T *__restrict__ A, int n,
   } else {
     const bool wany = __any_sync(0xffffffffu, beaten);
     if ((i & 31) == 0) sm.widx[0][i >> 5] = wany ? 1 : 0;
-    gsync<NB>();
+    bar();
     any = false;
 #pragma unroll
     for (int w = 0; w < Warps<NB>::v; w++) any = any || sm.widx[0][w] != 0;
-    gsync<NB>();  // the flags are read before the next system reuses them
+    bar();  // the flags are read before the next system reuses them
   }
   if (!any) {
     if (act) x[i] = rb / dg;
     return 0;
   }
-  return solve_pivoted<T, NB>(A, n, b, x, sm, i, eps);
+  return solve_pivoted<T, NB, Bar>(A, n, b, x, sm, i, eps, bar);
 }
 
 // ---------------------------------------------------------------------------
@@ -448,10 +463,10 @@ struct SpdSmem {
   T xs[NB];
 };
 
-template <typename T, int NB>
+template <typename T, int NB, class Bar = GSync<NB>>
 __device__ int solve_spd(const T *__restrict__ A, int n,
                          const T *__restrict__ b, T *__restrict__ x,
-                         SpdSmem<T, NB> &sm, int i) {
+                         SpdSmem<T, NB> &sm, int i, Bar bar = Bar()) {
   constexpr int C = Chunk<NB>::v;
   constexpr int W = VecOf<T>::w;
   constexpr int GW = NB < 32 ? NB : 32;  // rows of one warp (half warp)
@@ -473,7 +488,7 @@ __device__ int solve_spd(const T *__restrict__ A, int n,
       myoff = off;
       col[2] = T(1) / a[0];  // the pivot's reciprocal, divided once
     }
-    gsync<NB>();
+    bar();
     const T d = col[3];
     if (d <= T(0)) return -1;  // NaN passes, as in mat_chol
     const T rd = col[2];
@@ -508,7 +523,7 @@ __device__ int solve_spd(const T *__restrict__ A, int n,
       xi = rb * rdg;
       sm.xs[K] = xi;
     }
-    gsync<NB>();
+    bar();
     if (act && i < K) rb = fma(-sm.cols[myoff + 3 + (K - i)], sm.xs[K], rb);
   }
   if (act) x[i] = xi;

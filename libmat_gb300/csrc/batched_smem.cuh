@@ -18,9 +18,10 @@ struct SmemRows {
   T rows[NB][NB + 1];
 };
 
-template <typename T, int NB, int KIND>
+template <typename T, int NB, int KIND, class Bar = CtaBar>
 __device__ int solve_smem(const T *__restrict__ A, int n, const T *__restrict__ b,
-                          T *__restrict__ x, SmemRows<T, NB> &S, int i, T eps) {
+                          T *__restrict__ x, SmemRows<T, NB> &S, int i, T eps,
+                          Bar bar = Bar()) {
   BlkSmem<T, NB> &sm = S.b;
   T *row = S.rows[i];
   const int warp = i >> 5, lane = i & 31;
@@ -48,11 +49,11 @@ __device__ int solve_smem(const T *__restrict__ A, int n, const T *__restrict__ 
 #pragma unroll
       for (int c = 0; c < kBPW; c++) sm.pan[i][c] = c < pw ? row[K0 + c] : T(0);
     }
-    __syncthreads();
+    bar();
     if (warp == 0) {
       if (!blk_panel<T, NB, KIND>(sm, K0, pw, n, eps) && lane == 0) sm.fail = 1;
     }
-    __syncthreads();
+    bar();
     if (KIND == 1 && sm.fail) return -1;
     mylr = sm.lr[i];
     if (mylr >= K0 && mylr < K0 + pw) {
@@ -60,7 +61,7 @@ __device__ int solve_smem(const T *__restrict__ A, int n, const T *__restrict__ 
       for (int j = 0; j < tw; j++) rw[j] = row[K0 + pw + j];
       rw[tw] = rb;
     }
-    __syncthreads();
+    bar();
     if (i <= tw) {
       T u[kBPW];
 #pragma unroll
@@ -91,7 +92,7 @@ __device__ int solve_smem(const T *__restrict__ A, int n, const T *__restrict__ 
       T *col = sm.ucol + ucoff(K0 + c) + K0;
       for (int c2 = 0; c2 <= c; c2++) col[c2] = sm.pan[sm.pv[c2]][c];
     }
-    __syncthreads();
+    bar();
     if (mylr >= K0 + pw) {
       T l[kBPW];
       ld8<T>(&sm.pan[i][0], l);
@@ -111,7 +112,7 @@ __device__ int solve_smem(const T *__restrict__ A, int n, const T *__restrict__ 
       for (int c = 0; c < kBPW; c++) rb = fma(-u[c], l[c], rb);
     }
   }
-  __syncthreads();
+  bar();
   if (warp == 0) {
     constexpr int RPL = NB / 32;
     T s[RPL];
@@ -136,7 +137,7 @@ __device__ int solve_smem(const T *__restrict__ A, int n, const T *__restrict__ 
       }
     }
   }
-  __syncthreads();
+  bar();
   if (act) x[i] = sm.xv[i];
   return 0;
 }

@@ -45,6 +45,7 @@ struct KtScope {
   KtScope(const char *name, double flops, double bytes);
   ~KtScope();
 };
+bool ktime_on();
 
 // Grow-only device buffers keyed by slot, reused across calls (the device
 // counterpart of the reference's scratch arena, mat.h:865-895).

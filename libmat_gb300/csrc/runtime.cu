@@ -356,6 +356,7 @@ struct KtRec {
   double flops, bytes;
 };
 static bool g_kt_on = false;
+bool ktime_on() { return g_kt_on; }
 static std::vector<KtRec> g_kt;
 static std::vector<cudaEvent_t> g_kt_pool;
 

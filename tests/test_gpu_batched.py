@@ -21,22 +21,31 @@ TOL = {"f32": 2e-4, "f64": 1e-11}
 U = {"f32": 2.0 ** -24, "f64": 2.0 ** -53}
 
 
-@pytest.fixture(params=[1, 0], ids=["blocked", "gauss_jordan"])
+@pytest.fixture(params=["fused", "queues_gauss_jordan", "queues_blocked"])
 def algo(request, gpu):
-    """Every large bucket on one algorithm for the test, defaults restored."""
+    """Every schedule: the one persistent launch (replayed as a CUDA graph),
+    or one launch per queue with the large buckets on the register
+    Gauss-Jordan kernel or the blocked LU; defaults restored after."""
+    fused = request.param == "fused"
+    algo_ = 1 if request.param == "queues_blocked" else 0
     saved = {}
     for prec in ("f32", "f64"):
         L = gpu[prec]
+        saved[prec, "fused"] = L.c.matgb_batched_schedule(1 if fused else 0, -1, 1)
         for nb in (64, 96, 128):
             for kind in (0, 1):
                 a, c = C.c_int(), C.c_int()
                 L.check(L.c.matgb_batched_tune_get(nb, kind, C.byref(a), C.byref(c)))
                 saved[prec, nb, kind] = (a.value, c.value)
                 # the double build's 96 and 128 buckets have one form only
-                L.check(L.c.matgb_batched_tune(nb, kind, request.param, c.value))
+                L.check(L.c.matgb_batched_tune(nb, kind, algo_, c.value))
     yield request.param
-    for (prec, nb, kind), (a, c) in saved.items():
-        gpu[prec].c.matgb_batched_tune(nb, kind, a, c)
+    for key, v in saved.items():
+        if key[1] == "fused":
+            gpu[key[0]].c.matgb_batched_schedule(v, -1, -1)
+        else:
+            prec, nb, kind = key
+            gpu[prec].c.matgb_batched_tune(nb, kind, *v)
 
 
 def make_batch(count, nmax, dt, seed):
@@ -116,3 +125,58 @@ def test_batched_marks_unsupported_order(gpu):
                                             np.ones(100, dt)], [0, 1, 0])
         assert list(status) == [-2, 0, 0]
         assert np.allclose(xs[1], 0.25) and np.allclose(xs[2], 0.125)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_batched_graph_replay_same_buffers(gpu, prec):
+    """The one-launch schedule captures its launch sequence in a CUDA graph on
+    the first call with a set of buffers and replays it on later calls with
+    the same buffers: new data in the same buffers must give the new
+    solutions, and other buffers a new capture."""
+    L = gpu[prec]
+    O = Oracle(prec)
+    prev = L.c.matgb_batched_schedule(1, -1, 1)
+    try:
+        count = 200
+        outs = []
+        for seed in (3, 4):
+            mats, rhs, kinds = make_batch(count, 128, L.dtype, seed)
+            ns = np.array([m.shape[0] for m in mats], np.int32)
+            offA = np.zeros(count, np.int64)
+            offA[1:] = np.cumsum(ns.astype(np.int64) ** 2)[:-1]
+            offv = np.zeros(count, np.int64)
+            offv[1:] = np.cumsum(ns.astype(np.int64))[:-1]
+            outs.append((mats, rhs, kinds, ns, offA, offv))
+        # buffers sized for the larger of the two batches, reused by both
+        tot_a = max(sum(m.size for m in o[0]) for o in outs)
+        tot_v = max(sum(v.size for v in o[1]) for o in outs)
+        es = np.dtype(L.dtype).itemsize
+        dn, doA, dov = L.dalloc(4 * count), L.dalloc(8 * count), L.dalloc(8 * count)
+        dA, db, dx = L.dalloc(es * tot_a), L.dalloc(es * tot_v), L.dalloc(es * tot_v)
+        dk, dst = L.dalloc(count), L.dalloc(4 * count)
+        try:
+            for rep in range(3):  # calls 2 and 3 replay the graph of call 1 or 2
+                mats, rhs, kinds, ns, offA, offv = outs[rep % 2]
+                Acat = np.concatenate([m.ravel(order="F") for m in mats])
+                bcat = np.concatenate(rhs)
+                for d, a in ((dn, ns), (doA, offA), (dov, offv), (dA, Acat),
+                             (db, bcat), (dk, np.asarray(kinds, np.uint8))):
+                    L.h2d(d, a)
+                L.check(L.c.matgb_solve_batched_dev(count, dn, doA, dA, dov, db, dx,
+                                                    dk, dst), "batched")
+                x = np.empty_like(bcat)
+                L.d2h(x, dx)
+                st = np.empty(count, np.int32)
+                L.d2h(st, dst)
+                assert np.all(st == 0)
+                for s in range(0, count, 7):
+                    n = ns[s]
+                    xs = x[offv[s]:offv[s] + n]
+                    xr = O.solve(mats[s], rhs[s]) if kinds[s] == 0 else \
+                        O.solve_spd(mats[s], rhs[s])[0]
+                    assert np.abs(xs - xr).max() / np.abs(xr).max() <= TOL[prec]
+        finally:
+            for d in (dn, doA, dov, dA, db, dx, dk, dst):
+                L.dfree(d)
+    finally:
+        L.c.matgb_batched_schedule(prev, -1, -1)
