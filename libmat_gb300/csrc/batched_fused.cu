@@ -32,31 +32,31 @@ struct FusedState {
   unsigned arrive;           // grid barrier arrivals
 };
 
+// One group's shared memory: a general or an SPD system (the groups of a
+// phase run side by side, each on either kind, so each needs its own slot).
+template <typename T, int NB>
+union GroupSmem {
+  BatchSmem<T, NB> lu;
+  SpdSmem<T, NB> spd;
+};
+
 #ifdef MAT_DOUBLE_PRECISION
 template <typename T>
 union FusedSmem {
   SmemRows<T, 128> big;
-  BatchSmem<T, 64> lu64[2];
-  SpdSmem<T, 64> spd64[2];
-  BatchSmem<T, 32> lu32[4];
-  SpdSmem<T, 32> spd32[4];
-  BatchSmem<T, 16> lu16[8];
-  SpdSmem<T, 16> spd16[8];
+  GroupSmem<T, 64> g64[2];
+  GroupSmem<T, 32> g32[4];
+  GroupSmem<T, 16> g16[8];
 };
 constexpr int kFusedMinB = 1;
 #else
 template <typename T>
 union FusedSmem {
-  BatchSmem<T, 128> lu128;
-  SpdSmem<T, 128> spd128;
-  BatchSmem<T, 96> lu96;
-  SpdSmem<T, 96> spd96;
-  BatchSmem<T, 64> lu64[2];
-  SpdSmem<T, 64> spd64[2];
-  BatchSmem<T, 32> lu32[4];
-  SpdSmem<T, 32> spd32[4];
-  BatchSmem<T, 16> lu16[8];
-  SpdSmem<T, 16> spd16[8];
+  GroupSmem<T, 128> g128;
+  GroupSmem<T, 96> g96;
+  GroupSmem<T, 64> g64[2];
+  GroupSmem<T, 32> g32[4];
+  GroupSmem<T, 16> g16[8];
 };
 constexpr int kFusedMinB = 3;  // the 128-row register frame: 170 registers
 #endif
@@ -164,9 +164,9 @@ __global__ void __launch_bounds__(kFusedThreads, kFusedMinB)
       r = solve_smem<T, 128, 0>(A + offA[s], n, b + offv[s], x + offv[s], sm.big, tid, eps);
 #else
     if (qi & 1)
-      r = solve_spd<T, 128>(A + offA[s], n, b + offv[s], x + offv[s], sm.spd128, tid);
+      r = solve_spd<T, 128>(A + offA[s], n, b + offv[s], x + offv[s], sm.g128.spd, tid);
     else
-      r = solve_diag_first<T, 128>(A + offA[s], n, b + offv[s], x + offv[s], sm.lu128,
+      r = solve_diag_first<T, 128>(A + offA[s], n, b + offv[s], x + offv[s], sm.g128.lu,
                                    tid, eps);
 #endif
     if (tid == 0) status[s] = r;
@@ -187,9 +187,9 @@ __global__ void __launch_bounds__(kFusedThreads, kFusedMinB)
       const int n = nvec[s];
       int r;
       if (qi & 1)
-        r = solve_spd<T, 96>(A + offA[s], n, b + offv[s], x + offv[s], sm.spd96, tid, bar);
+        r = solve_spd<T, 96>(A + offA[s], n, b + offv[s], x + offv[s], sm.g96.spd, tid, bar);
       else
-        r = solve_diag_first<T, 96>(A + offA[s], n, b + offv[s], x + offv[s], sm.lu96,
+        r = solve_diag_first<T, 96>(A + offA[s], n, b + offv[s], x + offv[s], sm.g96.lu,
                                     tid, eps, bar);
       if (tid == 0) status[s] = r;
       bar();
@@ -211,9 +211,9 @@ __global__ void __launch_bounds__(kFusedThreads, kFusedMinB)
       const int n = nvec[s];
       int r;
       if (qi & 1)
-        r = solve_spd<T, 64>(A + offA[s], n, b + offv[s], x + offv[s], sm.spd64[g], i, bar);
+        r = solve_spd<T, 64>(A + offA[s], n, b + offv[s], x + offv[s], sm.g64[g].spd, i, bar);
       else
-        r = solve_diag_first<T, 64>(A + offA[s], n, b + offv[s], x + offv[s], sm.lu64[g],
+        r = solve_diag_first<T, 64>(A + offA[s], n, b + offv[s], x + offv[s], sm.g64[g].lu,
                                     i, eps, bar);
       if (i == 0) status[s] = r;
       bar();
@@ -233,9 +233,9 @@ __global__ void __launch_bounds__(kFusedThreads, kFusedMinB)
       const int n = nvec[s];
       int r;
       if (qi & 1)
-        r = solve_spd<T, 32>(A + offA[s], n, b + offv[s], x + offv[s], sm.spd32[g], i);
+        r = solve_spd<T, 32>(A + offA[s], n, b + offv[s], x + offv[s], sm.g32[g].spd, i);
       else
-        r = solve_diag_first<T, 32>(A + offA[s], n, b + offv[s], x + offv[s], sm.lu32[g],
+        r = solve_diag_first<T, 32>(A + offA[s], n, b + offv[s], x + offv[s], sm.g32[g].lu,
                                     i, eps);
       if (i == 0) status[s] = r;
       __syncwarp();
@@ -256,9 +256,9 @@ __global__ void __launch_bounds__(kFusedThreads, kFusedMinB)
       const int n = nvec[s];
       int r;
       if (qi & 1)
-        r = solve_spd<T, 16>(A + offA[s], n, b + offv[s], x + offv[s], sm.spd16[g], i);
+        r = solve_spd<T, 16>(A + offA[s], n, b + offv[s], x + offv[s], sm.g16[g].spd, i);
       else
-        r = solve_diag_first<T, 16>(A + offA[s], n, b + offv[s], x + offv[s], sm.lu16[g],
+        r = solve_diag_first<T, 16>(A + offA[s], n, b + offv[s], x + offv[s], sm.g16[g].lu,
                                     i, eps);
       if (i == 0) status[s] = r;
       __syncwarp(gm);

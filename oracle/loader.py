@@ -44,7 +44,43 @@ def build(ref=None):
 def _path(prec, kind):
     if kind == "port":
         return os.path.join(HERE, "build", f"liboracle_{prec}.so")
+    if kind == "neon":
+        return os.path.join(HERE, "build", f"libneon_{prec}.so")
     return os.path.join(HERE, "_ref", f"libref_{prec}.so")
+
+
+class NeonPort:
+    """The reference's NEON-path mat_solve restated (oracle/neon_port.c),
+    double only: the CPU baseline on hosts without the reference source.
+    On aarch64 it runs the NEON micro-kernel (arch() == "NEON")."""
+
+    def __init__(self):
+        path = _path("f64", "neon")
+        if not os.path.exists(path):
+            build()
+        self.lib = C.CDLL(path, mode=C.RTLD_LOCAL)
+        self.lib.np_arch.restype = C.c_char_p
+        self.lib.np_plu_inplace.restype = C.c_int
+
+    def arch(self):
+        return self.lib.np_arch().decode()
+
+    def solve(self, A, b):
+        A = np.asfortranarray(A, dtype=np.float64)
+        b = np.ascontiguousarray(np.asarray(b, np.float64).reshape(-1))
+        x = np.zeros(A.shape[0])
+        self.lib.np_solve(x.ctypes.data_as(C.c_void_p), A.ctypes.data_as(C.c_void_p),
+                          b.ctypes.data_as(C.c_void_p), C.c_size_t(A.shape[0]))
+        return x
+
+    def plu(self, A):
+        """(packed LU, perm, swaps)."""
+        M = np.array(A, dtype=np.float64, order="F", copy=True)
+        n = M.shape[0]
+        p = np.zeros(n, np.uint64)
+        s = self.lib.np_plu_inplace(M.ctypes.data_as(C.c_void_p), C.c_size_t(n),
+                                    p.ctypes.data_as(C.c_void_p))
+        return M, p.astype(np.int64), int(s)
 
 
 def available(prec="f32", kind="port"):
