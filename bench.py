@@ -19,8 +19,9 @@ solve, 2n^3/3 + 2n^2 FLOP.  Every step's backward error is checked.
 Reported beside it: the plain FP64 GPU LU solve of the same system (the
 baseline the mixed solver must beat by 3x), the tensor-core rank-K update's
 roofline (achieved TFLOP/s over the measured BF16 peak), an end-to-end figure
-through mat_solve_ir with pinned host buffers, the reference's algorithm on
-one host core (oracle port, f64, at reduced n), and secondary workloads: the
+through mat_solve_ir with pinned host buffers, the reference's CPU algorithm
+on one pinned host core (its NEON path restated, f64, at reduced n), and
+secondary workloads: the
 plain float32 GEMM and PLU solve at 8192, the SPD solve at 16384 with 64
 right-hand sides, and 100,000 batched uneven solves.
 
@@ -30,9 +31,11 @@ condition numbers hold to that relative accuracy); PyTorch is only the
 harness here, the solves run in libmatgb.  Torch tensors are row-major, so
 the library (column-major) sees A^T, which has the same singular values.
 
-Prints ONE JSON line.  --impl reference times the reference's algorithm on
-the host cores instead (the oracle port: the reference's own source is not
-present where this runs), on a bounded sample of the same workload.
+Prints ONE JSON line.  --impl reference times the reference's CPU algorithm
+for the solve instead -- its NEON-path mat_solve restated (oracle/
+neon_port.c; the reference's own source is not present where this runs) --
+single-threaded on one pinned host core, on a bounded sample of the same
+workload (one solve of the largest order that fits the arm's time).
 """
 import argparse
 import ctypes as C
@@ -770,67 +773,122 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
 
 
 # ----------------------------------------------------------------- CPU legs
-def cpu_sample(n=1024, budget_s=12.0):
-    """The reference's mat_solve (plain PLU + triangular solves) in double,
-    oracle port on one core, on an n x n N(0,1) sample.  TFLOP/s."""
-    from oracle.loader import Oracle
+# The reference's own CPU path for the headline's solve (mat_solve in double)
+# is timed through oracle/neon_port.c: the reference's NEON-path algorithm
+# restated (blocked PLU with its packed 8 x 4 GEMM micro-kernel), which takes
+# the NEON micro-kernel on the GPU host's Grace cores.  The reference's own
+# source is not present on that host, so its build cannot run there.  One
+# pinned core, as the reference is single-threaded.
+
+
+def _pin_one_core():
+    cpus = sorted(os.sched_getaffinity(0))
+    core = cpus[-1]
+    os.sched_setaffinity(0, {core})
+    return core
+
+
+def _neon_worker(n_list, budget_s, seed, q):
+    """In a fresh process pinned to one core: time the NEON-path mat_solve
+    at the largest order in n_list that finishes within budget_s, return
+    (n, seconds per solve, solves, arch, core)."""
+    core = _pin_one_core()
+    from oracle.loader import NeonPort
     from libmat_gb300 import rng
-    O = Oracle("f64", "port")
-    A = rng.normal(1001, (n, n), np.float64)
-    b = rng.normal(2001, (n,), np.float64)
-    flops = 2 * n ** 3 / 3 + 2 * n * n
+    N = NeonPort()
+    # calibrate on the smallest order
+    n0 = n_list[0]
+    A = rng.normal(seed, (n0, n0), np.float64)
+    b = rng.normal(seed + 1, (n0,), np.float64)
+    t0 = time.perf_counter()
+    N.solve(A, b)
+    t_n0 = time.perf_counter() - t0
+    n = n0
+    for cand in n_list:
+        if t_n0 * (cand / n0) ** 3 * 3 <= budget_s:
+            n = cand
+    A = rng.normal(seed + 2, (n, n), np.float64)
+    b = rng.normal(seed + 3, (n,), np.float64)
     reps, t0 = 0, time.perf_counter()
     while True:
-        O.solve(A, b)
+        N.solve(A, b)
         reps += 1
         el = time.perf_counter() - t0
-        if el > budget_s or reps >= 50:
+        if el > budget_s * 0.5 or reps >= 20:
             break
-    return flops * reps / el / 1e12, el / reps
+    q.put((n, el / reps, reps, N.arch(), core))
 
 
-def _ref_worker(args):
-    n, seed = args
-    from oracle.loader import Oracle
-    from libmat_gb300 import rng
-    O = Oracle("f64", "port")
-    A = rng.normal(seed, (n, n), np.float64)
-    b = rng.normal(seed + 1, (n,), np.float64)
-    O.solve(A, b)
-    return 1
+def neon_sample(n_list=(1024, 2048, 3072, 4096), budget_s=20.0, seed=1001):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    p = ctx.Process(target=_neon_worker, args=(n_list, budget_s, seed, q))
+    p.start()
+    out = q.get(timeout=budget_s * 10 + 120)
+    p.join()
+    return out
+
+
+def cpu_sample():
+    """The reference's mat_solve (NEON path restated) in double on one pinned
+    host core, at the largest order that fits a ~20 s budget.  TFLOP/s."""
+    n, per, reps, arch, core = neon_sample()
+    flops = 2 * n ** 3 / 3 + 2 * n * n
+    return {"value": flops / per / 1e12, "unit": "TFLOP/s", "cores": 1,
+            "kind": "port",
+            "sample": f"reference mat_solve algorithm (NEON path: blocked PLU "
+                      f"with the packed 8x4 micro-kernel, restated in "
+                      f"oracle/neon_port.c) in f64 at n={n}, {reps} solves, "
+                      f"{per:.2f} s per solve, core {core} pinned",
+            "mat_arch": arch}
 
 
 def run_reference(args):
-    """Reference arm: the reference's algorithm (oracle port of mat_solve in
-    double) on all host cores, one independent n x n solve per core per
-    step."""
+    """Reference arm: the reference's CPU algorithm for the headline solve
+    (mat_solve in double, NEON path restated), single-threaded on one pinned
+    host core as the reference runs; each step one solve at the largest order
+    whose warm-up + timed steps fit about two minutes."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import multiprocessing as mp
-    cores = os.cpu_count() or 1
-    n = 1024
+    core = _pin_one_core()
+    from oracle.loader import NeonPort
+    from libmat_gb300 import rng
+    N = NeonPort()
+    total = max(1, args.steps + args.warmup)
+    n0 = 1024
+    A = rng.normal(7, (n0, n0), np.float64)
+    b = rng.normal(8, (n0,), np.float64)
+    t0 = time.perf_counter()
+    N.solve(A, b)
+    t_n0 = time.perf_counter() - t0
+    n = n0
+    for cand in (1024, 1536, 2048, 3072, 4096, 6144, 8192):
+        if t_n0 * (cand / n0) ** 3 * total <= 120.0:
+            n = cand
     flops = 2 * n ** 3 / 3 + 2 * n * n
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        for i in range(args.warmup):
-            pool.map(_ref_worker, [(n, 100 + i * cores + j) for j in range(cores)])
-        t0 = time.perf_counter()
-        for i in range(args.steps):
-            pool.map(_ref_worker, [(n, 5000 + i * cores + j) for j in range(cores)])
-        el = time.perf_counter() - t0
-    tf = flops * cores * args.steps / el / 1e12
+    for i in range(args.warmup):
+        N.solve(rng.normal(100 + i, (n, n), np.float64),
+                rng.normal(200 + i, (n,), np.float64))
+    mats = [(rng.normal(5000 + i, (n, n), np.float64),
+             rng.normal(6000 + i, (n,), np.float64)) for i in range(min(args.steps, 3))]
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        A, b = mats[i % len(mats)]
+        N.solve(A, b)
+    el = time.perf_counter() - t0
+    tf = flops * args.steps / el / 1e12
+    sample = (f"one f64 solve of n={n} per step (the reference's mat_solve, "
+              f"NEON path restated in oracle/neon_port.c), core {core} pinned")
     line = {
         "impl": "reference", "metric": METRIC, "value": tf, "unit": "TFLOP/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "mixed_lu_ir_16384_f64",
-                   "sample": f"{cores} independent f64 solves of n={n} per step "
-                             "(reference's plain LU solve, bounded sample)"},
-        "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": cores,
-                         "kind": "port",
-                         "sample": f"n={n} f64 N(0,1), 1 RHS, {cores} processes"},
+        "config": {"workload": "mixed_lu_ir_16384_f64", "sample": sample},
+        "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": 1,
+                         "kind": "port", "sample": sample, "mat_arch": N.arch()},
         "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -909,10 +967,7 @@ def main():
                      "blas_t": run_blas_t(mg)}
     cpu = None
     if not args.no_cpu:
-        v, per = cpu_sample()
-        cpu = {"value": v, "unit": "TFLOP/s", "cores": 1, "kind": "port",
-               "sample": f"reference mat_solve algorithm in f64 at n=1024, "
-                         f"{per:.2f} s per solve"}
+        cpu = cpu_sample()
     line = {"metric": METRIC, "value": res["value"], "unit": res["unit"],
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": res["ms_per_step"], "higher_is_better": True,
