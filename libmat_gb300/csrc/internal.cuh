@@ -36,6 +36,10 @@ void fail_void(const char *where);
 
 // Host-side launch accounting + launch-error check.
 int launched(const char *name);
+// The counter itself (a CUDA graph replay adds its kernels by hand; a
+// capture, which launches nothing, is taken back out).
+unsigned long long launch_counter();
+void launch_counter_set(unsigned long long v);
 
 // Optional per-kernel timing (matgb_ktime_enable): a scope records CUDA events
 // on the library stream around one launch and tags it with the launch's

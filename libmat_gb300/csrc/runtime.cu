@@ -86,6 +86,9 @@ int launch_check(const void *func, const char *name, size_t smem) {
                    fa.sharedSizeBytes, fa.numRegs, cudaGetErrorString(e2));
 }
 
+unsigned long long launch_counter() { return g_launches.load(); }
+void launch_counter_set(unsigned long long v) { g_launches.store(v); }
+
 int launched(const char *name) {
   g_launches.fetch_add(1, std::memory_order_relaxed);
   cudaError_t e = cudaGetLastError();
