@@ -158,3 +158,47 @@ def test_report_struct_layout_matches_ctypes(tmp_path):
         assert int(got[name]) == C.sizeof(st), name
         for f, _ in st._fields_:
             assert int(got[f"{name}.{f}"]) == getattr(st, f).offset, (name, f)
+
+
+def test_batched_schedule_file_is_read(tmp_path):
+    """The batched solver's schedule table comes from the tuner's JSON file
+    (read at the first batched call; no device needed): entries for this
+    build override the defaults, entries for the other precision and
+    malformed ones are skipped; the committed table parses."""
+    import json
+    import sys
+    doc = {"fused": 1, "fused_ctas_per_sm": 2, "entries": [
+        {"prec": "f32", "nb": 96, "kind": 1, "algo": 1, "ctas_per_sm": 3},
+        {"prec": "f64", "nb": 96, "kind": 1, "algo": 0, "ctas_per_sm": 5},
+        {"prec": "f32", "nb": 16, "kind": 0, "algo": 1, "ctas_per_sm": 2},
+        {"nb": 32, "kind": 0}]}
+    f = tmp_path / "tune.json"
+    f.write_text(json.dumps(doc))
+    code = (
+        "import ctypes as C, sys; sys.path.insert(0, %r)\n"
+        "import libmat_gb300 as mg\n"
+        "L = mg.load('f32'); a, c = C.c_int(), C.c_int()\n"
+        "assert L.c.matgb_batched_tune_get(96, 1, C.byref(a), C.byref(c)) == 0\n"
+        "print(a.value, c.value)\n"
+        "assert L.c.matgb_batched_tune_get(16, 0, C.byref(a), C.byref(c)) == 0\n"
+        "print(a.value, c.value)\n"
+        "print(L.c.matgb_batched_schedule(-1, -1, -1))\n"
+        "print(L.c.matgb_batched_tune_source().decode())\n") % ROOT
+    env = dict(os.environ, LIBMATGB_BATCHED_TUNE=str(f))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True,
+                       text=True, env=env)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout.split("\n")
+    assert out[0] == "1 3"   # the f32 entry for (96, SPD)
+    assert out[1] == "0 0"   # blocked form refused below order 64
+    assert out[2] == "1"     # fused schedule chosen by the file
+    assert "tune.json (1 entries)" in out[3]
+    # the committed table
+    env = dict(os.environ)
+    env.pop("LIBMATGB_BATCHED_TUNE", None)
+    r = subprocess.run([sys.executable, "-c", code.replace(
+        "assert L.c.matgb_batched_tune_get(96, 1, C.byref(a), C.byref(c)) == 0\n", "").replace(
+        "assert L.c.matgb_batched_tune_get(16, 0, C.byref(a), C.byref(c)) == 0\n", "")],
+        capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stderr
+    assert "batched_tune.json (10 entries)" in r.stdout
