@@ -40,7 +40,16 @@ namespace mgb {
 constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 64;
 constexpr int kTcThreads = 320;
 constexpr uint32_t kTcWaitLimit = 1u << 24;  // ~1.5 s of polling
-constexpr uint32_t kTcSpin = 256;  // producer / MMA polls before sleeping
+// producer / MMA polls before sleeping, and whether the epilogue pulls its C
+// region towards L2 during the main loop (build-time overrides for
+// measurement: -DMGB_TC_SPIN=n, -DMGB_TC_PREFETCH=0)
+#ifndef MGB_TC_SPIN
+#define MGB_TC_SPIN 256
+#endif
+#ifndef MGB_TC_PREFETCH
+#define MGB_TC_PREFETCH 1
+#endif
+constexpr uint32_t kTcSpin = MGB_TC_SPIN;
 // K blocks per launch (all segments): bounds one CTA's main loop (3 x 16384
 // columns of K, ~0.3 ms on one SM), far inside the wait limit; longer sums
 // are split by the caller
@@ -178,6 +187,21 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
         d[j] = (rok && rd && cbase + col < N) ? cp[(int64_t)col * ldc] : 0.f;
       }
     };
+    // Pull this warp's whole C region (32 rows x 128 columns, one 128-byte
+    // line per column) towards L2 while the MMAs run, so the chunk loads
+    // below find it there: the DRAM reads of C overlap the main loop
+    // instead of the epilogue.
+    if (MGB_TC_PREFETCH && rd) {
+      const int row0 = m0 + q * 32;
+      if (row0 < M) {
+        const float *c0 = C + (int64_t)cbase * ldc + row0;
+#pragma unroll
+        for (int j = lane; j < kTcBN / 2; j += 32)
+          if (cbase + j < N && (tri != 1 || cbase + j <= row0 + 31) &&
+              (tri != 2 || cbase + j >= row0))
+            tc::prefetch_l2(c0 + (int64_t)j * ldc);
+      }
+    }
     float cur[CH];
     load(cur, 0);
     const float rs = (rinv && rok) ? __ldg(&rinv[row]) : 1.f;

@@ -75,6 +75,11 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map,
       : "memory");
 }
 
+// Bring the line holding p towards the L2 cache (no register written).
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map))
                : "memory");
