@@ -42,12 +42,15 @@ constexpr int kTcThreads = 320;
 constexpr uint32_t kTcWaitLimit = 1u << 24;  // ~1.5 s of polling
 // producer / MMA polls before sleeping, and whether the epilogue pulls its C
 // region towards L2 during the main loop (build-time overrides for
-// measurement: -DMGB_TC_SPIN=n, -DMGB_TC_PREFETCH=0)
+// measurement: -DMGB_TC_SPIN=n, -DMGB_TC_PREFETCH=1).  Measured on the split
+// update at 16000 x 15856 x 192: 0.574 ms spinning, 0.579 ms sleeping from
+// the first poll; the L2 prefetch took it to 0.588 ms (the chunked loads
+// already overlap the other CTA's main loop), so it is off.
 #ifndef MGB_TC_SPIN
 #define MGB_TC_SPIN 256
 #endif
 #ifndef MGB_TC_PREFETCH
-#define MGB_TC_PREFETCH 1
+#define MGB_TC_PREFETCH 0
 #endif
 constexpr uint32_t kTcSpin = MGB_TC_SPIN;
 // K blocks per launch (all segments): bounds one CTA's main loop (3 x 16384
@@ -76,7 +79,7 @@ struct TcSmem {
 // col <= row); 2 upper (col >= row).  rinv / cinv (may be null): per-row and
 // per-column power-of-two factors applied to the accumulator before alpha
 // (the inverses of the operands' packing scales; exact).
-template <int ST, int MINB>
+template <int ST, int MINB, bool SC>
 __global__ void __launch_bounds__(kTcThreads, MINB)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0,
                    const __grid_constant__ CUtensorMap tmA1,
@@ -204,7 +207,8 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
     }
     float cur[CH];
     load(cur, 0);
-    const float rs = (rinv && rok) ? __ldg(&rinv[row]) : 1.f;
+    float rs = 1.f;
+    if constexpr (SC) rs = rok ? __ldg(&rinv[row]) : 1.f;
     const bool ready = tc::mbar_wait(&s.done, 0, kTcWaitLimit);
     tc::tc_fence_after();
     if (ready && !s.timeout) {
@@ -214,10 +218,12 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
         float nxt[CH];
         if (ch + 1 < NCH) load(nxt, ch + 1);
         float cs[CH];
+        if constexpr (SC) {
 #pragma unroll
-        for (int j = 0; j < CH; j++) {
-          const int col = cbase + ch * CH + j;
-          cs[j] = (cinv && col < N) ? __ldg(&cinv[col]) : 1.f;
+          for (int j = 0; j < CH; j++) {
+            const int col = cbase + ch * CH + j;
+            cs[j] = col < N ? __ldg(&cinv[col]) : 1.f;
+          }
         }
         float v[CH];
         tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) +
@@ -229,8 +235,12 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
             const int col = ch * CH + j;
             const bool in = tri == 0 || (tri == 1 ? cbase + col <= row
                                                    : cbase + col >= row);
-            if (cbase + col < N && in)
-              cp[(int64_t)col * ldc] = fmaf(al, (v[j] * rs) * cs[j], beta * cur[j]);
+            if (cbase + col < N && in) {
+              if constexpr (SC)
+                cp[(int64_t)col * ldc] = fmaf(al, (v[j] * rs) * cs[j], beta * cur[j]);
+              else
+                cp[(int64_t)col * ldc] = fmaf(al, v[j], beta * cur[j]);
+            }
           }
         }
         if (ch + 1 < NCH) {
@@ -256,7 +266,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 static int *g_tc_err = nullptr;
 static bool g_tc_ready = false;
 
-template <int ST, int MINB>
+template <int ST>
 static constexpr size_t tc_smem_bytes() {
   return sizeof(TcSmem<ST>) + 1024;
 }
@@ -272,12 +282,18 @@ static int tc_setup() {
   g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
   MGB_CUDA(cudaMalloc(&g_tc_err, sizeof(int)));
   MGB_CUDA(cudaMemset(g_tc_err, 0, sizeof(int)));
-  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<2, 2>,
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<2, 2, false>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)tc_smem_bytes<2, 2>()));
-  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<4, 1>,
+                                (int)tc_smem_bytes<2>()));
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<2, 2, true>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)tc_smem_bytes<4, 1>()));
+                                (int)tc_smem_bytes<2>()));
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<4, 1, false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tc_smem_bytes<4>()));
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<4, 1, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tc_smem_bytes<4>()));
   g_tc_ready = true;
   return 0;
 }
@@ -340,16 +356,23 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
   KtScope kt(nm, 2.0 * M * N * K * frac * nseg,
              4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N * frac +
                  2.0 * (M + N) * K * (split ? 2 : 1));
-  if (deep)
-    tc_gemm_kernel<4, 1><<<grid, kTcThreads, tc_smem_bytes<4, 1>(), cx->stream>>>(
-        ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,
-        alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv,
-        g_tc_err);
+  if ((rinv == nullptr) != (cinv == nullptr))
+    return set_error(MATGB_ERR_ARG, "tc_gemm: row and column scales go together");
+  const bool sc = rinv != nullptr;
+#define MGB_TC_LAUNCH(ST_, MB_, SC_)                                           \
+  tc_gemm_kernel<ST_, MB_, SC_><<<grid, kTcThreads, tc_smem_bytes<ST_>(),      \
+                                  cx->stream>>>(                               \
+      ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,  \
+      alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv, g_tc_err)
+  if (deep && sc)
+    MGB_TC_LAUNCH(4, 1, true);
+  else if (deep)
+    MGB_TC_LAUNCH(4, 1, false);
+  else if (sc)
+    MGB_TC_LAUNCH(2, 2, true);
   else
-    tc_gemm_kernel<2, 2><<<grid, kTcThreads, tc_smem_bytes<2, 2>(), cx->stream>>>(
-        ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,
-        alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv,
-        g_tc_err);
+    MGB_TC_LAUNCH(2, 2, false);
+#undef MGB_TC_LAUNCH
   MGB_LAUNCHED("tc_gemm");
   return 0;
 }
