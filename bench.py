@@ -644,6 +644,41 @@ def run_lu_full(mg, steps=3, warmup=3):
     return out
 
 
+def run_qr(mg, steps=3, warmup=2):
+    """mat_qr's device form (Householder, blocked WY) on square 4096 and tall
+    8192 x 2048 matrices, float and double, R and Q (m x m).  FLOPs: LAPACK's
+    counts, 2mn^2 - 2n^3/3 for the factorisation and 4m^2n - 4mn^2 + 4n^3/3
+    for the explicit Q."""
+    out = {}
+    for prec, m, n in (("f32", 4096, 4096), ("f32", 8192, 2048), ("f64", 4096, 4096)):
+        L = mg.load(prec)
+        c = L.c
+        es = 4 if prec == "f32" else 8
+        dA0, dR, dQ = L.dalloc(m * n * es), L.dalloc(m * n * es), L.dalloc(m * m * es)
+        L.check(c.matgb_fill_normal_dev(dA0, m * n, 4001), "fill")
+
+        def one():
+            L.check(c.matgb_memcpy_d2d(dR, dA0, m * n * es), "d2d")
+            L.check(c.matgb_qr_dev(m, n, dR, m, dQ, m), "qr")
+        for _ in range(warmup):
+            one()
+        tot = 0.0
+        for _ in range(steps):
+            L.check(c.matgb_memcpy_d2d(dR, dA0, m * n * es), "d2d")
+            L.sync()
+            L.check(c.matgb_event_record(0), "ev")
+            L.check(c.matgb_qr_dev(m, n, dR, m, dQ, m), "qr")
+            L.check(c.matgb_event_record(1), "ev")
+            L.sync()
+            tot += c.matgb_event_elapsed_ms(0, 1)
+        ms = tot / steps
+        fl = 2 * m * n * n - 2 * n ** 3 / 3 + 4 * m * m * n - 4 * m * n * n + 4 * n ** 3 / 3
+        out[f"{prec}_{m}x{n}"] = {"ms": ms, "tflops": fl / (ms * 1e-3) / 1e12}
+        for d in (dA0, dR, dQ):
+            L.dfree(d)
+    return out
+
+
 def run_blas_t(mg, steps=5, warmup=3):
     """mat_gemv_t's device form on a 16384 x 16384 f32 matrix (1.07 GB) and
     on a 4M x 64 one (row chunks), and AXPY over 2^28 f32 entries: HBM-bound,
@@ -906,7 +941,8 @@ def main():
                     help="2 FP16 split (3 products), 0 FP16, 1 BF16, -1 FP32")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--only", choices=["plain_f32", "spd", "batched", "lu_full", "blas_t"],
+    ap.add_argument("--only", choices=["plain_f32", "spd", "batched", "lu_full", "blas_t",
+                                       "qr"],
                     help="run one secondary workload alone and print its JSON "
                          "(small cases for profiling)")
     ap.add_argument("--count", type=int, default=100000,
@@ -932,6 +968,8 @@ def main():
             out = run_blas_t(mg, steps=args.steps, warmup=args.warmup)
         elif args.only == "lu_full":
             out = run_lu_full(mg, steps=args.steps, warmup=args.warmup)
+        elif args.only == "qr":
+            out = run_qr(mg, steps=args.steps, warmup=args.warmup)
         else:
             out = run_batched(mg, count=args.count, steps=args.steps,
                               warmup=args.warmup)
@@ -964,7 +1002,7 @@ def main():
     if not args.no_secondary:
         secondary = {"plain_f32": run_plain_f32(mg), "spd": run_spd(mg),
                      "batched": run_batched(mg), "lu_full": run_lu_full(mg),
-                     "blas_t": run_blas_t(mg)}
+                     "qr": run_qr(mg), "blas_t": run_blas_t(mg)}
     cpu = None
     if not args.no_cpu:
         cpu = cpu_sample()

@@ -158,13 +158,17 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
             int lower, const int32_t *skip, const void *Alo = nullptr,
             const void *Blo = nullptr, const float *rinv = nullptr,
-            const float *cinv = nullptr);
+            const float *cinv = nullptr, const void *Amid = nullptr,
+            const void *Bmid = nullptr);
 // FP32-accurate float GEMM / SYRK on the tensor cores (tc_sgemm.cu): op(A)
 // and op(B) packed to FP16 hi + remainder under per-row / per-column
 // power-of-two scales, three products per update; tri as tc_gemm's lower.
+// parts 3: hi + mid + remainder, six products (about 33 bits of each
+// operand: the FP32 products' own rounding is then the larger error).
 int tc_sgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, float alpha,
              const float *A, int64_t lda, const float *B, int64_t ldb,
-             float beta, float *C, int64_t ldc, int tri, bool same_ab = false);
+             float beta, float *C, int64_t ldc, int tri, bool same_ab = false,
+             int parts = 2);
 // Whether the plain float paths (GEMM, SYRK, Cholesky) use the tensor cores
 // (matgb_plain_tensor_core), and the size from which they do.
 bool plain_tc_on();

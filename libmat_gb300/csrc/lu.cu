@@ -1743,6 +1743,15 @@ static int trailing_update(int64_t n, T *A, int64_t lda, int64_t kb,
     return gemm_skip_t<T>(false, false, n - ke, c1 - c0, ke - kb, T(-1),
                           A + ke + kb * lda, lda, A + kb + c0 * lda, lda, T(1),
                           A + ke + c0 * lda, lda, 0, nullptr);
+  if (lp == 3) {
+    // the plain float LU: the three-part split (about 33 bits of each
+    // operand), per-row / per-column scales (tc_sgemm.cu)
+    if (sizeof(T) != 4) return set_error(MATGB_ERR_ARG, "tensor-core LU is float");
+    return tc_sgemm(false, false, n - ke, c1 - c0, ke - kb, -1.f,
+                    (const float *)(A + ke + kb * lda), lda,
+                    (const float *)(A + kb + c0 * lda), lda, 1.f,
+                    (float *)(A + ke + c0 * lda), lda, 0, false, 3);
+  }
   if (sizeof(T) != 4) return set_error(MATGB_ERR_ARG, "tensor-core LU is float");
   return lp_trailing_update(n, (float *)A, lda, kb, ke, c0, c1, lp, first, amax3,
                             l21_ready, u12_ready);
@@ -1924,15 +1933,18 @@ int laswp(elem_t *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2,
   return laswp_t<elem_t>(A, lda, c0, c1, c2, c3, ipiv, k1, k2, nullptr);
 }
 
-// The plain LU (mat_plu, mat_solve, matgb_getrf_dev) keeps its trailing
-// updates in the element type (SIMT GEMM): the pivot sequence must follow the
-// reference's on every data-determined step, and the three-product FP16
-// split (about 22 bits per operand) is noisier than FP32 -- on the 8192
-// N(0,1) plain config it changed a pivot at step 6370, where FP32 updates
-// follow the reference up to step 8116, the first step at which the
-// reference's own float and double pivots part.
+// The plain LU (mat_plu, mat_solve, matgb_getrf_dev): the pivot sequence
+// must follow the reference's on every data-determined step.  The
+// three-product FP16 split (about 22 bits per operand) is noisier than FP32
+// -- on the 8192 N(0,1) plain config it changed a pivot at step 6370, where
+// FP32 updates follow the reference up to step 8116, the first step at which
+// the reference's own float and double pivots part.  The float build's
+// orders from 1024 up therefore take the six-product three-part split (about
+// 33 bits per operand, more accurate than the FP32 products it replaces)
+// unless matgb_plain_tensor_core(0) chose the SIMT GEMM.
 int getrf(int64_t n, elem_t *A, int64_t lda, int32_t *ipiv, int32_t *perm) {
-  return getrf_t<elem_t>(n, A, lda, ipiv, perm, kPivotEps, -1);
+  const int lp = (sizeof(elem_t) == 4 && plain_tc_on() && n >= kPlainTcMinN) ? 3 : -1;
+  return getrf_t<elem_t>(n, A, lda, ipiv, perm, kPivotEps, lp);
 }
 
 int getrs(int64_t n, int64_t nrhs, const elem_t *LU, int64_t lda,

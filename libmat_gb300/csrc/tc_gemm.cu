@@ -32,6 +32,8 @@
 // flight, still frees its TMEM and returns.
 #include <cudaTypedefs.h>
 
+#include <initializer_list>
+
 #include "internal.cuh"
 #include "tc_ptx.cuh"
 
@@ -58,9 +60,10 @@ constexpr uint32_t kTcSpin = MGB_TC_SPIN;
 // are split by the caller
 constexpr int kTcMaxKB = 3 * 16384 / kTcBK;
 
-// Two ring depths: 2 stages with two CTAs per SM (short K, the LU and
-// Cholesky updates: one CTA's epilogue overlaps the other's main loop), and
-// 4 stages with one CTA per SM (long K, the plain GEMM: deeper prefetch).
+// Two ring depths: 2 stages with two CTAs per SM (short K, up to 32 K blocks
+// over all segments: the LU and Cholesky updates, where one CTA's epilogue
+// overlaps the other's main loop), and 4 stages with one CTA per SM (long K,
+// the plain GEMM: deeper prefetch).
 template <int ST>
 struct TcSmem {
   // 1024-byte aligned swizzle atoms
@@ -73,8 +76,8 @@ struct TcSmem {
   volatile int timeout;
 };
 
-// Segment s of the K axis (kps K blocks each) reads A from tmA1 when bit s of
-// amask is set (else tmA0), B likewise with bmask.
+// Segment s of the K axis (kps K blocks each) reads A from map (amask >> 2s)
+// & 3 of tmA0 / tmA1 / tmA2, B likewise from bmask (up to 6 segments).
 // tri: 0 every tile; 1 lower (tiles on/below the diagonal, elements with
 // col <= row); 2 upper (col >= row).  rinv / cinv (may be null): per-row and
 // per-column power-of-two factors applied to the accumulator before alpha
@@ -83,8 +86,10 @@ template <int ST, int MINB, bool SC>
 __global__ void __launch_bounds__(kTcThreads, MINB)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA0,
                    const __grid_constant__ CUtensorMap tmA1,
+                   const __grid_constant__ CUtensorMap tmA2,
                    const __grid_constant__ CUtensorMap tmB0,
-                   const __grid_constant__ CUtensorMap tmB1, int M, int N,
+                   const __grid_constant__ CUtensorMap tmB1,
+                   const __grid_constant__ CUtensorMap tmB2, int M, int N,
                    int kps, int nseg, unsigned amask, unsigned bmask,
                    float alpha, const float *__restrict__ alpha_scale,
                    float beta, float *__restrict__ C, int64_t ldc,
@@ -132,8 +137,9 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
       }
       if (s.timeout) break;
       const int seg = kb / kps, kx = (kb % kps) * kTcBK;
-      const CUtensorMap *ma = ((amask >> seg) & 1) ? &tmA1 : &tmA0;
-      const CUtensorMap *mb = ((bmask >> seg) & 1) ? &tmB1 : &tmB0;
+      const unsigned sa = (amask >> (2 * seg)) & 3u, sb = (bmask >> (2 * seg)) & 3u;
+      const CUtensorMap *ma = sa == 2 ? &tmA2 : sa == 1 ? &tmA1 : &tmA0;
+      const CUtensorMap *mb = sb == 2 ? &tmB2 : sb == 1 ? &tmB1 : &tmB0;
       tc::mbar_arrive_expect_tx(&s.full[st], (kTcBM + kTcBN) * kTcBK * 2);
       tc::tma_load_2d(s.a[st], ma, kx, m0, &s.full[st]);
       tc::tma_load_2d(s.b[st], mb, kx, n0, &s.full[st]);
@@ -322,19 +328,21 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
             int lower, const int32_t *skip, const void *Alo, const void *Blo,
-            const float *rinv, const float *cinv) {
+            const float *rinv, const float *cinv, const void *Amid,
+            const void *Bmid) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (M <= 0 || N <= 0) return 0;
   const bool split = Alo && Blo;
-  const int nseg = split ? 3 : 1;
+  const bool split3 = split && Amid && Bmid;
+  const int nseg = split3 ? 6 : split ? 3 : 1;
   if (K <= 0 || K % kTcBK || (K / kTcBK) * nseg > kTcMaxKB || lda % 8 ||
       ldb % 8 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15) ||
-      ((uintptr_t)Alo & 15) || ((uintptr_t)Blo & 15) || M > INT32_MAX ||
-      N > INT32_MAX)
+      ((uintptr_t)Alo & 15) || ((uintptr_t)Blo & 15) || ((uintptr_t)Amid & 15) ||
+      ((uintptr_t)Bmid & 15) || M > INT32_MAX || N > INT32_MAX)
     return set_error(MATGB_ERR_ARG, "tc_gemm: unsupported shape/alignment");
   MGB_TRY(tc_setup());
-  CUtensorMap ma, mb, mal, mbl;
+  CUtensorMap ma, mb, mal, mbl, mam, mbm;
   MGB_TRY(make_map(&ma, A, bf16, M, K, lda, kTcBM));
   MGB_TRY(make_map(&mb, B, bf16, N, K, ldb, kTcBN));
   if (split) {
@@ -344,25 +352,43 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
     mal = ma;
     mbl = mb;
   }
+  if (split3) {
+    MGB_TRY(make_map(&mam, Amid, bf16, M, K, lda, kTcBM));
+    MGB_TRY(make_map(&mbm, Bmid, bf16, N, K, ldb, kTcBN));
+  } else {
+    mam = ma;
+    mbm = mb;
+  }
   dim3 grid((unsigned)((M + kTcBM - 1) / kTcBM), (unsigned)((N + kTcBN - 1) / kTcBN));
   const uint32_t idesc = tc::idesc_f16(bf16 ? 1 : 0, kTcBM, kTcBN);
   const double frac = lower ? 0.5 : 1.0;
-  // segments: [Ah|Ah|Al] . [Bh|Bl|Bh]
-  const unsigned amask = split ? 4u : 0u, bmask = split ? 2u : 0u;
+  // map per segment, 2 bits each (0 hi, 1 lo, 2 mid):
+  //   split:  [Ah|Ah|Al] . [Bh|Bl|Bh]
+  //   split3: [Ah|Ah|Am|Ah|Am|Al] . [Bh|Bm|Bh|Bl|Bm|Bh]  (the terms of weight
+  //           1, 2^-11 and 2^-22; mid*lo, lo*mid and lo*lo are dropped)
+  auto sel = [](std::initializer_list<unsigned> v) {
+    unsigned m = 0, i = 0;
+    for (unsigned x : v) m |= x << (2 * i++);
+    return m;
+  };
+  const unsigned amask = split3 ? sel({0, 0, 2, 0, 2, 1}) : split ? sel({0, 0, 1}) : 0u;
+  const unsigned bmask = split3 ? sel({0, 2, 0, 1, 2, 0}) : split ? sel({0, 1, 0}) : 0u;
   // long K (the plain GEMM): the deeper ring, one CTA per SM
-  const bool deep = K * nseg > 16 * kTcBK;
-  const char *nm = deep ? (split ? "tc_gemm_split_k" : "tc_gemm_k")
-                        : (split ? "tc_gemm_split" : "tc_gemm");
+  const bool deep = K * nseg > 32 * kTcBK;
+  const char *nm = split3 ? (deep ? "tc_gemm_split3_k" : "tc_gemm_split3")
+                   : deep   ? (split ? "tc_gemm_split_k" : "tc_gemm_k")
+                            : (split ? "tc_gemm_split" : "tc_gemm");
   KtScope kt(nm, 2.0 * M * N * K * frac * nseg,
              4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N * frac +
-                 2.0 * (M + N) * K * (split ? 2 : 1));
+                 2.0 * (M + N) * K * (split3 ? 3 : split ? 2 : 1));
   if ((rinv == nullptr) != (cinv == nullptr))
     return set_error(MATGB_ERR_ARG, "tc_gemm: row and column scales go together");
   const bool sc = rinv != nullptr;
 #define MGB_TC_LAUNCH(ST_, MB_, SC_)                                           \
   tc_gemm_kernel<ST_, MB_, SC_><<<grid, kTcThreads, tc_smem_bytes<ST_>(),      \
                                   cx->stream>>>(                               \
-      ma, mal, mb, mbl, (int)M, (int)N, (int)(K / kTcBK), nseg, amask, bmask,  \
+      ma, mal, mam, mb, mbl, mbm, (int)M, (int)N, (int)(K / kTcBK), nseg,      \
+      amask, bmask,                                                            \
       alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv, g_tc_err)
   if (deep && sc)
     MGB_TC_LAUNCH(4, 1, true);

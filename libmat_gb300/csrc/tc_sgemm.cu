@@ -76,11 +76,20 @@ __device__ __forceinline__ int pack_exp(unsigned a) {
   return sh;
 }
 
-__device__ __forceinline__ void split_store(float v, __half *hi, __half *lo,
-                                            int64_t at) {
+// v = hi + lo (two parts), or hi + mid + lo (three: mid null otherwise);
+// each remainder is exact in FP32
+__device__ __forceinline__ void split_store(float v, __half *hi, __half *mid,
+                                            __half *lo, int64_t at) {
   const __half h = __float2half_rn(v);
   hi[at] = h;
-  lo[at] = __float2half_rn(v - __half2float(h));
+  const float r = v - __half2float(h);
+  if (mid) {
+    const __half m = __float2half_rn(r);
+    mid[at] = m;
+    lo[at] = __float2half_rn(r - __half2float(m));
+  } else {
+    lo[at] = __float2half_rn(r);
+  }
 }
 
 // Convert rows x K (scaled by 2^pack_exp(amax[r])) into hi / lo, row-major with
@@ -90,8 +99,8 @@ __device__ __forceinline__ void split_store(float v, __half *hi, __half *lo,
 __global__ void pack_split_kernel(int64_t rows, int64_t K, int64_t Kp,
                                   const float *__restrict__ P, int64_t ld,
                                   bool contig, const unsigned *__restrict__ amax,
-                                  __half *__restrict__ hi, __half *__restrict__ lo,
-                                  float *__restrict__ inv) {
+                                  __half *__restrict__ hi, __half *__restrict__ mid,
+                                  __half *__restrict__ lo, float *__restrict__ inv) {
   __shared__ float tile[kPackTile][kPackTile + 1];
   const int64_t r0 = (int64_t)blockIdx.x * kPackTile;  // rows: grid x
   const int64_t k0 = (int64_t)blockIdx.y * kPackTile;  // K (<= 16384): grid y
@@ -113,23 +122,26 @@ __global__ void pack_split_kernel(int64_t rows, int64_t K, int64_t Kp,
       v = gk < K ? __ldg(P + gr * ld + gk) : 0.f;
     else
       v = tile[tx][rr];
-    split_store(ldexpf(v, sh), hi, lo, gr * Kp + gk);
+    split_store(ldexpf(v, sh), hi, mid, lo, gr * Kp + gk);
     if (blockIdx.y == 0 && tx == 0) inv[gr] = ldexpf(1.f, -sh);
   }
 }
 
 struct Pack {
-  __half *hi, *lo;
+  __half *hi, *mid, *lo;  // mid null for two parts
   float *inv;
 };
 
-// Packs a rows x K operand into the FP16 split form: ws_slot holds hi and lo
-// (2 * rows * Kp halves), inv and amax come from `scratch`.
+// Packs a rows x K operand into the FP16 split form: ws_slot holds the parts
+// (parts * rows * Kp halves), inv and amax come from the caller's scratch.
 int pack_operand(int64_t rows, int64_t K, int64_t Kp, const float *P, int64_t ld,
-                 bool contig, int ws_slot, float *inv, unsigned *amax, Pack *out) {
+                 bool contig, int ws_slot, float *inv, unsigned *amax, int parts,
+                 Pack *out) {
   cudaStream_t st = ctx()->stream;
-  __half *h = (__half *)ws(ws_slot, (size_t)2 * rows * Kp * sizeof(__half));
+  __half *h = (__half *)ws(ws_slot, (size_t)parts * rows * Kp * sizeof(__half));
   if (!h) return MATGB_ERR_NOMEM;
+  __half *lo = h + rows * Kp;
+  __half *md = parts == 3 ? h + 2 * rows * Kp : nullptr;
   MGB_CUDA(cudaMemsetAsync(amax, 0, (size_t)rows * sizeof(unsigned), st));
   {
     KtScope kt("tc_pack_amax", 0.0, 4.0 * rows * K);
@@ -151,12 +163,13 @@ int pack_operand(int64_t rows, int64_t K, int64_t Kp, const float *P, int64_t ld
     KtScope kt("tc_pack_split", 0.0, 4.0 * rows * K + 4.0 * rows * Kp);
     const dim3 g((unsigned)((rows + kPackTile - 1) / kPackTile),
                  (unsigned)((Kp + kPackTile - 1) / kPackTile));
-    pack_split_kernel<<<g, 256, 0, st>>>(rows, K, Kp, P, ld, contig, amax, h,
-                                         h + rows * Kp, inv);
+    pack_split_kernel<<<g, 256, 0, st>>>(rows, K, Kp, P, ld, contig, amax, h, md,
+                                         lo, inv);
     MGB_LAUNCHED("tc_pack_split");
   }
   out->hi = h;
-  out->lo = h + rows * Kp;
+  out->mid = md;
+  out->lo = lo;
   out->inv = inv;
   return 0;
 }
@@ -168,12 +181,14 @@ int g_plain_tc = 1;
 bool plain_tc_on() { return g_plain_tc != 0; }
 
 // K is split into chunks of at most this many columns (each chunk one launch
-// accumulating into C), which bounds a CTA's main loop.
+// accumulating into C), which bounds a CTA's main loop (16384 columns in
+// three segments, 8192 in six).
 constexpr int64_t kSgemmKChunk = 16384;
 
 int tc_sgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, float alpha,
              const float *A, int64_t lda, const float *B, int64_t ldb,
-             float beta, float *C, int64_t ldc, int tri, bool same_ab) {
+             float beta, float *C, int64_t ldc, int tri, bool same_ab, int parts) {
+  if (parts != 2 && parts != 3) return set_error(MATGB_ERR_ARG, "tc_sgemm: parts 2 or 3");
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (m <= 0 || n <= 0) return 0;
@@ -185,8 +200,9 @@ int tc_sgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, float alpha,
     return gemm_skip_t<float>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C,
                               ldc, tri, nullptr);
   }
-  for (int64_t kc0 = 0; kc0 < k; kc0 += kSgemmKChunk) {
-    const int64_t kc = k - kc0 < kSgemmKChunk ? k - kc0 : kSgemmKChunk;
+  const int64_t kchunk = parts == 3 ? kSgemmKChunk / 2 : kSgemmKChunk;
+  for (int64_t kc0 = 0; kc0 < k; kc0 += kchunk) {
+    const int64_t kc = k - kc0 < kchunk ? k - kc0 : kchunk;
     const int64_t Kp = (kc + 63) / 64 * 64;
     // the chunk's columns of op(A) (rows i, K-contiguous when ta) and rows of
     // op(B)^T (rows j: columns of op(B), K-contiguous when !tb)
@@ -197,16 +213,18 @@ int tc_sgemm(bool ta, bool tb, int64_t m, int64_t n, int64_t k, float alpha,
     float *rinv = sc, *cinv = sc + m;
     unsigned *amax = reinterpret_cast<unsigned *>(sc + m + n);
     Pack pa, pb;
-    MGB_TRY(pack_operand(m, kc, Kp, Ac, lda, ta, WS_TCA, rinv, amax, &pa));
+    MGB_TRY(pack_operand(m, kc, Kp, Ac, lda, ta, WS_TCA, rinv, amax, parts, &pa));
     if (same_ab) {
       pb = pa;
       pb.inv = rinv;
     } else {
-      MGB_TRY(pack_operand(n, kc, Kp, Bc, ldb, !tb, WS_TCB, cinv, amax + m, &pb));
+      MGB_TRY(pack_operand(n, kc, Kp, Bc, ldb, !tb, WS_TCB, cinv, amax + m, parts,
+                           &pb));
     }
     const float b = kc0 == 0 ? beta : 1.f;
     MGB_TRY(tc_gemm(0, m, n, Kp, pa.hi, Kp, pb.hi, Kp, alpha, nullptr, b, C, ldc,
-                    tri, nullptr, pa.lo, pb.lo, rinv, same_ab ? rinv : cinv));
+                    tri, nullptr, pa.lo, pb.lo, rinv, same_ab ? rinv : cinv, pa.mid,
+                    pb.mid));
   }
   return 0;
 }

@@ -1,8 +1,8 @@
-"""GPU: the float build's tensor-core products (FP16 hi + remainder split under
-power-of-two row / column scales, three products, FP32 accumulation) behind
-mat_gemm / mat_mul / mat_syrk and the plain Cholesky's SYRK updates, through
-the C ABI (the plain LU keeps FP32 SIMT updates; its test here checks that
-the switch leaves its pivots with the reference's).
+"""GPU: the float build's tensor-core products behind mat_gemm / mat_mul /
+mat_syrk and the plain Cholesky's SYRK updates (FP16 hi + remainder split
+under power-of-two row / column scales, three products, FP32 accumulation)
+and behind the plain LU's trailing updates (hi + mid + remainder, six
+products, about 33 bits of each operand), through the C ABI.
 
 Each case is checked against an FP64 product of the same float inputs (the
 exact answer to ~1e-16) and against the oracle where it is quick, within the
@@ -165,3 +165,36 @@ def test_tc_plain_lu_and_chol_vs_oracle(tc_mode, n):
     Lo, ro = O.chol(S)
     assert rc == ro == 0
     assert rel(Lc, Lo) <= 2e-4
+
+
+@pytest.mark.parametrize("n", [2048, 3000])
+def test_tc_plain_lu_matches_simt_lu(tc_mode, n):
+    """The plain float LU with its trailing updates on the tensor cores (the
+    six-product split) against the same LU with FP32 SIMT updates, through
+    matgb_getrf_dev: the same pivots on the data-determined steps (all but
+    the last 5%, where the float Schur complement is rounding noise -- as
+    at the 8192 config, where the reference's own float and double pivots
+    part at step 8116) and the factors up to the first differing step equal
+    to FP32 rounding (2e-4 of max |ref|, the parity suite's factor bound)."""
+    L = tc_mode
+    A = rng.uniform(71 + n, (n, n), -1.0, 1.0, np.float32)
+    out = {}
+    for on in (1, 0):
+        L.c.matgb_plain_tensor_core(on)
+        dA, dp = L.dalloc(A.nbytes), L.dalloc(8 * n)
+        try:
+            L.h2d(dA, np.asfortranarray(A))
+            L.check(L.c.matgb_getrf_dev(n, dA, n, dp, dp + 4 * n), "getrf")
+            LU = np.empty((n, n), np.float32, order="F")
+            L.d2h(LU, dA)
+            piv = np.empty(2 * n, np.int32)
+            L.d2h(piv, dp)
+        finally:
+            L.dfree(dA)
+            L.dfree(dp)
+        out[on] = (LU, piv)
+    p1, p0 = out[1][1][n:], out[0][1][n:]
+    diff = np.nonzero(p1 != p0)[0]
+    k = int(diff[0]) if len(diff) else n
+    assert k >= int(0.95 * n), k
+    assert rel(out[1][0][:, :k], out[0][0][:, :k]) <= 2e-4
