@@ -725,9 +725,14 @@ def run_blas_t(mg, steps=5, warmup=3):
 
 
 def run_batched(mg, count=100000, steps=5, warmup=3):
+    """The 100k-system workload in the plain FP32 mode (the reference's
+    operations, pivots and rounding per system) and in the mixed-precision
+    mode (tensor-core kernels refined to an FP32-level residual) -- with the
+    tuned per-queue routing ("mixed") and with every queue of orders 33..128
+    on the tensor cores ("mixed_all_tensor_core"); the plain figures at the
+    top level."""
     from libmat_gb300 import batched_data
     L = mg.load("f32")
-    rs = np.random.default_rng(7)  # the sample of systems checked below
     arrs = batched_data.make(count)
     ns, offA, offv, A, b, kinds = (arrs[k] for k in ("n", "oA", "ov", "A", "b", "k"))
     totA, totv = A.size, b.size
@@ -737,74 +742,104 @@ def run_batched(mg, count=100000, steps=5, warmup=3):
     for k, v in arrs.items():
         L.h2d(d[k], v)
     L.sync()
+    byt = 4 * (totA + 2 * totv)
+    pk, src = peaks()
+    # algorithmic FLOPs of the reference's path: PLU 2n^3/3, Cholesky n^3/3,
+    # plus the two triangular solves 2n^2 (the kernels' Gauss-Jordan form
+    # does more); the mean intensity (~12 FLOP/B) is above the FP32 FFMA
+    # ridge, so the FP32 fraction is given beside the HBM one
+    nn = ns.astype(np.float64)
+    flops = float(np.sum(np.where(kinds == 0, 2 * nn ** 3 / 3, nn ** 3 / 3) + 2 * nn ** 2))
+    fp32_peak = pk.get("fp32_tflops") or L.c.matgb_measure_fma_peak(0)
+    from oracle.loader import Oracle
+    O64 = Oracle("f64", "port")
 
     def run():
         L.check(L.c.matgb_solve_batched_dev(count, d["n"], d["oA"], d["A"],
                                             d["ov"], d["b"], dx, d["k"], st),
                 "batched")
 
-    for _ in range(warmup):
-        run()
-    L.sync()
-    L.check(L.c.matgb_event_record(0), "ev")
-    for _ in range(steps):
-        run()
-    L.check(L.c.matgb_event_record(1), "ev")
-    L.sync()
-    ms = L.c.matgb_event_elapsed_ms(0, 1) / steps
-    # per-queue kernel times of one more pass
-    L.c.matgb_ktime_enable(1)
-    run()
-    L.sync()
-    kt = ktable(L)
-    L.c.matgb_ktime_enable(0)
-    byt = 4 * (totA + 2 * totv)
-    status = np.empty(count, np.int32)
-    L.d2h(status, st)
-    x = np.empty(totv, np.float32)
-    L.d2h(x, dx)
-    # a sample of 100 systems: backward error, and forward error against the
-    # FP64 oracle (the reference's mat_solve / mat_solve_spd in double)
-    from oracle.loader import Oracle
-    O64 = Oracle("f64", "port")
-    worst, worst_fe = 0.0, 0.0
-    for s in rs.integers(0, count, 100):
-        n = ns[s]
-        M = A[offA[s]:offA[s] + n * n].reshape(n, n, order="F").astype(np.float64)
-        xs = x[offv[s]:offv[s] + n].astype(np.float64)
-        bs = b[offv[s]:offv[s] + n]
-        worst = max(worst, np.abs(M @ xs - bs).max() /
-                    (np.abs(M).sum(1).max() * np.abs(xs).max() + np.abs(bs).max()))
-        xt = O64.solve(M, bs) if kinds[s] == 0 else O64.solve_spd(M, bs)[0]
-        worst_fe = max(worst_fe, np.abs(xs - xt).max() / np.abs(xt).max())
+    def measure(mode):
+        mixed = mode > 0
+        prev = L.c.matgb_batched_mixed(mode)
+        try:
+            for _ in range(warmup):
+                run()
+            L.sync()
+            L.check(L.c.matgb_event_record(0), "ev")
+            for _ in range(steps):
+                run()
+            L.check(L.c.matgb_event_record(1), "ev")
+            L.sync()
+            ms = L.c.matgb_event_elapsed_ms(0, 1) / steps
+            stats = (C.c_int(), C.c_int(), C.c_int())
+            L.check(L.c.matgb_batched_mixed_stats(*(C.byref(v) for v in stats)))
+            # per-queue kernel times of one more pass
+            L.c.matgb_ktime_enable(1)
+            run()
+            L.sync()
+            kt = ktable(L)
+            L.c.matgb_ktime_enable(0)
+        finally:
+            L.c.matgb_batched_mixed(prev)
+        status = np.empty(count, np.int32)
+        L.d2h(status, st)
+        x = np.empty(totv, np.float32)
+        L.d2h(x, dx)
+        # a sample of 100 systems: backward error, and forward error against
+        # the FP64 oracle (the reference's mat_solve / mat_solve_spd in double)
+        rs = np.random.default_rng(7)
+        worst, worst_fe = 0.0, 0.0
+        for s in rs.integers(0, count, 100):
+            n = ns[s]
+            M = A[offA[s]:offA[s] + n * n].reshape(n, n, order="F").astype(np.float64)
+            xs = x[offv[s]:offv[s] + n].astype(np.float64)
+            bs = b[offv[s]:offv[s] + n]
+            worst = max(worst, np.abs(M @ xs - bs).max() /
+                        (np.abs(M).sum(1).max() * np.abs(xs).max() + np.abs(bs).max()))
+            xt = O64.solve(M, bs) if kinds[s] == 0 else O64.solve_spd(M, bs)[0]
+            worst_fe = max(worst_fe, np.abs(xs - xt).max() / np.abs(xt).max())
+        gbs = byt / (ms * 1e-3) / 1e9
+        tfl = flops / (ms * 1e-3) / 1e12
+        out = {"ms": ms, "solves_per_s": count / (ms * 1e-3), "hbm_gbs": gbs,
+               "hbm_frac": gbs / pk["hbm_gbs"], "tflops": tfl,
+               "fp32_frac": tfl / fp32_peak if fp32_peak else None,
+               "status_nonzero": int((status != 0).sum()),
+               "bwd_err_sample_max": worst, "fwd_err_sample_max": worst_fe,
+               "kernels": [{"name": r[0], "ms": round(r[2], 4)} for r in kt]}
+        if mixed:
+            out.update({"refinement_corrections": stats[0].value,
+                        "unconverged": stats[1].value,
+                        "form": ("the queues the tuning table routes (compiled-in: "
+                                 "general 97..128)" if mode == 1 else
+                                 "every queue of orders 33..128") +
+                                " on the tensor-core kernels: matrix in TMEM, blocked "
+                                "Gauss-Jordan (32-column panels), transforms and "
+                                "trailing updates as TF32 hi + remainder tcgen05 "
+                                "products (FP32 accumulate), FP32 refinement to "
+                                "|r|/(|A||x|+|b|) <= n 2^-24; the other queues on "
+                                "the FP32 kernels"})
+        return out
+
+    plain = measure(0)
+    mixed = measure(1)
+    mixed_all = measure(2)
     for v in list(d.values()) + [dx, st]:
         L.dfree(v)
-    pk, src = peaks()
-    gbs = byt / (ms * 1e-3) / 1e9
-    # algorithmic FLOPs of the reference's path: PLU 2n^3/3, Cholesky n^3/3,
-    # plus the two triangular solves 2n^2 (the kernel's Gauss-Jordan form
-    # does more); the mean intensity (~12 FLOP/B) is above the FP32 FFMA
-    # ridge, so the FP32 fraction is given beside the HBM one
-    nn = ns.astype(np.float64)
-    flops = float(np.sum(np.where(kinds == 0, 2 * nn ** 3 / 3, nn ** 3 / 3) + 2 * nn ** 2))
-    fp32_peak = pk.get("fp32_tflops") or L.c.matgb_measure_fma_peak(0)
-    tfl = flops / (ms * 1e-3) / 1e12
     fused = L.c.matgb_batched_schedule(-1, -1, -1)
-    return {"workload": "batched_100k_uneven_f32", "ms": ms,
-            "schedule": ("one persistent cooperative launch, replayed as a "
-                         "CUDA graph" if fused else "one launch per (bucket, "
-                         "kind) queue"),
-            "tune_source": L.c.matgb_batched_tune_source().decode(),
-            "solves_per_s": count / (ms * 1e-3), "bytes": byt,
-            "hbm_gbs": gbs, "hbm_frac": gbs / pk["hbm_gbs"],
-            "hbm_peak_source": src, "flops": flops, "tflops": tfl,
-            "fp32_peak_tflops": fp32_peak,
-            "fp32_frac": tfl / fp32_peak if fp32_peak else None,
-            "status_nonzero": int((status != 0).sum()),
-            "bwd_err_sample_max": worst, "fwd_err_sample_max": worst_fe,
-            "fwd_err_oracle": "reference mat_solve / mat_solve_spd in double "
-                              "(oracle port), 100 sampled systems",
-            "kernels": [{"name": r[0], "ms": round(r[2], 4)} for r in kt]}
+    res = {"workload": "batched_100k_uneven_f32",
+           "schedule": ("one persistent cooperative launch, replayed as a "
+                        "CUDA graph" if fused else "one launch per (bucket, "
+                        "kind) queue, replayed as a CUDA graph"),
+           "tune_source": L.c.matgb_batched_tune_source().decode(),
+           "bytes": byt, "hbm_peak_source": src, "flops": flops,
+           "fp32_peak_tflops": fp32_peak,
+           "fwd_err_oracle": "reference mat_solve / mat_solve_spd in double "
+                             "(oracle port), 100 sampled systems"}
+    res.update(plain)
+    res["mixed"] = mixed
+    res["mixed_all_tensor_core"] = mixed_all
+    return res
 
 
 # ----------------------------------------------------------------- CPU legs

@@ -324,17 +324,47 @@ int matgb_solve_batched_dev(int64_t count, const int32_t *n,
  * one entry.  No counterpart in the reference. */
 int matgb_batched_tune(int nb, int kind, int algo, int ctas_per_sm);
 int matgb_batched_tune_get(int nb, int kind, int *algo, int *ctas_per_sm);
-/* The batched solver's launch schedule: fused = 1 (the default) files and
+/* The batched solver's launch schedule: fused = 1 files and
  * solves every system in ONE persistent cooperative launch (orders 65..128
  * one per CTA, 33..64 two, 17..32 four, 1..16 eight; largest first), 0 = one
  * launch per (bucket, kind) queue with the per-bucket algorithms above;
  * ctas_per_sm caps the fused launch's resident CTAs per SM (0: as many as
- * fit); graphs = 1 (the default) captures the fused launch sequence in a CUDA
- * graph and replays it while the same buffers are passed.  -1 leaves a
- * setting unchanged.  Returns the previous fused setting. */
+ * fit); graphs = 1 (the default) captures either launch sequence in a CUDA
+ * graph and replays it while the same buffers are passed.  The compiled-in
+ * default is fused = 0 (measured faster on the 100k-system workload); the
+ * tuner's file may choose.  -1 leaves a setting unchanged.  Returns the
+ * previous fused setting. */
 int matgb_batched_schedule(int fused, int ctas_per_sm, int graphs);
 /* Where the schedule came from: "defaults" or the file and its entry count. */
 const char *matgb_batched_tune_source(void);
+/* The mixed-precision batched mode (float build only).  A queue of orders
+ * 33..128 that it routes to the tensor-core kernels is solved with the
+ * matrix held in tensor memory, blocked Gauss-Jordan in 32-column panels
+ * whose transforms and trailing updates run as TF32 hi + remainder products
+ * with FP32 accumulation (~21 bits), then FP32 residuals and corrections
+ * until the normwise backward error |r|/(|A||x| + |b|) <= n 2^-24 (at most 4
+ * corrections).  Its status[s] is then 0 (converged), 1 (not converged: x
+ * holds the last iterate), -1 (an SPD pivot <= 0, x untouched) or -3 (a wait
+ * for the tensor core gave up).  A general system keeps the diagonal pivots
+ * when, in every panel, partial pivoting would keep them within the 32-row
+ * pivot block and the panel's transform entries stay within 1; otherwise it
+ * is factored again with partial pivoting (on the values this factorisation
+ * computes, so the pivots may differ from the reference's on near-ties).
+ * on = 1: the queues chosen per (bucket, kind) by matgb_batched_mixed_tune /
+ * the tuner's file (compiled-in: general 97..128); on = 2: every queue of
+ * orders 33..128; 0: off (the FP32 kernels only, the reference's
+ * semantics).  Queues not routed keep the FP32 kernels.  on = -1 only
+ * queries.  Returns the previous setting (an error code for on > 0 in the
+ * double build).  No counterpart in the reference. */
+int matgb_batched_mixed(int on);
+/* Route queue (nb = 64, 96 or 128, kind 0 general / 1 SPD) to the
+ * tensor-core kernel (use_tc = 1) or the FP32 kernel (0) when the mixed mode
+ * is 1. */
+int matgb_batched_mixed_tune(int nb, int kind, int use_tc);
+/* The last batched call's mixed-mode counts (synchronises the library
+ * stream): refinement corrections taken, systems with status 1, and whether
+ * a wait gave up.  Any pointer may be NULL. */
+int matgb_batched_mixed_stats(int *corrections, int *unconverged, int *timeouts);
 
 /* ---- Host (Mat) superset ------------------------------------------------- */
 /* AX = B for every column of B (mat_solve reads only column 0, mat.h:4825). */

@@ -171,6 +171,9 @@ class Lib:
             "matgb_batched_tune_get": (_I, [_I, _I, C.POINTER(_I), C.POINTER(_I)]),
             "matgb_batched_tune_source": (C.c_char_p, []),
             "matgb_batched_schedule": (_I, [_I, _I, _I]),
+            "matgb_batched_mixed": (_I, [_I]),
+            "matgb_batched_mixed_tune": (_I, [_I, _I, _I]),
+            "matgb_batched_mixed_stats": (_I, [C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
             "matgb_library_dir": (C.c_char_p, []),
             "matgb_gesv_ir_multi_dev": (_I, [_S, _S, _P, _S, _P, _S, _P, _S,
                                              C.POINTER(MatIROpts),

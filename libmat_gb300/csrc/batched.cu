@@ -57,6 +57,16 @@ static BatchTune g_tune[kNumBuckets][2] = {
 static int g_fused = 0;       // 1: one persistent launch; 0: a launch per queue
 static int g_fused_ctas = 0;  // resident CTAs per SM for it (0: as many as fit)
 static int g_graphs = 1;      // replay the launch sequence as a CUDA graph
+// The mixed-precision mode (float build): 0 off; 1 the queues of orders
+// 33..128 whose entry below is 1 take the tensor-core kernels (batched_tc.cu),
+// refined to an FP32-level residual, the others keep the FP32 kernels; 2 every
+// queue of orders 33..128 takes them.  Compiled-in: the 97..128 general queue
+// only -- measured on the 100k-system workload, the tensor-core kernel took
+// 1.20 ms there against 1.59 ms for the register kernel, and lost on the
+// other queues (SPD 97..128: 1.55 against 1.21 ms).  The tuner's file
+// ("mixed_tc" entries) may choose.
+static int g_mixed = 0;
+static int g_mixed_tc[kNumBuckets][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {1, 0}};
 static bool g_graphs_broken = false;
 static std::once_flag g_tune_once;
 static char g_tune_source[512] = "defaults";
@@ -118,7 +128,18 @@ static void load_tune_file() {
         continue;
       }
     }
-    int nb, kind, algo, ctas;
+    int nb, kind, algo, ctas, mtc;
+    if (sizeof(elem_t) == 4 && int_after(p, "\"nb\"", e, &nb) &&
+        int_after(p, "\"kind\"", e, &kind) && int_after(p, "\"mixed_tc\"", e, &mtc) &&
+        (kind == 0 || kind == 1) && (mtc == 0 || mtc == 1)) {
+      for (int bk = 2; bk < kNumBuckets; bk++)
+        if (bucket_nb(bk) == nb) {
+          g_mixed_tc[bk][kind] = mtc;
+          used++;
+        }
+      p = e;
+      continue;
+    }
     if (int_after(p, "\"nb\"", e, &nb) && int_after(p, "\"kind\"", e, &kind) &&
         int_after(p, "\"algo\"", e, &algo) &&
         int_after(p, "\"ctas_per_sm\"", e, &ctas) && (kind == 0 || kind == 1) &&
@@ -204,6 +225,7 @@ struct GraphKey {
   }
 };
 static GraphKey g_gkey{};
+static BatchQueues *g_last_q = nullptr;  // the last queue-schedule call's state
 static cudaGraphExec_t g_gexec = nullptr;
 static int g_tune_version = 0;  // bumped by matgb_batched_tune / _schedule
 static int g_graph_kernels = 0;
@@ -285,7 +307,11 @@ static int enqueue_queues(int64_t count, const int32_t *n, const int64_t *offA,
           {batched_bucket_64_lu, batched_bucket_64_chol},
           {batched_bucket_96_lu, batched_bucket_96_chol},
           {batched_bucket_128_lu, batched_bucket_128_chol}};
-      MGB_TRY(fns[bk][kd](qi, list, q, n, offA, A, offv, b, x, status));
+      if ((g_mixed == 2 && bk >= 2) || (g_mixed == 1 && g_mixed_tc[bk][kd]))
+        MGB_TRY(batched_tc_bucket(bk, kd, qi, list, q, n, offA, A, offv, b, x, status,
+                                  0));
+      else
+        MGB_TRY(fns[bk][kd](qi, list, q, n, offA, A, offv, b, x, status));
     }
   check_sizes_kernel<<<g, 256, 0, st>>>(count, n, nmax, status);
   MGB_LAUNCHED("check_sizes");
@@ -300,12 +326,14 @@ int solve_batched(int64_t count, const int32_t *n, const int64_t *offA,
   if (count <= 0) return 0;
   if (count > INT32_MAX / kNumQueues) return set_error(MATGB_ERR_ARG, "batch too large");
   (void)batched_tune(0, 0);  // the schedule table, loaded once
-  if (g_fused) return solve_fused(count, n, offA, A, offv, b, x, kind, status);
+  // the one-launch schedule has no mixed-precision phases
+  if (g_fused && !g_mixed) return solve_fused(count, n, offA, A, offv, b, x, kind, status);
   BatchQueues *q = (BatchQueues *)ws(WS_T2, sizeof(BatchQueues) + 256);
   int32_t *list = (int32_t *)ws(WS_V1, (size_t)count * sizeof(int32_t));
   if (!q || !list) return MATGB_ERR_NOMEM;
+  g_last_q = q;
   const GraphKey key{count, {n, offA, A, offv, b, x, kind, status, list, q, cx->stream},
-                     0, 0, g_tune_version};
+                     0, g_mixed, g_tune_version};
   return run_graph(key, [&] {
     return enqueue_queues(count, n, offA, A, offv, b, x, kind, status, q, list);
   });
@@ -350,6 +378,47 @@ extern "C" int matgb_batched_schedule(int fused, int ctas_per_sm, int graphs) {
   if (graphs >= 0) g_graphs = graphs ? 1 : 0;
   g_tune_version++;
   return prev;
+}
+
+extern "C" int matgb_batched_mixed(int on) {
+  (void)batched_tune(0, 0);  // the file's entries first
+  const int prev = g_mixed;
+  if (on >= 0) {
+    if (on > 2) return set_error(MATGB_ERR_ARG, "batched_mixed: on must be 0, 1 or 2");
+#ifdef MAT_DOUBLE_PRECISION
+    if (on) return set_error(MATGB_ERR_ARG, "the mixed batched solver is float-only");
+#endif
+    g_mixed = on;
+    g_tune_version++;
+  }
+  return prev;
+}
+
+extern "C" int matgb_batched_mixed_tune(int nb, int kind, int use_tc) {
+  (void)batched_tune(0, 0);
+  if ((kind != 0 && kind != 1) || (use_tc != 0 && use_tc != 1))
+    return set_error(MATGB_ERR_ARG, "batched_mixed_tune: bad kind/use_tc");
+  for (int bk = 2; bk < kNumBuckets; bk++)
+    if (bucket_nb(bk) == nb) {
+      g_mixed_tc[bk][kind] = use_tc;
+      g_tune_version++;
+      return 0;
+    }
+  return set_error(MATGB_ERR_ARG, "batched_mixed_tune: nb must be 64, 96 or 128");
+}
+
+extern "C" int matgb_batched_mixed_stats(int *corrections, int *unconverged, int *timeouts) {
+  int h[3] = {0, 0, 0};
+  if (g_last_q) {
+    Ctx *cx = ctx();
+    if (!cx) return MATGB_ERR_NO_DEVICE;
+    MGB_CUDA(cudaStreamSynchronize(cx->stream));
+    MGB_CUDA(cudaMemcpy(h, &g_last_q->tc_corr, sizeof h, cudaMemcpyDeviceToHost));
+  }
+  if (corrections) *corrections = h[0];
+  if (unconverged) *unconverged = h[1];
+  if (timeouts) *timeouts = h[2];
+  return 0;
 }
 
 extern "C" const char *matgb_batched_tune_source(void) {

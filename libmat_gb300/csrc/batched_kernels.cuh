@@ -25,7 +25,16 @@ struct BatchQueues {
   int count[kNumQueues];  // systems per queue
   int next[kNumQueues];   // work counters
   int fill[kNumQueues];   // scatter cursors
+  // mixed-precision (tensor-core) kernels: refinement corrections taken,
+  // systems left above the FP32-level residual, a wait that gave up
+  int tc_corr, tc_unconv, tc_err;
 };
+
+// The mixed-precision kernels of buckets 64 / 96 / 128 (batched_tc.cu).
+int batched_tc_bucket(int bucket, int kind, int queue, const int32_t *list, BatchQueues *q,
+                      const int32_t *n, const int64_t *offA, const elem_t *A,
+                      const int64_t *offv, const elem_t *b, elem_t *x, int32_t *status,
+                      int ctas_per_sm);
 
 // Per (size bucket, kind) schedule, chosen by the tuner (tune_batched.py
 // writes batched_tune.json, which the library reads at the first batched

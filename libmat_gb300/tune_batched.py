@@ -9,6 +9,9 @@ Measures, on the device, on the batched workload (libmat_gb300.batched_data):
     runs as its own launch, one after another, so a queue's time does not
     depend on the other queues' choices and every queue's candidates are
     swept at once, configuration by configuration;
+  * for the mixed-precision mode, each queue of orders 33..128 on the
+    tensor-core kernel against its best FP32 candidate ("mixed_tc" entries:
+    1 where the tensor-core kernel was faster);
 and writes the faster schedule (with the fastest candidate per queue) to
 libmat_gb300/batched_tune.json, which the library reads at its first batched
 call (compiled-in defaults otherwise).
@@ -136,12 +139,25 @@ def main():
             table.setdefault(key, {})[chosen[key]] = ms
             if key not in best or ms < best[key][1]:
                 best[key] = (chosen[key], ms)
+    # the mixed-precision mode: each queue of orders 33..128 on the
+    # tensor-core kernel against its best FP32 candidate
+    for (nb, kind), ((algo, ctas), _) in best.items():
+        L.check(L.c.matgb_batched_tune(nb, kind, algo, ctas), "tune")
+    prev = L.c.matgb_batched_mixed(2)
+    run()
+    tc = timings(L, run, args.reps)
+    L.c.matgb_batched_mixed(prev)
     for v in list(d.values()) + [dx, st]:
         L.dfree(v)
     entries = []
     for (nb, kind), ((algo, ctas), ms) in sorted(best.items()):
         entries.append({"prec": "f32", "nb": nb, "kind": kind, "algo": algo,
                         "ctas_per_sm": ctas, "ms": round(ms, 4)})
+    for (nb, kind), ms in sorted(tc.items()):
+        if nb >= 64 and (nb, kind) in best:
+            entries.append({"prec": "f32", "nb": nb, "kind": kind,
+                            "mixed_tc": int(ms < best[nb, kind][1]),
+                            "tc_ms": round(ms, 4)})
     queues_ms = sum(ms for _, ms in best.values())
     fctas, fms = min(fused_ms.items(), key=lambda kv: kv[1]) if fused_ms else (0, None)
     fused = int(fms is not None and fms <= queues_ms)
