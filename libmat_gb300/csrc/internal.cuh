@@ -57,7 +57,10 @@ enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
   WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_SWM, WS_SWG,
   WS_RZA, WS_RZB, WS_RZC, WS_RZE, WS_TCA, WS_TCB, WS_TCS, WS_QR,
-  WS_NSLOTS
+  // the tensor-core trailing update's packing buffers, one set per side
+  // stream of a chunked factorisation (set 0 is WS_T0..WS_T2)
+  WS_CU0,
+  WS_NSLOTS = WS_CU0 + 3 * 8
 };
 void *ws(int slot, size_t bytes);
 
@@ -117,21 +120,38 @@ int laswp_t(T *A, int64_t lda, int64_t c0, int64_t c1, int64_t c2, int64_t c3,
 template <typename T>
 int lu_panel_t(T *A, int64_t lda, int64_t n, int64_t k0, int w, int32_t *ipiv,
                T eps, int *w_used);
+// Columns of the matrix arriving in chunks while it is factored: chunk k
+// (columns [k*cw, (k+1)*cw), cw a multiple of the outer block) is in the
+// matrix once ev[k] has completed.  Chunk 0 is waited for before the first
+// block.  Chunk k >= 1 catches up on a side stream of its own -- the row
+// swaps, U12 solve and trailing update of each finished block applied to its
+// columns, block after block, the same operations in another order -- and
+// joins the main stream's updates just before the look-ahead reaches its
+// first block.
+constexpr int kMaxChunks = 64;
+struct ArrivalPlan {
+  int nchunks = 0;
+  int64_t cw = 0;
+  cudaEvent_t ev[kMaxChunks] = {};
+};
 // lp: -1 = trailing updates by the SIMT GEMM in T; 0 = FP16, 1 = BF16
 // tensor-core updates (T = float only; FP32 panels and trailing matrix).
+// arr (may be null): the columns arrive in chunks (see ArrivalPlan).
 template <typename T>
 int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
-            int lp);
+            int lp, const ArrivalPlan *arr = nullptr);
 // Tensor-core trailing update of columns [c0,c1) after outer block [kb,ke)
 // (mixed.cu): packs U12[:, c0:c1] to 16 bits, and L21 too on the block's
 // first call (first = true).
 // amax3 (may be null): the block's max slots [|L21|, |U12| look-ahead, |U12|
 // rest], zeroed once per factorisation; l21_ready / u12_ready: already filled
 // by the factorisation kernels.
+// wset: the packing buffers' set (0: the main stream's; s >= 1: side
+// stream s of a chunked factorisation).
 int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
                        int64_t ke, int64_t c0, int64_t c1, int lp, bool first,
                        unsigned *amax3 = nullptr, bool l21_ready = false,
-                       bool u12_ready = false);
+                       bool u12_ready = false, int wset = 0);
 // y = beta*y + alpha*A^T x and y += alpha*x (blas_t.cu).
 template <typename T>
 int gemv_t_t(int64_t m, int64_t n, T alpha, const T *A, int64_t lda,

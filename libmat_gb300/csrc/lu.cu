@@ -29,6 +29,8 @@
 #include <cooperative_groups.h>
 #include <limits.h>
 
+#include <vector>
+
 #include "internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -1757,9 +1759,37 @@ static int trailing_update(int64_t n, T *A, int64_t lda, int64_t kb,
                             l21_ready, u12_ready);
 }
 
+// Side streams (lowest priority) and events of a chunked factorisation:
+// blk[j] after block j's swap map, done[k] after chunk k's last catch-up.
+struct ChunkRes {
+  cudaStream_t side[kMaxChunks] = {};
+  cudaEvent_t done[kMaxChunks] = {};
+  std::vector<cudaEvent_t> blk;
+  bool ready = false;
+};
+static ChunkRes g_chunk;
+
+static int chunk_setup(int nblk) {
+  if (!g_chunk.ready) {
+    int lo = 0, hi = 0;
+    MGB_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    for (int k = 0; k < 9; k++) {
+      MGB_CUDA(cudaStreamCreateWithPriority(&g_chunk.side[k], cudaStreamNonBlocking, lo));
+      MGB_CUDA(cudaEventCreateWithFlags(&g_chunk.done[k], cudaEventDisableTiming));
+    }
+    g_chunk.ready = true;
+  }
+  while ((int)g_chunk.blk.size() < nblk) {
+    cudaEvent_t e;
+    MGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    g_chunk.blk.push_back(e);
+  }
+  return 0;
+}
+
 template <typename T>
 int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
-            int lp) {
+            int lp, const ArrivalPlan *arr) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (n <= 0) return 0;
@@ -1800,6 +1830,70 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     amax_all = reinterpret_cast<unsigned *>(scb + 64);
     MGB_CUDA(cudaMemsetAsync(amax_all, 0, (size_t)12 * (nblk + 1), main));
   }
+  // Chunked arrival needs every finished block's swap map kept (the late
+  // chunks take the swaps then), the columns left of the blocks unswapped
+  // until the end (their L21 rows are used in the order they were factored
+  // in), the tensor-core updates (per-stream packing buffers) and chunks
+  // aligned to the blocks; otherwise every chunk is waited for first.
+  if (arr && (!defer || lp < 0 || lp == 3 || arr->cw % NB != 0 || arr->nchunks < 1 ||
+              arr->nchunks > 9)) {
+    for (int k = 0; k < arr->nchunks; k++) MGB_CUDA(cudaStreamWaitEvent(main, arr->ev[k], 0));
+    arr = nullptr;
+  }
+  if (arr) {
+    MGB_TRY(chunk_setup(nblk));
+    MGB_CUDA(cudaStreamWaitEvent(main, arr->ev[0], 0));
+    // the side streams' packing buffers, at their largest, before the loop
+    const int Kp = (int)((NB + 63) / 64 * 64);
+    for (int k = 1; k < arr->nchunks; k++)
+      for (int q = 0; q < 2; q++)
+        if (!ws(WS_CU0 + 3 * (k - 1) + q, (size_t)(n - NB) * Kp * 4) ||
+            !ws(WS_CU0 + 3 * (k - 1) + 2, 256))
+          return MATGB_ERR_NOMEM;
+  }
+  std::vector<char> kept((size_t)nblk, 0);
+  int joined = 1;  // chunks 0..joined-1 are in the main stream's updates
+  auto columns_in = [&]() -> int64_t {
+    if (!arr) return n;
+    const int64_t e = (int64_t)joined * arr->cw;
+    return e < n ? e : n;
+  };
+  // Chunk k (k >= 1) catches up on side stream k (low priority): once it has
+  // arrived and block j's pivots and swap map exist, block j's row swaps,
+  // U12 solve and trailing update are applied to its columns, block after
+  // block, while the factorisation goes on.  It joins the main stream's
+  // updates just before the look-ahead reaches its first block (the main
+  // stream waits there for its last catch-up step).
+  auto catch_up = [&](int64_t jb) -> int {
+    const int j = (int)(jb / NB);
+    const int64_t je = jb + NB;
+    for (int k = joined; k < arr->nchunks; k++) {
+      const int64_t c0 = (int64_t)k * arr->cw;
+      const int64_t c1 = c0 + arr->cw < n ? c0 + arr->cw : n;
+      if (je > c0) continue;  // (blocks inside a chunk come after its join)
+      cudaStream_t sk = g_chunk.side[k];
+      if (jb == 0) MGB_CUDA(cudaStreamWaitEvent(sk, arr->ev[k], 0));
+      MGB_CUDA(cudaStreamWaitEvent(sk, g_chunk.blk[j], 0));
+      StreamSwap sw(sk);
+      if (kept[j])
+        MGB_TRY(laswp_map<T>(A, lda, c0, c1, 0, 0, &maps[j], nullptr, NB));
+      else
+        MGB_TRY(laswp_t<T>(A, lda, c0, c1, 0, 0, ipiv, jb, je, nullptr));
+      bool u_dummy = false;
+      MGB_TRY(trsm_unit_lower<T>((int)NB, c1 - c0, A + jb + jb * lda, lda,
+                                 A + jb + c0 * lda, lda, nullptr, &u_dummy));
+      // the packing scales from this stream's own max slots (the block's
+      // shared slots would be raised by the other chunks' streams while
+      // this one's packing reads them)
+      if constexpr (sizeof(T) == 4)
+        MGB_TRY(lp_trailing_update(n, (float *)A, lda, jb, je, c0, c1, lp, true, nullptr,
+                                   false, false, k));
+      else
+        return set_error(MATGB_ERR_ARG, "chunked LU is float");
+      MGB_CUDA(cudaEventRecord(g_chunk.done[k], sk));
+    }
+    return 0;
+  };
   // main -> hi: everything queued so far (input copies, perm init, slots)
   MGB_CUDA(cudaEventRecord(g_la.ev[0], main));
   MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[0], 0));
@@ -1822,11 +1916,20 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       if (!done) bmap = nullptr;
       l21_ready = done && lp == 2;
       if (!done) MGB_TRY(factor_block<T>(n, A, lda, kb, ke, ipiv, eps));
+      kept[kb / NB] = defer && (bmap != nullptr || kb > 0);
     }
     MGB_CUDA(cudaEventRecord(g_la.ev[1], hi));
     MGB_CUDA(cudaStreamWaitEvent(main, g_la.ev[1], 0));
 
     const int64_t nn = (n - ke) < NB ? (n - ke) : NB;
+    // the look-ahead's columns must have joined (a plan that is too late
+    // for them costs a wait here, never a wrong result); the look-ahead
+    // then packs this block's L21 afresh
+    while (arr && joined < arr->nchunks && columns_in() < ke + nn) {
+      MGB_CUDA(cudaStreamWaitEvent(main, arr->ev[joined], 0));
+      MGB_CUDA(cudaStreamWaitEvent(main, g_chunk.done[joined], 0));
+      joined++;
+    }
     if (ke < n) {
       // look-ahead: the next block's columns are swapped, solved and updated
       // first, then the panel stream is released; everything else (the other
@@ -1845,20 +1948,27 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       MGB_CUDA(cudaEventRecord(g_la.ev[2], main));
       MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[2], 0));
     }
+    const int64_t cend = columns_in();
     // the columns right of the look-ahead (and, unless deferred, the columns
     // left of the block) and the permutation; a deferred pass keeps this
     // block's net map
+    const int64_t r1 = cend > ke + nn ? cend : ke + nn;
     if (bmap)
-      MGB_TRY(laswp_map<T>(A, lda, 0, defer ? 0 : kb, ke + nn, n, bmap, perm, nb));
+      MGB_TRY(laswp_map<T>(A, lda, 0, defer ? 0 : kb, ke + nn, r1, bmap, perm, nb));
     else
-      MGB_TRY(laswp_t<T>(A, lda, 0, defer ? 0 : kb, ke + nn, n, ipiv, kb, ke, perm,
+      MGB_TRY(laswp_t<T>(A, lda, 0, defer ? 0 : kb, ke + nn, r1, ipiv, kb, ke, perm,
                          defer && kb > 0 ? &maps[kb / NB] : nullptr));
-    if (ke + nn < n) {
+    if (arr && joined < arr->nchunks && nb == NB) {
+      // this block's pivots and swap map exist from here on (main stream)
+      MGB_CUDA(cudaEventRecord(g_chunk.blk[kb / NB], main));
+      MGB_TRY(catch_up(kb));
+    }
+    if (ke + nn < r1) {
       bool u12_ready = false;
-      MGB_TRY(trsm_unit_lower<T>((int)nb, n - ke - nn, A + kb + kb * lda, lda,
+      MGB_TRY(trsm_unit_lower<T>((int)nb, r1 - ke - nn, A + kb + kb * lda, lda,
                                  A + kb + (ke + nn) * lda, lda,
                                  amax3 ? amax3 + 2 : nullptr, &u12_ready));
-      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, n, lp, false, amax3,
+      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, r1, lp, false, amax3,
                                  l21_ready, u12_ready));
     }
   }
@@ -1909,7 +2019,8 @@ int precond_solve(bool spd, int64_t n, const float *W, const int32_t *perm,
                           SwapMap *);                                          \
   template int lu_panel_t<T>(T *, int64_t, int64_t, int64_t, int, int32_t *,  \
                              T, int *);                                        \
-  template int getrf_t<T>(int64_t, T *, int64_t, int32_t *, int32_t *, T, int); \
+  template int getrf_t<T>(int64_t, T *, int64_t, int32_t *, int32_t *, T, int,      \
+                          const ArrivalPlan *);                                     \
   template int getrs_t<T>(int64_t, int64_t, const T *, int64_t,               \
                           const int32_t *, const T *, int64_t, T *, int64_t);
 MGB_LU_INST(float)

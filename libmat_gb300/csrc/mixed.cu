@@ -166,15 +166,18 @@ static unsigned grid_cap(int64_t tot, int per = 256) {
 // Without amax3 the maxima are found here in a zeroed scratch slot.
 int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
                        int64_t ke, int64_t c0, int64_t c1, int lp, bool first,
-                       unsigned *amax3, bool l21_ready, bool u12_ready) {
+                       unsigned *amax3, bool l21_ready, bool u12_ready, int wset) {
   const int nb = (int)(ke - kb);
   const int Kp = (nb + 63) / 64 * 64;
   const int64_t m = n - ke, ncols = n - ke, nc = c1 - c0;
   const bool split = lp == 2;
   const size_t an = (size_t)m * Kp, bn_ = (size_t)ncols * Kp;
-  uint16_t *A16 = (uint16_t *)ws(WS_T0, an * 2 * (split ? 2 : 1));
-  uint16_t *B16 = (uint16_t *)ws(WS_T1, bn_ * 2 * (split ? 2 : 1));
-  float *scb = (float *)ws(WS_T2, 256);
+  const int s0 = wset == 0 ? WS_T0 : WS_CU0 + 3 * (wset - 1);
+  const int s1 = wset == 0 ? WS_T1 : s0 + 1, s2 = wset == 0 ? WS_T2 : s0 + 2;
+  if (wset < 0 || wset > 8) return set_error(MATGB_ERR_ARG, "lp_trailing_update: bad set");
+  uint16_t *A16 = (uint16_t *)ws(s0, an * 2 * (split ? 2 : 1));
+  uint16_t *B16 = (uint16_t *)ws(s1, bn_ * 2 * (split ? 2 : 1));
+  float *scb = (float *)ws(s2, 256);
   if (!A16 || !B16 || !scb) return MATGB_ERR_NOMEM;
   uint16_t *A16lo = split ? A16 + an : nullptr;
   uint16_t *B16lo = split ? B16 + bn_ : nullptr;
@@ -273,11 +276,11 @@ template <typename S>
 __global__ void to_float_rowsum_kernel(int64_t n, const S *__restrict__ A,
                                        int64_t lda, float *__restrict__ W,
                                        int64_t ldw, double *__restrict__ rowsum,
-                                       int chunk) {
+                                       int chunk, int64_t ncols) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t j0 = (int64_t)blockIdx.y * chunk;
-  const int64_t j1 = j0 + chunk < n ? j0 + chunk : n;
+  const int64_t j1 = j0 + chunk < ncols ? j0 + chunk : ncols;
   double s = 0;
 #pragma unroll 8
   for (int64_t j = j0; j < j1; j++) {
@@ -424,9 +427,32 @@ static IrEvents g_ir;
 constexpr int64_t kResid64MinN = 1024;
 static int g_resid64_on = 1;
 
+// Copy stream and events for a matrix that arrives from the host in column
+// chunks while the factorisation runs (ArrivalPlan).
+struct ArrivalRes {
+  cudaStream_t cs = nullptr;
+  cudaEvent_t start = nullptr;
+  cudaEvent_t ev[kMaxChunks] = {};
+  bool ready = false;
+};
+static ArrivalRes g_arr;
+// From this order up a host matrix is copied in chunks under the
+// factorisation (below it the copy is short).
+constexpr int64_t kArrivalMinN = 8192;
+
+static int arrival_setup() {
+  if (g_arr.ready) return 0;
+  MGB_CUDA(cudaStreamCreateWithFlags(&g_arr.cs, cudaStreamNonBlocking));
+  MGB_CUDA(cudaEventCreateWithFlags(&g_arr.start, cudaEventDisableTiming));
+  for (auto &e : g_arr.ev) MGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  g_arr.ready = true;
+  return 0;
+}
+
 int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
              const elem_t *B, int64_t ldb, elem_t *X, int64_t ldx,
-             const MatIROpts &o, MatIRReport *rep, int *not_spd) {
+             const MatIROpts &o, MatIRReport *rep, int *not_spd,
+             const elem_t *hA = nullptr) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (not_spd) *not_spd = 0;
@@ -479,21 +505,60 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   float ms_factor = 0.f;
   for (int attempt = 0; attempt < 2; attempt++) {
     MGB_CUDA(cudaEventRecord(g_ir.e[0], st));
-    {
-      constexpr int kChunk = 64;
+    constexpr int kChunk = 64;
+    ArrivalPlan plan;
+    const ArrivalPlan *pl = nullptr;
+    if (hA && attempt == 0) {
+      // the host matrix: copied in column chunks on a copy stream (into A,
+      // which the refinement's residuals read) and converted to FP32 chunk by
+      // chunk; the LU starts on the first chunk (ArrivalPlan)
+      MGB_TRY(arrival_setup());
+      constexpr int64_t blk = 144;  // the float LU's outer block
+      int64_t cw = n;
+      if (!spd && n >= kArrivalMinN && lda == n) {
+        // eight chunks: the LU starts after an eighth of the copy
+        cw = (n / 8) / blk * blk;
+        if (cw < 8 * blk) cw = 8 * blk;
+      }
+      plan.cw = cw;
+      plan.nchunks = (int)((n + cw - 1) / cw);
+      MGB_CUDA(cudaEventRecord(g_arr.start, st));
+      MGB_CUDA(cudaStreamWaitEvent(g_arr.cs, g_arr.start, 0));
+      for (int k = 0; k < plan.nchunks; k++) {
+        const int64_t c0 = (int64_t)k * cw, c1 = c0 + cw < n ? c0 + cw : n;
+        MGB_CUDA(cudaMemcpyAsync(const_cast<elem_t *>(A) + c0 * lda, hA + c0 * n,
+                                 (size_t)(n * (c1 - c0)) * sizeof(elem_t),
+                                 cudaMemcpyHostToDevice, g_arr.cs));
+        const dim3 g((unsigned)((n + 255) / 256), (unsigned)((c1 - c0 + kChunk - 1) / kChunk));
+        to_float_rowsum_kernel<elem_t><<<g, 256, 0, g_arr.cs>>>(
+            n, A + c0 * lda, lda, W + c0 * n, n, rowsum, kChunk, c1 - c0);
+        MGB_LAUNCHED("to_float");
+        plan.ev[k] = g_arr.ev[k];
+        MGB_CUDA(cudaEventRecord(plan.ev[k], g_arr.cs));
+      }
+      pl = &plan;
+      if (spd)  // the Cholesky takes the whole matrix
+        for (int k = 0; k < plan.nchunks; k++) MGB_CUDA(cudaStreamWaitEvent(st, plan.ev[k], 0));
+    } else {
       const dim3 g((unsigned)((n + 255) / 256), (unsigned)((n + kChunk - 1) / kChunk));
       to_float_rowsum_kernel<elem_t><<<g, 256, 0, st>>>(
-          n, A, lda, W, n, attempt == 0 ? rowsum : nullptr, kChunk);
+          n, A, lda, W, n, attempt == 0 ? rowsum : nullptr, kChunk, n);
       MGB_LAUNCHED("to_float");
-      if (attempt == 0) {
-        rowmax_kernel<<<grid_cap(n), 256, 0, st>>>(n, rowsum, red);
-        MGB_LAUNCHED("rowmax");
-      }
+    }
+    if (attempt == 0 && !pl) {
+      rowmax_kernel<<<grid_cap(n), 256, 0, st>>>(n, rowsum, red);
+      MGB_LAUNCHED("rowmax");
     }
     if (spd)
       MGB_TRY(potrf_t<float>(n, W, n, info, lp));
     else
-      MGB_TRY(getrf_t<float>(n, W, n, piv, piv + n, 0.f, lp));
+      MGB_TRY(getrf_t<float>(n, W, n, piv, piv + n, 0.f, lp, pl));
+    if (pl) {
+      // every chunk is in (the LU joined them all); then |A|inf
+      for (int k = 0; k < plan.nchunks; k++) MGB_CUDA(cudaStreamWaitEvent(st, plan.ev[k], 0));
+      rowmax_kernel<<<grid_cap(n), 256, 0, st>>>(n, rowsum, red);
+      MGB_LAUNCHED("rowmax");
+    }
     MGB_CUDA(cudaEventRecord(g_ir.e[1], st));
     MGB_CUDA(cudaEventSynchronize(g_ir.e[1]));
     if (attempt == 0) {
@@ -701,8 +766,9 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
 }
 
 int gesv_ir(int64_t n, const elem_t *A, int64_t lda, const elem_t *b,
-            elem_t *x, const MatIROpts &o, MatIRReport *rep) {
-  return solve_ir(false, n, 1, A, lda, b, n, x, n, o, rep, nullptr);
+            elem_t *x, const MatIROpts &o, MatIRReport *rep,
+            const elem_t *hA = nullptr) {
+  return solve_ir(false, n, 1, A, lda, b, n, x, n, o, rep, nullptr, hA);
 }
 
 }  // namespace mgb
@@ -829,14 +895,13 @@ int mat_solve_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,
   elem_t *db = (elem_t *)ws(WS_B, (size_t)n * sizeof(elem_t));
   elem_t *dx = (elem_t *)ws(WS_X, (size_t)n * sizeof(elem_t));
   if (!dA || !db || !dx) return MATGB_ERR_NOMEM;
-  MGB_CUDA(cudaMemcpyAsync(dA, A->data, (size_t)n * n * sizeof(elem_t),
-                           cudaMemcpyHostToDevice, st));
   MGB_CUDA(cudaMemcpyAsync(db, b->data, (size_t)n * sizeof(elem_t),
                            cudaMemcpyHostToDevice, st));
   MatIROpts o;
   matgb_ir_default_opts(&o);
   if (opts) o = *opts;
-  MGB_TRY(gesv_ir(n, dA, n, db, dx, o, rep));
+  // A is copied in column chunks while the factorisation runs
+  MGB_TRY(gesv_ir(n, dA, n, db, dx, o, rep, A->data));
   MGB_CUDA(cudaMemcpyAsync(x->data, dx, (size_t)n * sizeof(elem_t),
                            cudaMemcpyDeviceToHost, st));
   MGB_CUDA(cudaStreamSynchronize(st));

@@ -201,4 +201,9 @@ def test_batched_schedule_file_is_read(tmp_path):
         "assert L.c.matgb_batched_tune_get(16, 0, C.byref(a), C.byref(c)) == 0\n", "")],
         capture_output=True, text=True, env=env)
     assert r.returncode == 0, r.stderr
-    assert "batched_tune.json (10 entries)" in r.stdout
+    # every entry of the committed file is used: the per-queue schedule and,
+    # for the mixed-precision mode, the per-queue routing ("mixed_tc")
+    import json
+    with open(os.path.join(ROOT, "libmat_gb300", "batched_tune.json")) as fh:
+        entries = json.load(fh)["entries"]
+    assert f"batched_tune.json ({len(entries)} entries)" in r.stdout

@@ -17,7 +17,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from libmat_gb300 import rng
+from libmat_gb300 import MatIRReport, rng
 
 pytestmark = pytest.mark.gpu
 
@@ -252,6 +252,44 @@ def test_ir_f32_reaches_fp32_backward_error(gpu):
     b = rng.normal(56, (n,), np.float32)
     x, rep = L.mat_solve_ir(A, b, lp_format=1)
     assert rep["converged"] == 1 and rep["backward_error"] <= n * 2.0 ** -24, rep
+
+
+@pytest.mark.parametrize("n", [8192, 8292])
+def test_ir_host_matrix_in_chunks(gpu, n):
+    """mat_solve_ir with a host matrix from order 8192 up: A is copied in
+    column chunks while the LU runs (the chunks that arrive later catch up
+    with the blocks already factored).  The solution reaches the FP64
+    backward-error target and agrees with the device-pointer entry (A copied
+    first) to well within kappa * u."""
+    L = gpu["f64"]
+    rs = np.random.default_rng(n)
+    A = np.asfortranarray(rs.standard_normal((n, n)))
+    b = rs.standard_normal(n)
+    # three solves: the same factors each time (the chunks' catch-ups on
+    # their own streams must not race), the split's usual Krylov count
+    runs = [L.mat_solve_ir(A, b) for _ in range(3)]
+    for x, rep in runs:
+        assert rep["converged"] == 1 and rep["lp_format"] == 2, rep
+        assert rep["krylov_steps"] <= 12, rep
+    assert len({r["krylov_steps"] for _, r in runs}) == 1
+    x, rep = runs[0]
+    eta = np.abs(b - A @ x).max() / (np.abs(A).sum(1).max() * np.abs(x).max()
+                                     + np.abs(b).max())
+    assert eta <= n * 2.0 ** -53, (eta, rep)
+    dA, db, dx = L.dalloc(A.nbytes), L.dalloc(b.nbytes), L.dalloc(b.nbytes)
+    try:
+        L.h2d(dA, A)
+        L.h2d(db, b)
+        o = L.ir_opts()
+        rep2 = MatIRReport()
+        L.check(L.c.matgb_gesv_ir_dev(n, dA, n, db, dx, C.byref(o), C.byref(rep2)),
+                "gesv_ir_dev")
+        x2 = np.empty(n)
+        L.d2h(x2, dx)
+    finally:
+        for d in (dA, db, dx):
+            L.dfree(d)
+    assert np.abs(x - x2).max() / np.abs(x2).max() <= 1e-8
 
 
 def test_ir_reports_nonconvergence_for_singular(gpu):
