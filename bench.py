@@ -332,7 +332,10 @@ def run_headline(args, mg):
         "dtype": "f64 (FP32 factors, FP16 tensor-core updates, FP32 accumulate)",
         "gpu_launches": launches,
         "config": {"workload": f"mixed_lu_ir_{n}_f64", "n": n, "nrhs": 1,
-                   "kappas": list(KAPPAS), "factor_format": {2: "fp16 split (hi+lo, 3 products)", 1: "bf16",
+                   "kappas": list(KAPPAS),
+                   "factor_format": {3: "three-part fp16 split (hi+mid+lo, 6 products, "
+                                        "per-row/column scales)",
+                                     2: "fp16 split (hi+lo, 3 products)", 1: "bf16",
                                      0: "fp16", -1: "fp32 simt"}[args.lp],
                    "refinement": "FGMRES (FP64) preconditioned by the factors",
                    "A": "U diag(sigma) V^T, U,V from QR of seeded N(0,1)",
@@ -973,7 +976,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--lp", type=int, default=2,
-                    help="2 FP16 split (3 products), 0 FP16, 1 BF16, -1 FP32")
+                    help="3 three-part FP16 split (6 products), 2 FP16 split (3 "
+                         "products), 0 FP16, 1 BF16, -1 FP32")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--only", choices=["plain_f32", "spd", "batched", "lu_full", "blas_t",

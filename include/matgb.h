@@ -177,7 +177,10 @@ typedef struct {
                         powers of two and split into FP16 hi + remainder,
                         three tensor-core products per update (FP32-level
                         factors; refinement converges to kappa ~ 1e6 and
-                        beyond); 0 = FP16 (one product, U12 scaled);
+                        beyond); 3 = three-part FP16 split (hi + mid +
+                        remainder, six products, ~33 bits of each operand,
+                        per-row / per-column scales; LU only, the Cholesky
+                        takes 2); 0 = FP16 (one product, U12 scaled);
                         1 = BF16 (one product; at n ~ 1e4 too coarse to
                         refine past kappa ~ 1e2); -1 = FP32 SIMT updates    */
   int max_iter;      /* factor solves over all attempts (default 100)        */
@@ -244,8 +247,8 @@ int mat_solve_spd_ir(Vec *x, const Mat *A, const Vec *b, const MatIROpts *opts,
 int matgb_potrf_lp_dev(size_t n, float *A, size_t lda, int32_t *info,
                        int lp_format);
 /* The FP32 LU alone (device, in place) with trailing updates on the tensor
- * cores (lp_format 2 FP16 split, 1 BF16, 0 FP16) or, for lp_format -1, the
- * FP32 SIMT GEMM.
+ * cores (lp_format 3 three-part FP16 split, 2 FP16 split, 1 BF16, 0 FP16)
+ * or, for lp_format -1, the FP32 SIMT GEMM.
  * ipiv/perm as matgb_getrf_dev.  Pivots are never skipped (threshold 0). */
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
                        int32_t *perm, int lp_format);
@@ -278,6 +281,12 @@ int matgb_tc_gemm_split_dev(size_t M, size_t N, size_t K, const void *Ah,
 /* 0, or MATGB_ERR_TIMEOUT if a tensor-core kernel gave up a bounded wait
  * since the last call (clears the flag; synchronises). */
 int matgb_tc_status(void);
+/* Short-K tensor-core products (the trailing updates): 1 (default) = the
+ * persistent form (one CTA per SM, tiles from a counter, two TMEM
+ * accumulators so a tile's epilogue runs under the next tile's MMAs);
+ * 0 = one CTA per tile, two per SM.  -1 queries.  Returns the previous
+ * setting. */
+int matgb_tc_persistent(int on);
 
 /* y = alpha*A*x + beta*y like matgb_gemv_dev, for callers that must not
  * allocate device memory -- e.g. code that runs inside another runtime's

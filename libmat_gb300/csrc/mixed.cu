@@ -457,10 +457,10 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (not_spd) *not_spd = 0;
   if (n <= 0 || nrhs <= 0) return 0;
-  if (o.lp_format < -1 || o.lp_format > 2)
+  if (o.lp_format < -1 || o.lp_format > 3)
     return set_error(MATGB_ERR_ARG,
-                     "lp_format must be 2 (FP16 split), 1 (BF16), 0 (FP16) or "
-                     "-1 (FP32)");
+                     "lp_format must be 3 (three-part FP16 split), 2 (FP16 split), 1 "
+                     "(BF16), 0 (FP16) or -1 (FP32)");
   if (!g_ir.ready) {
     for (auto &e : g_ir.e) MGB_CUDA(cudaEventCreate(&e));
     g_ir.ready = true;
@@ -495,7 +495,8 @@ int solve_ir(bool spd, int64_t n, int64_t nrhs, const elem_t *A, int64_t lda,
   const double tol = o.tol > 0 ? o.tol : (double)n * eps;
   const int maxit = o.max_iter > 0 ? o.max_iter : 100;
 
-  int lp = o.lp_format;
+  // the three-part split is an LU form (the Cholesky takes the two-part one)
+  int lp = spd && o.lp_format == 3 ? 2 : o.lp_format;
   double eta = INFINITY, rn = 0, xn = 0, fwd = INFINITY;
   int it = 0, converged = 0, refinements = 0, ksteps = 0;
   const bool use_krylov = o.krylov != 0 && nrhs == 1;
@@ -810,7 +811,7 @@ int matgb_resid64_dev(size_t n, size_t nrhs, const mat_elem_t *A, size_t lda,
 int matgb_getrf_lp_dev(size_t n, float *A, size_t lda, int32_t *ipiv,
                        int32_t *perm, int lp_format) {
   if (lda < n) return set_error(MATGB_ERR_ARG, "getrf_lp: lda < n");
-  if (lp_format < -1 || lp_format > 2)
+  if (lp_format < -1 || lp_format > 3)
     return set_error(MATGB_ERR_ARG, "getrf_lp: lp_format");
   return getrf_t<float>((int64_t)n, A, (int64_t)lda, ipiv, perm, 0.f,
                         lp_format);

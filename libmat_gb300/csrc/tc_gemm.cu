@@ -267,10 +267,289 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
   }
 }
 
+// ---- persistent form (short K: the trailing updates) ------------------------
+// One CTA per SM pulls 128 x 256 tiles from a per-stream counter (dynamic, so
+// CTAs that start late -- behind the LU's panel kernel on some SMs -- take
+// fewer tiles), through a 4-stage ring, with two TMEM accumulators: the
+// epilogue of tile i (8 warps, three C chunks in flight per thread) runs
+// under the main loop of tile i+1.  Warp 8 lane 0 takes the tile indices and
+// issues the TMA loads; warp 9 allocates TMEM (512 columns) and issues the
+// MMAs; the tile indices reach the MMA thread and the epilogue warps through
+// a 4-slot ring.  Every wait is bounded as in tc_gemm_kernel.
+constexpr int kTcPTiles = 4;
+
+template <int BN, int ST>
+struct TcPSmem {
+  uint16_t a[ST][kTcBM * kTcBK];
+  uint16_t b[ST][BN * kTcBK];
+  uint64_t full[ST];
+  uint64_t empty[ST];
+  uint64_t acc_full[2];
+  uint64_t acc_empty[2];
+  uint64_t tfull[kTcPTiles];
+  uint64_t tempty[kTcPTiles];
+  uint64_t drain;
+  int tile[kTcPTiles];
+  uint32_t tmem_base;
+  volatile int timeout;
+};
+
+template <bool SC, int BN, int ST, int MINB>
+__global__ void __launch_bounds__(kTcThreads, MINB)
+    tc_gemm_pkernel(const __grid_constant__ CUtensorMap tmA0,
+                    const __grid_constant__ CUtensorMap tmA1,
+                    const __grid_constant__ CUtensorMap tmA2,
+                    const __grid_constant__ CUtensorMap tmB0,
+                    const __grid_constant__ CUtensorMap tmB1,
+                    const __grid_constant__ CUtensorMap tmB2, int M, int N,
+                    int kps, int nseg, unsigned amask, unsigned bmask,
+                    float alpha, const float *__restrict__ alpha_scale,
+                    float beta, float *__restrict__ C, int64_t ldc,
+                    uint32_t idesc, int tri, const int32_t *__restrict__ skip,
+                    const float *__restrict__ rinv, const float *__restrict__ cinv,
+                    int *__restrict__ err, int mtiles, int ntiles,
+                    int *__restrict__ ctr) {
+  extern __shared__ __align__(1024) unsigned char tcp_smem[];
+  constexpr int kTcPStages = ST;
+  TcPSmem<BN, ST> &s = *reinterpret_cast<TcPSmem<BN, ST> *>(
+      tcp_smem + ((1024u - (tc::smem_u32(tcp_smem) & 1023u)) & 1023u));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nkb = kps * nseg, ntot = mtiles * ntiles;
+  if (skip && *skip != 0) return;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kTcPStages; i++) {
+      tc::mbar_init(&s.full[i], 1);
+      tc::mbar_init(&s.empty[i], 1);
+    }
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&s.acc_full[i], 1);
+      tc::mbar_init(&s.acc_empty[i], 8);
+    }
+    for (int i = 0; i < kTcPTiles; i++) {
+      tc::mbar_init(&s.tfull[i], 1);
+      tc::mbar_init(&s.tempty[i], 9);
+    }
+    tc::mbar_init(&s.drain, 1);
+    s.timeout = 0;
+    tc::fence_barrier_init();
+  }
+  if (warp == 9) tc::tmem_alloc(&s.tmem_base, 2 * BN);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = s.tmem_base;
+
+  if (warp == 8 && lane == 0) {
+    // ---- tile indices and TMA loads
+    tc::prefetch_tmap(&tmA0);
+    tc::prefetch_tmap(&tmB0);
+    int g = 0;
+    for (int i = 0;; i++) {
+      const int slot = i % kTcPTiles, use = i / kTcPTiles;
+      if (use > 0 && !tc::mbar_wait(&s.tempty[slot], (use - 1) & 1, kTcWaitLimit, kTcSpin)) {
+        s.timeout = 1;
+        break;
+      }
+      int t = -1;
+      while (!s.timeout) {
+        const int c = atomicAdd(ctr, 1);
+        if (c >= ntot) break;
+        const int m0 = (c % mtiles) * kTcBM, n0 = (c / mtiles) * BN;
+        if (tri == 1 && n0 >= m0 + kTcBM) continue;  // strictly above the diagonal
+        if (tri == 2 && m0 >= n0 + BN) continue;
+        t = c;
+        break;
+      }
+      s.tile[slot] = t;
+      tc::mbar_arrive(&s.tfull[slot]);
+      if (t < 0) break;
+      const int m0 = (t % mtiles) * kTcBM, n0 = (t / mtiles) * BN;
+      for (int kb = 0; kb < nkb; kb++, g++) {
+        const int st = g % kTcPStages, u = g / kTcPStages;
+        if (u > 0 && !tc::mbar_wait(&s.empty[st], (u - 1) & 1, kTcWaitLimit, kTcSpin)) {
+          s.timeout = 1;
+          break;
+        }
+        if (s.timeout) break;
+        const int seg = kb / kps, kx = (kb % kps) * kTcBK;
+        const unsigned sa = (amask >> (2 * seg)) & 3u, sb = (bmask >> (2 * seg)) & 3u;
+        const CUtensorMap *ma = sa == 2 ? &tmA2 : sa == 1 ? &tmA1 : &tmA0;
+        const CUtensorMap *mb = sb == 2 ? &tmB2 : sb == 1 ? &tmB1 : &tmB0;
+        tc::mbar_arrive_expect_tx(&s.full[st], (kTcBM + BN) * kTcBK * 2);
+        tc::tma_load_2d(s.a[st], ma, kx, m0, &s.full[st]);
+        tc::tma_load_2d(s.b[st], mb, kx, n0, &s.full[st]);
+      }
+      if (s.timeout) break;
+    }
+    // no copy may still be in flight when the CTA leaves
+    for (int q = g - kTcPStages > 0 ? g - kTcPStages : 0; q < g; q++)
+      tc::mbar_wait(&s.full[q % kTcPStages], (q / kTcPStages) & 1, kTcWaitLimit);
+  } else if (warp == 9 && lane == 0) {
+    // ---- MMAs into accumulator i % 2
+    int g = 0;
+    bool issued = false;
+    for (int i = 0;; i++) {
+      const int slot = i % kTcPTiles, use = i / kTcPTiles;
+      if (!tc::mbar_wait(&s.tfull[slot], use & 1, kTcWaitLimit, kTcSpin)) {
+        s.timeout = 1;
+        atomicExch(err, 1);
+        break;
+      }
+      const int t = s.tile[slot];
+      tc::mbar_arrive(&s.tempty[slot]);
+      if (t < 0 || s.timeout) break;
+      const int a = i & 1, au = i >> 1;
+      if (au > 0 && !tc::mbar_wait(&s.acc_empty[a], (au - 1) & 1, kTcWaitLimit, kTcSpin)) {
+        s.timeout = 1;
+        atomicExch(err, 1);
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t acc = tmem + (uint32_t)(a * BN);
+      bool ok = true;
+      for (int kb = 0; kb < nkb; kb++, g++) {
+        const int st = g % kTcPStages, u = g / kTcPStages;
+        if (s.timeout || !tc::mbar_wait(&s.full[st], u & 1, kTcWaitLimit, kTcSpin)) {
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t a0 = tc::smem_u32(s.a[st]), b0 = tc::smem_u32(s.b[st]);
+#pragma unroll
+        for (int kk = 0; kk < kTcBK / 16; kk++)
+          tc::mma_f16(acc, tc::desc_k_sw128(a0 + kk * 32), tc::desc_k_sw128(b0 + kk * 32),
+                      idesc, (kb | kk) ? 1u : 0u);
+        issued = true;
+        tc::mma_commit(&s.empty[st]);
+      }
+      tc::mma_commit(&s.acc_full[a]);
+      if (!ok) {
+        s.timeout = 1;
+        atomicExch(err, 1);
+        break;
+      }
+    }
+    // every MMA this thread issued has finished before TMEM is freed
+    if (issued) {
+      tc::mma_commit(&s.drain);
+      tc::mbar_wait(&s.drain, 0, kTcWaitLimit);
+    }
+  } else if (warp < 8) {
+    // ---- epilogue: warp w reads TMEM lane quarter w%4, column half w/4
+    constexpr int CH = 16, NCH = BN / 2 / CH;
+    const int q = warp & 3, half = warp >> 2;
+    const bool rd = beta != 0.f;
+    for (int i = 0;; i++) {
+      const int slot = i % kTcPTiles, use = i / kTcPTiles;
+      if (!tc::mbar_wait(&s.tfull[slot], use & 1, kTcWaitLimit)) {
+        atomicExch(err, 2);
+        break;
+      }
+      const int t = s.tile[slot];
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&s.tempty[slot]);
+      if (t < 0 || s.timeout) break;
+      const int m0 = (t % mtiles) * kTcBM, n0 = (t / mtiles) * BN;
+      const int row = m0 + q * 32 + lane;
+      const int cbase = n0 + half * (BN / 2);
+      const bool rok = row < M;
+      float *cp = C + (int64_t)cbase * ldc + row;
+      auto load = [&](float (&d)[CH], int ch) {
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+          const int col = ch * CH + j;
+          d[j] = (rok && rd && cbase + col < N) ? cp[(int64_t)col * ldc] : 0.f;
+        }
+      };
+      // C chunks 0 and 1 in flight before the accumulator is ready, and two
+      // ahead of the one being finished after that
+      float c0[CH], c1[CH];
+      load(c0, 0);
+      if (NCH > 1) load(c1, 1);
+      float rs = 1.f;
+      if constexpr (SC) rs = rok ? __ldg(&rinv[row]) : 1.f;
+      const int a = i & 1, au = i >> 1;
+      const bool ready = tc::mbar_wait(&s.acc_full[a], au & 1, kTcWaitLimit);
+      tc::tc_fence_after();
+      if (!ready) {
+        atomicExch(err, 2);
+        break;
+      }
+      const float al = alpha_scale ? alpha * (*alpha_scale) : alpha;
+#pragma unroll 1
+      for (int ch = 0; ch < NCH; ch++) {
+        float c2[CH];
+        if (ch + 2 < NCH) load(c2, ch + 2);
+        float cs[CH];
+        if constexpr (SC) {
+#pragma unroll
+          for (int j = 0; j < CH; j++) {
+            const int col = cbase + ch * CH + j;
+            cs[j] = col < N ? __ldg(&cinv[col]) : 1.f;
+          }
+        }
+        float v[CH];
+        tc::tmem_ld16(tmem + (uint32_t)(a * BN) + ((uint32_t)(q * 32) << 16) +
+                          (uint32_t)(half * (BN / 2) + ch * CH),
+                      v);
+        if (rok) {
+#pragma unroll
+          for (int j = 0; j < CH; j++) {
+            const int col = ch * CH + j;
+            const bool in = tri == 0 || (tri == 1 ? cbase + col <= row : cbase + col >= row);
+            if (cbase + col < N && in) {
+              if constexpr (SC)
+                cp[(int64_t)col * ldc] = fmaf(al, (v[j] * rs) * cs[j], beta * c0[j]);
+              else
+                cp[(int64_t)col * ldc] = fmaf(al, v[j], beta * c0[j]);
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+          c0[j] = c1[j];
+          c1[j] = c2[j];
+        }
+      }
+      // this accumulator is read: the MMAs of tile i+2 may overwrite it
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&s.acc_empty[a]);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 9) {
+    __syncwarp();
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 2 * BN);
+  }
+}
+
 // ---- host side ----------------------------------------------------------------
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 static int *g_tc_err = nullptr;
 static bool g_tc_ready = false;
+// The persistent form's tile counters, one per stream that launches it (the
+// launches of one stream are ordered, so each is zeroed before its launch
+// without racing another launch that still uses it).
+constexpr int kTcCtrs = 32;
+static int *g_tc_ctr = nullptr;
+static cudaStream_t g_tc_ctr_stream[kTcCtrs];
+static int g_tc_nctr = 0;
+static int *tile_counter(cudaStream_t st) {
+  for (int i = 0; i < g_tc_nctr; i++)
+    if (g_tc_ctr_stream[i] == st) return g_tc_ctr + i;
+  if (g_tc_nctr == kTcCtrs) return nullptr;
+  g_tc_ctr_stream[g_tc_nctr] = st;
+  return g_tc_ctr + g_tc_nctr++;
+}
+// 1 (default): short-K products take the persistent form; 0: the 2-stage
+// two-CTAs-per-SM form (matgb_tc_persistent).
+static int g_tc_persistent = 1;
+// the persistent form's tile width and ring depth: two CTAs per SM
+// (2 x 3 stages x 32 KB of shared memory, 2 x 2 x 128 TMEM columns)
+constexpr int kTcPBN = 128, kTcPST = 3;
 
 template <int ST>
 static constexpr size_t tc_smem_bytes() {
@@ -300,6 +579,10 @@ static int tc_setup() {
   MGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<4, 1, true>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)tc_smem_bytes<4>()));
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_pkernel<false, kTcPBN, kTcPST, 2>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(TcPSmem<kTcPBN, kTcPST>) + 1024)));
+  MGB_CUDA(cudaMalloc(&g_tc_ctr, kTcCtrs * sizeof(int)));
   g_tc_ready = true;
   return 0;
 }
@@ -390,7 +673,27 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
       ma, mal, mam, mb, mbl, mbm, (int)M, (int)N, (int)(K / kTcBK), nseg,      \
       amask, bmask,                                                            \
       alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv, g_tc_err)
-  if (deep && sc)
+  // the persistent form serves the unscaled short-K products (its scaled
+  // epilogue does not fit the two-CTA register budget)
+  int *ctr = (!deep && !sc && g_tc_persistent) ? tile_counter(cx->stream) : nullptr;
+  if (ctr) {
+    CUtensorMap pb, pbl, pbm;  // B boxes of the persistent form's tile width
+    MGB_TRY(make_map(&pb, B, bf16, N, K, ldb, kTcPBN));
+    if (split) MGB_TRY(make_map(&pbl, Blo, bf16, N, K, ldb, kTcPBN)); else pbl = pb;
+    if (split3) MGB_TRY(make_map(&pbm, Bmid, bf16, N, K, ldb, kTcPBN)); else pbm = pb;
+    const int mt = (int)((M + kTcBM - 1) / kTcBM), nt = (int)((N + kTcPBN - 1) / kTcPBN);
+    const int g = mt * nt < 2 * cx->sms ? mt * nt : 2 * cx->sms;
+    const uint32_t pidesc = tc::idesc_f16(bf16 ? 1 : 0, kTcBM, kTcPBN);
+    MGB_CUDA(cudaMemsetAsync(ctr, 0, sizeof(int), cx->stream));
+#define MGB_TC_PLAUNCH(SC_)                                                        \
+  tc_gemm_pkernel<SC_, kTcPBN, kTcPST, 2>                                          \
+      <<<g, kTcThreads, sizeof(TcPSmem<kTcPBN, kTcPST>) + 1024, cx->stream>>>(     \
+          ma, mal, mam, pb, pbl, pbm, (int)M, (int)N, (int)(K / kTcBK), nseg,      \
+          amask, bmask, alpha, alpha_scale, beta, C, ldc, pidesc, lower, skip,     \
+          rinv, cinv, g_tc_err, mt, nt, ctr)
+    MGB_TC_PLAUNCH(false);
+#undef MGB_TC_PLAUNCH
+  } else if (deep && sc)
     MGB_TC_LAUNCH(4, 1, true);
   else if (deep)
     MGB_TC_LAUNCH(4, 1, false);
@@ -435,6 +738,12 @@ int matgb_tc_gemm_split_dev(size_t M, size_t N, size_t K, const void *Ah,
   return tc_gemm(0, (int64_t)M, (int64_t)N, (int64_t)K, Ah, (int64_t)lda, Bh,
                  (int64_t)ldb, alpha, nullptr, beta, C, (int64_t)ldc, 0,
                  nullptr, Al, Bl);
+}
+
+int matgb_tc_persistent(int on) {
+  const int prev = g_tc_persistent;
+  if (on >= 0) g_tc_persistent = on ? 1 : 0;
+  return prev;
 }
 
 int matgb_tc_status(void) {

@@ -34,6 +34,12 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar,
       : "memory");
 }
 
+// Plain arrival (release semantics at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
 __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
