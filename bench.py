@@ -861,20 +861,51 @@ def _pin_one_core():
     return core
 
 
-def _neon_worker(n_list, budget_s, seed, q):
-    """In a fresh process pinned to one core: time the NEON-path mat_solve
+def _cpu_solver(own=False):
+    """The timed CPU solve: the NEON-path restatement of the reference's
+    mat_solve (oracle/neon_port.c; the conservative baseline -- the
+    reference's own double NEON path does not compile on aarch64, so its own
+    double build there is its slower SCALAR path), or with own=True the
+    reference's own mat_solve built from its header (the copy in
+    oracle/_ref/src travels to the GPU host; -O3, single-threaded).
+    Returns (solve, arch, kind, what) or None when own=True and that build
+    is absent."""
+    from oracle import loader
+    if own:
+        try:
+            if loader.ref_dir() and not loader.available("f64", "time"):
+                loader.build()
+            if loader.available("f64", "time"):
+                o = loader.Oracle("f64", "time")
+                return (o.solve, o.arch(), "reference",
+                        "the reference's own mat_solve (its mat.h built with -O3, "
+                        "single-threaded)")
+        except Exception:
+            pass
+        return None
+    N = loader.NeonPort()
+    return (N.solve, N.arch(), "port",
+            "reference mat_solve algorithm (NEON path: blocked PLU with the packed "
+            "8x4 micro-kernel, restated in oracle/neon_port.c)")
+
+
+def _neon_worker(n_list, budget_s, seed, q, own=False):
+    """In a fresh process pinned to one core: time the reference's mat_solve
     at the largest order in n_list that finishes within budget_s, return
-    (n, seconds per solve, solves, arch, core)."""
+    (n, seconds per solve, solves, arch, core, kind, what), or None."""
     core = _pin_one_core()
-    from oracle.loader import NeonPort
     from libmat_gb300 import rng
-    N = NeonPort()
+    got = _cpu_solver(own)
+    if got is None:
+        q.put(None)
+        return
+    solve, arch, kind, what = got
     # calibrate on the smallest order
     n0 = n_list[0]
     A = rng.normal(seed, (n0, n0), np.float64)
     b = rng.normal(seed + 1, (n0,), np.float64)
     t0 = time.perf_counter()
-    N.solve(A, b)
+    solve(A, b)
     t_n0 = time.perf_counter() - t0
     n = n0
     for cand in n_list:
@@ -884,57 +915,77 @@ def _neon_worker(n_list, budget_s, seed, q):
     b = rng.normal(seed + 3, (n,), np.float64)
     reps, t0 = 0, time.perf_counter()
     while True:
-        N.solve(A, b)
+        solve(A, b)
         reps += 1
         el = time.perf_counter() - t0
         if el > budget_s * 0.5 or reps >= 20:
             break
-    q.put((n, el / reps, reps, N.arch(), core))
+    q.put((n, el / reps, reps, arch, core, kind, what))
 
 
-def neon_sample(n_list=(1024, 2048, 3072, 4096), budget_s=20.0, seed=1001):
+def neon_sample(n_list=(1024, 2048, 3072, 4096), budget_s=20.0, seed=1001, own=False):
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    p = ctx.Process(target=_neon_worker, args=(n_list, budget_s, seed, q))
+    p = ctx.Process(target=_neon_worker, args=(n_list, budget_s, seed, q, own))
     p.start()
     out = q.get(timeout=budget_s * 10 + 120)
     p.join()
     return out
 
 
+def own_build_sample():
+    """The reference's own double build on this host, timed beside the
+    baseline (None where it is absent)."""
+    got = neon_sample((512, 1024, 2048), budget_s=10.0, seed=1101, own=True)
+    if got is None:
+        return None
+    n, per, reps, arch, core, _, what = got
+    flops = 2 * n ** 3 / 3 + 2 * n * n
+    out = {"value": flops / per / 1e12, "unit": "TFLOP/s", "cores": 1,
+           "mat_arch": arch,
+           "sample": f"{what} in f64 at n={n}, {reps} solves, {per:.2f} s per "
+                     f"solve, core {core} pinned"}
+    import platform
+    if arch != "NEON" and platform.machine() in ("aarch64", "arm64"):
+        out["note"] = ("its double NEON path does not compile on aarch64 (gcc 13: "
+                       "vfmaq_laneq_f64 lanes 2 and 3 of a two-lane vector, "
+                       "mat.h:5439-5440): this is its SCALAR path")
+    return out
+
+
 def cpu_sample():
-    """The reference's mat_solve (NEON path restated) in double on one pinned
-    host core, at the largest order that fits a ~20 s budget.  TFLOP/s."""
-    n, per, reps, arch, core = neon_sample()
+    """The reference's mat_solve in double on one pinned host core, at the
+    largest order that fits a ~20 s budget (the NEON-path restatement), with
+    the reference's own build timed beside it.  TFLOP/s."""
+    n, per, reps, arch, core, kind, what = neon_sample()
     flops = 2 * n ** 3 / 3 + 2 * n * n
     return {"value": flops / per / 1e12, "unit": "TFLOP/s", "cores": 1,
-            "kind": "port",
-            "sample": f"reference mat_solve algorithm (NEON path: blocked PLU "
-                      f"with the packed 8x4 micro-kernel, restated in "
-                      f"oracle/neon_port.c) in f64 at n={n}, {reps} solves, "
+            "kind": kind,
+            "sample": f"{what} in f64 at n={n}, {reps} solves, "
                       f"{per:.2f} s per solve, core {core} pinned",
-            "mat_arch": arch}
+            "mat_arch": arch, "reference_own_build": own_build_sample()}
 
 
 def run_reference(args):
     """Reference arm: the reference's CPU algorithm for the headline solve
-    (mat_solve in double, NEON path restated), single-threaded on one pinned
-    host core as the reference runs; each step one solve at the largest order
-    whose warm-up + timed steps fit about two minutes."""
+    (mat_solve in double, its NEON path as restated in oracle/neon_port.c --
+    its own double NEON code does not compile on aarch64), single-threaded on
+    one pinned host core as the reference runs; each step one solve at the
+    largest order whose warm-up + timed steps fit about two minutes.  The
+    reference's own double build (its SCALAR path there) is timed beside it."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     core = _pin_one_core()
-    from oracle.loader import NeonPort
     from libmat_gb300 import rng
-    N = NeonPort()
+    solve, arch, kind, what = _cpu_solver()
     total = max(1, args.steps + args.warmup)
     n0 = 1024
     A = rng.normal(7, (n0, n0), np.float64)
     b = rng.normal(8, (n0,), np.float64)
     t0 = time.perf_counter()
-    N.solve(A, b)
+    solve(A, b)
     t_n0 = time.perf_counter() - t0
     n = n0
     for cand in (1024, 1536, 2048, 3072, 4096, 6144, 8192):
@@ -942,18 +993,17 @@ def run_reference(args):
             n = cand
     flops = 2 * n ** 3 / 3 + 2 * n * n
     for i in range(args.warmup):
-        N.solve(rng.normal(100 + i, (n, n), np.float64),
-                rng.normal(200 + i, (n,), np.float64))
+        solve(rng.normal(100 + i, (n, n), np.float64),
+              rng.normal(200 + i, (n,), np.float64))
     mats = [(rng.normal(5000 + i, (n, n), np.float64),
              rng.normal(6000 + i, (n,), np.float64)) for i in range(min(args.steps, 3))]
     t0 = time.perf_counter()
     for i in range(args.steps):
         A, b = mats[i % len(mats)]
-        N.solve(A, b)
+        solve(A, b)
     el = time.perf_counter() - t0
     tf = flops * args.steps / el / 1e12
-    sample = (f"one f64 solve of n={n} per step (the reference's mat_solve, "
-              f"NEON path restated in oracle/neon_port.c), core {core} pinned")
+    sample = f"one f64 solve of n={n} per step ({what}), core {core} pinned"
     line = {
         "impl": "reference", "metric": METRIC, "value": tf, "unit": "TFLOP/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -961,7 +1011,8 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "mixed_lu_ir_16384_f64", "sample": sample},
         "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": 1,
-                         "kind": "port", "sample": sample, "mat_arch": N.arch()},
+                         "kind": kind, "sample": sample, "mat_arch": arch,
+                         "reference_own_build": own_build_sample()},
         "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }

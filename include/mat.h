@@ -292,4 +292,15 @@ MATGB_API void mat_solve_trilt(Vec *x, const Mat *L, const Vec *b);
 }
 #endif
 
+/* A translation unit that defines MAT_IMPLEMENTATION gets the standard
+ * headers the reference's implementation section includes (mat.h:858-862),
+ * as code written against the reference may rely on them. */
+#ifdef MAT_IMPLEMENTATION
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#endif
+
 #endif /* MAT_H_ */
