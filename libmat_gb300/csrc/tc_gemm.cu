@@ -480,14 +480,6 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
       for (int ch = 0; ch < NCH; ch++) {
         float c2[CH];
         if (ch + 2 < NCH) load(c2, ch + 2);
-        float cs[CH];
-        if constexpr (SC) {
-#pragma unroll
-          for (int j = 0; j < CH; j++) {
-            const int col = cbase + ch * CH + j;
-            cs[j] = col < N ? __ldg(&cinv[col]) : 1.f;
-          }
-        }
         float v[CH];
         tc::tmem_ld16(tmem + (uint32_t)(a * BN) + ((uint32_t)(q * 32) << 16) +
                           (uint32_t)(half * (BN / 2) + ch * CH),
@@ -498,8 +490,11 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
             const int col = ch * CH + j;
             const bool in = tri == 0 || (tri == 1 ? cbase + col <= row : cbase + col >= row);
             if (cbase + col < N && in) {
+              // (the column's scale read here, not staged: the two-CTA
+              // register budget)
               if constexpr (SC)
-                cp[(int64_t)col * ldc] = fmaf(al, (v[j] * rs) * cs[j], beta * c0[j]);
+                cp[(int64_t)col * ldc] =
+                    fmaf(al, (v[j] * rs) * __ldg(&cinv[cbase + col]), beta * c0[j]);
               else
                 cp[(int64_t)col * ldc] = fmaf(al, v[j], beta * c0[j]);
             }
@@ -580,6 +575,9 @@ static int tc_setup() {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)tc_smem_bytes<4>()));
   MGB_CUDA(cudaFuncSetAttribute(tc_gemm_pkernel<false, kTcPBN, kTcPST, 2>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(TcPSmem<kTcPBN, kTcPST>) + 1024)));
+  MGB_CUDA(cudaFuncSetAttribute(tc_gemm_pkernel<true, kTcPBN, kTcPST, 2>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(TcPSmem<kTcPBN, kTcPST>) + 1024)));
   MGB_CUDA(cudaMalloc(&g_tc_ctr, kTcCtrs * sizeof(int)));
@@ -673,9 +671,7 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
       ma, mal, mam, mb, mbl, mbm, (int)M, (int)N, (int)(K / kTcBK), nseg,      \
       amask, bmask,                                                            \
       alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv, g_tc_err)
-  // the persistent form serves the unscaled short-K products (its scaled
-  // epilogue does not fit the two-CTA register budget)
-  int *ctr = (!deep && !sc && g_tc_persistent) ? tile_counter(cx->stream) : nullptr;
+  int *ctr = (!deep && g_tc_persistent) ? tile_counter(cx->stream) : nullptr;
   if (ctr) {
     CUtensorMap pb, pbl, pbm;  // B boxes of the persistent form's tile width
     MGB_TRY(make_map(&pb, B, bf16, N, K, ldb, kTcPBN));
@@ -691,7 +687,10 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
           ma, mal, mam, pb, pbl, pbm, (int)M, (int)N, (int)(K / kTcBK), nseg,      \
           amask, bmask, alpha, alpha_scale, beta, C, ldc, pidesc, lower, skip,     \
           rinv, cinv, g_tc_err, mt, nt, ctr)
-    MGB_TC_PLAUNCH(false);
+    if (sc)
+      MGB_TC_PLAUNCH(true);
+    else
+      MGB_TC_PLAUNCH(false);
 #undef MGB_TC_PLAUNCH
   } else if (deep && sc)
     MGB_TC_LAUNCH(4, 1, true);
