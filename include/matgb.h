@@ -74,6 +74,12 @@ double matgb_event_elapsed_ms(int slot0, int slot1);
 int matgb_ktime_enable(int on);
 int matgb_ktime_get(int i, char *name, int cap, long long *launches,
                     double *ms, double *flops, double *bytes);
+/* The i-th timed scope in launch order: its name, start and end in
+ * milliseconds from the first scope's start, and its stream (numbered by
+ * first appearance: 0 is the library stream when it launched first).  A
+ * timeline of the streams; synchronises the device; non-zero past the end. */
+int matgb_ktime_trace(int i, char *name, int cap, double *t0_ms, double *t1_ms,
+                      int *stream);
 /* Peak issue rate of the SIMT FMA pipes, measured with a dependent-chain-free
  * FMA kernel: which = 0 for FP32 (FFMA), 1 for FP64 (DFMA).  TFLOP/s. */
 double matgb_measure_fma_peak(int which);
@@ -282,11 +288,17 @@ int matgb_tc_gemm_split_dev(size_t M, size_t N, size_t K, const void *Ah,
  * since the last call (clears the flag; synchronises). */
 int matgb_tc_status(void);
 /* Short-K tensor-core products (the trailing updates): 1 (default) = the
- * persistent form (one CTA per SM, tiles from a counter, two TMEM
- * accumulators so a tile's epilogue runs under the next tile's MMAs);
- * 0 = one CTA per tile, two per SM.  -1 queries.  Returns the previous
- * setting. */
+ * persistent form (two CTAs per SM pulling 128 x 128 tiles from a counter,
+ * two TMEM accumulators each so a tile's epilogue runs under the next
+ * tile's MMAs); 0 = one CTA per 128 x 256 tile.  -1 queries.  Returns the
+ * previous setting. */
 int matgb_tc_persistent(int on);
+/* The mixed LU's look-ahead after a fused 144-column block (split FP16
+ * update): 1 (default) = the next block's row swaps, U12 solve and both
+ * operands' packing in one launch, U12 scaled per column; 0 = the separate
+ * swap, solve and packing launches with one U12 scale.  -1 queries.
+ * Returns the previous setting. */
+int matgb_la_prep(int on);
 
 /* y = alpha*A*x + beta*y like matgb_gemv_dev, for callers that must not
  * allocate device memory -- e.g. code that runs inside another runtime's

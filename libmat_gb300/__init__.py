@@ -96,6 +96,10 @@ class Lib:
                                      C.POINTER(C.c_double),
                                      C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]),
+            "matgb_ktime_trace": (_I, [_I, C.c_char_p, _I,
+                                       C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int)]),
             "matgb_measure_fma_peak": (C.c_double, [_I]),
             "matgb_plain_tensor_core": (_I, [_I]),
             "matgb_device_alloc": (_P, [_S]),
@@ -155,6 +159,7 @@ class Lib:
                                        C.c_float, C.c_float, _P, _S]),
             "matgb_tc_status": (_I, []),
             "matgb_tc_persistent": (_I, [_I]),
+            "matgb_la_prep": (_I, [_I]),
             "matgb_tc_gemm_split_dev": (_I, [_S, _S, _S, _P, _P, _S, _P, _P, _S,
                                              C.c_float, C.c_float, _P, _S]),
             "matgb_getrf_lp_dev": (_I, [_S, _P, _S, _P, _P, _I]),

@@ -57,6 +57,8 @@ enum WsSlot {
   WS_A = 0, WS_B, WS_C, WS_X, WS_L, WS_U, WS_PIV, WS_INFO,
   WS_T0, WS_T1, WS_T2, WS_T3, WS_V0, WS_V1, WS_K, WS_KV, WS_RS, WS_SWM, WS_SWG,
   WS_RZA, WS_RZB, WS_RZC, WS_RZE, WS_TCA, WS_TCB, WS_TCS, WS_QR,
+  // the mixed look-ahead's U12 column scales and L21 scale (la_prep)
+  WS_LAS,
   // the tensor-core trailing update's packing buffers, one set per side
   // stream of a chunked factorisation (set 0 is WS_T0..WS_T2)
   WS_CU0,
@@ -172,7 +174,8 @@ int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
 // Alo/Blo (may be null): remainders of A and B for the three-product split.
 // lower: 0 every element, 1 lower triangle, 2 upper triangle (tiles and
 // elements outside it are skipped); rinv/cinv (may be null): per-row and
-// per-column power-of-two factors applied to the product before alpha.
+// per-column power-of-two factors applied to the product before alpha (rinv
+// only together with cinv).
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
             const float *alpha_scale, float beta, float *C, int64_t ldc,

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "lp_pack.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -1399,6 +1400,235 @@ static int trsm_unit_lower(int tb, int64_t ncols, const T *L, int64_t ldl, T *B,
   return trsm_left_t<T>(true, false, true, tb, ncols, L, ldl, B, ldb, nullptr);
 }
 
+// ---- the mixed look-ahead's operands in one launch --------------------------
+// After a fused block (TB pivots, its net row map on the device), the
+// split tensor-core update of the next block's nn columns needs those
+// columns swapped, U12 = L11^{-1} A12 solved, U12 and L21 packed as FP16
+// hi + remainder -- otherwise four launches on the look-ahead's critical
+// path.  One launch, two roles:
+//  * CTAs [0, ncb): eight columns each, one warp per column: the block's row
+//    swaps on the column (laswp_kernel's moves), the solve (the arithmetic of
+//    trsm_unit_warp_kernel, with L11 staged by cp.async under the swaps), and
+//    the column packed with a power-of-two scale of its own (cinv[j] = its
+//    inverse, applied in the product's epilogue);
+//  * the other CTAs: L21 (rows ke.., the block's columns) packed with the
+//    block's scale s_L from the fused kernel's max, 32-row slabs transposed
+//    through shared memory (pack_l21_kernel's output).
+// CTA 0 leaves 1/s_L for the epilogue.  A per-column scale keeps every U12
+// column's entries as far from FP16's subnormals as the block scale keeps
+// the largest.
+template <int TB>
+__global__ void __launch_bounds__(256)
+    la_prep_kernel(float *__restrict__ A, int64_t lda, int64_t n, int64_t kb, int nn,
+                   const SwapMap *__restrict__ map, const unsigned *__restrict__ amax_l,
+                   int ncb, uint16_t *__restrict__ a16, uint16_t *__restrict__ a16lo,
+                   uint16_t *__restrict__ b16, uint16_t *__restrict__ b16lo,
+                   float *__restrict__ cinv, float *__restrict__ linv) {
+  constexpr int RPL = (TB + 31) / 32;
+  constexpr int Kp = (TB + 63) / 64 * 64;  // K of the product, zero-padded
+  constexpr int LS = TB + 4;                // staged L11's column stride (16-byte)
+  static_assert(TB % 4 == 0, "16-byte rows of L11");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *smf = reinterpret_cast<float *>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t ke = kb + TB;
+  const float sL = fp16_scale(__ldg(amax_l));
+  if (blockIdx.x == 0 && threadIdx.x == 0) *linv = 1.f / sL;  // a power of two: exact
+  if ((int)blockIdx.x < ncb) {
+    float *Ls = smf;  // Ls[k*LS + i] = L(i, k)
+    int32_t *spos = reinterpret_cast<int32_t *>(smf + TB * LS);
+    int32_t *ssrc = spos + 2 * kSwapMax;
+    // the warp's column, rows kb..ke, after the swaps
+    float *top = reinterpret_cast<float *>(ssrc + 2 * kSwapMax) + warp * TB;
+    const float *L = A + kb + kb * lda;
+    // L11 staged by asynchronous copies, a warp per column: 16 bytes at a
+    // time when the columns start on 16-byte boundaries
+    if (lda % 4 == 0 && (reinterpret_cast<uintptr_t>(L) & 15) == 0) {
+      for (int k = warp; k < TB; k += 8)
+        for (int c = lane; c < TB / 4; c += 32) {
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&Ls[k * LS + 4 * c]);
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
+                       "l"(&L[4 * c + (int64_t)k * lda])
+                       : "memory");
+        }
+    } else {
+      for (int k = warp; k < TB; k += 8)
+        for (int i = lane; i < TB; i += 32) {
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&Ls[k * LS + i]);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst),
+                       "l"(&L[i + (int64_t)k * lda])
+                       : "memory");
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    // every map slot at once (the entries past cnt are not used), and the
+    // column's top rows before the swaps, in flight together
+    for (int r = threadIdx.x; r < 2 * kSwapMax; r += 256) {
+      spos[r] = __ldg(&map->pos[r]);
+      ssrc[r] = __ldg(&map->src[r]);
+    }
+    const int cnt = __ldg(&map->cnt);
+    const int j = (int)blockIdx.x * 8 + warp;
+    float *col = A + (ke + j) * lda;
+    float x[RPL];
+    if (j < nn) {
+#pragma unroll
+      for (int r = 0; r < RPL; r++) {
+        const int i = lane + 32 * r;
+        x[r] = i < TB ? col[kb + i] : 0.f;
+      }
+    }
+    __syncthreads();
+    if (j < nn) {
+      constexpr int MPL = 2 * kSwapMax / 32;  // map entries per lane
+      float v[MPL];
+#pragma unroll
+      for (int q = 0; q < MPL; q++)
+        if (lane + 32 * q < cnt) v[q] = col[ssrc[lane + 32 * q]];
+#pragma unroll
+      for (int r = 0; r < RPL; r++)
+        if (lane + 32 * r < TB) top[lane + 32 * r] = x[r];
+      __syncwarp();
+      // the moves (laswp_kernel's), the top rows' new values kept on chip
+#pragma unroll
+      for (int q = 0; q < MPL; q++)
+        if (lane + 32 * q < cnt) {
+          const int32_t p = spos[lane + 32 * q];
+          col[p] = v[q];
+          if (p < ke) top[p - kb] = v[q];
+        }
+      __syncwarp();
+#pragma unroll
+      for (int r = 0; r < RPL; r++)
+        if (lane + 32 * r < TB) x[r] = top[lane + 32 * r];
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    if (j >= nn) return;
+    float *b = col + kb;
+#pragma unroll
+    for (int k = 0; k < TB - 1; k++) {
+      const float xk = __shfl_sync(0xffffffffu, x[k / 32], k % 32);
+#pragma unroll
+      for (int r = k / 32; r < RPL; r++) {
+        const int i = lane + 32 * r;
+        if (i > k && i < TB) x[r] = fmaf(-Ls[k * LS + i], xk, x[r]);
+      }
+    }
+    float m = 0.f;  // NaN ignored here; it propagates through the product
+#pragma unroll
+    for (int r = 0; r < RPL; r++) {
+      const int i = lane + 32 * r;
+      if (i > 0 && i < TB) b[i] = x[r];
+      if (i < TB) m = fmaxf(m, fabsf(x[r]));
+    }
+    for (int off = 16; off; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    const float sc = fp16_scale(__float_as_uint(m));
+    if (lane == 0) cinv[j] = 1.f / sc;
+    uint16_t *oh = b16 + (int64_t)j * Kp, *ol = b16lo + (int64_t)j * Kp;
+#pragma unroll
+    for (int r = 0; r < Kp / 32; r++) {
+      const int i = lane + 32 * r;
+      float vv = 0.f;
+#pragma unroll
+      for (int q = 0; q < RPL; q++)
+        if (q == r && i < TB) vv = sc * x[q];
+      const uint16_t h = to16<0>(vv);
+      oh[i] = h;
+      ol[i] = to16<0>(vv - from16<0>(h));
+    }
+    return;
+  }
+  // ---- L21 ----
+  const int64_t m = n - ke;
+  float *t = smf;  // t[k*33 + r]
+  const int64_t nl = (int64_t)gridDim.x - ncb;
+  constexpr int nch = Kp / 16;  // 16-entry chunks of an output row
+  constexpr int KPW = (TB + 7) / 8;  // columns per warp
+  for (int64_t s0 = ((int64_t)blockIdx.x - ncb) * 32; s0 < m; s0 += nl * 32) {
+    const int64_t i = s0 + lane;
+    // every load of the warp's columns in flight before the first store
+    float v[KPW];
+    const float *src = A + ke + i + (kb + warp) * lda;
+#pragma unroll
+    for (int q = 0; q < KPW; q++)
+      v[q] = (i < m && warp + 8 * q < TB) ? src[(int64_t)8 * q * lda] : 0.f;
+#pragma unroll
+    for (int q = 0; q < KPW; q++)
+      if (warp + 8 * q < TB) t[(warp + 8 * q) * 33 + lane] = sL * v[q];
+    __syncthreads();
+    for (int task = threadIdx.x; task < 32 * nch; task += 256) {
+      const int r = task & 31, c = task >> 5;
+      const int64_t row = s0 + r;
+      if (row >= m) continue;
+      uint32_t hw[8], lw[8];
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int k0 = 16 * c + 2 * e;
+        const float v0 = k0 < TB ? t[k0 * 33 + r] : 0.f;
+        const float v1 = k0 + 1 < TB ? t[(k0 + 1) * 33 + r] : 0.f;
+        const uint16_t h0 = to16<0>(v0), h1 = to16<0>(v1);
+        const uint16_t l0 = to16<0>(v0 - from16<0>(h0)), l1 = to16<0>(v1 - from16<0>(h1));
+        hw[e] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lw[e] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+      }
+      uint4 *dh = reinterpret_cast<uint4 *>(a16 + row * Kp + 16 * c);
+      uint4 *dl = reinterpret_cast<uint4 *>(a16lo + row * Kp + 16 * c);
+      dh[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+      dh[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+      dl[0] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+      dl[1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+    }
+    __syncthreads();
+  }
+}
+
+// The look-ahead of a fused float block for the split update (lp 2): the
+// operands from la_prep_kernel, then C[ke:n, ke:ke+nn] -= L21 U12 on the
+// tensor cores with U12's column scales.  The packing buffers are the ones
+// lp_trailing_update uses (set 0): the rest of the block's update reuses
+// the packed L21 from here.
+static int g_la_prep = 1;
+
+static int la_prep_update(int64_t n, float *A, int64_t lda, int64_t kb, int nn,
+                          const SwapMap *map, const unsigned *amax_l) {
+  constexpr int TB = kFusedMaxBw;
+  const int64_t ke = kb + TB, m = n - ke;
+  const int Kp = (TB + 63) / 64 * 64;
+  const size_t an = (size_t)m * Kp, bn = (size_t)(n - ke) * Kp;
+  uint16_t *A16 = (uint16_t *)ws(WS_T0, an * 4);
+  uint16_t *B16 = (uint16_t *)ws(WS_T1, bn * 4);
+  // (the packing scratch WS_T2 holds the blocks' max slots: a slot of its own)
+  float *scb = (float *)ws(WS_LAS, 4096);
+  if (!A16 || !B16 || !scb) return MATGB_ERR_NOMEM;
+  float *linv = scb, *cinv = scb + 32;
+  auto k = la_prep_kernel<TB>;
+  const size_t smem = ((size_t)TB * (TB + 4) + 4 * kSwapMax + 8 * TB) * sizeof(float);
+  static bool attr = false;
+  if (!attr) {
+    MGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const int ncb = (nn + 7) / 8;
+  const int64_t slabs = (m + 31) / 32;
+  int64_t nl = 2 * (int64_t)ctx()->sms - ncb;
+  if (nl > slabs) nl = slabs;
+  if (nl < 1) nl = 1;
+  {
+    // bytes: the swaps (as laswp's scope counts them), L11, L21 read, both
+    // packed operands (hi + remainder) written
+    KtScope kt("la_prep", (double)TB * TB * nn,
+               4.0 * (4.0 * TB * nn + (double)TB * TB + (double)m * TB) +
+                   4.0 * ((double)m + nn) * Kp);
+    k<<<(unsigned)(ncb + nl), 256, smem, ctx()->stream>>>(A, lda, n, kb, nn, map, amax_l, ncb,
+                                                          A16, A16 + an, B16, B16 + bn, cinv,
+                                                          linv);
+    MGB_LAUNCHED("la_prep");
+  }
+  return tc_gemm(0, m, nn, Kp, A16, Kp, B16, Kp, -1.f, linv, 1.f, A + ke + ke * lda, lda, 0,
+                 nullptr, A16 + an, B16 + bn, nullptr, cinv);
+}
+
 __global__ void iota_kernel(int32_t *p, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -1935,16 +2165,22 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       // first, then the panel stream is released; everything else (the other
       // columns, the columns left of the block, the permutation) follows
       // off the critical path
-      if (bmap)
-        MGB_TRY(laswp_map<T>(A, lda, ke, ke + nn, 0, 0, bmap, nullptr, nb));
-      else
-        MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
-      bool u12_ready = false;
-      MGB_TRY(trsm_unit_lower<T>((int)nb, nn, A + kb + kb * lda, lda,
-                                 A + kb + ke * lda, lda, amax3 ? amax3 + 1 : nullptr,
-                                 &u12_ready));
-      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true, amax3,
-                                 l21_ready, u12_ready));
+      if (sizeof(T) == 4 && g_la_prep && bmap && lp == 2 && amax3 && l21_ready &&
+          nb == kFusedMaxBw) {
+        // swaps, U12 solve and both operands' packing in one launch
+        MGB_TRY(la_prep_update(n, (float *)A, lda, kb, (int)nn, bmap, amax3));
+      } else {
+        if (bmap)
+          MGB_TRY(laswp_map<T>(A, lda, ke, ke + nn, 0, 0, bmap, nullptr, nb));
+        else
+          MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
+        bool u12_ready = false;
+        MGB_TRY(trsm_unit_lower<T>((int)nb, nn, A + kb + kb * lda, lda,
+                                   A + kb + ke * lda, lda, amax3 ? amax3 + 1 : nullptr,
+                                   &u12_ready));
+        MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true, amax3,
+                                   l21_ready, u12_ready));
+      }
       MGB_CUDA(cudaEventRecord(g_la.ev[2], main));
       MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[2], 0));
     }
@@ -2085,6 +2321,12 @@ int matgb_getrs_dev(size_t n, size_t nrhs, const mat_elem_t *LU, size_t lda,
   if (B == X) return set_error(MATGB_ERR_ARG, "getrs: B and X must differ");
   return getrs((int64_t)n, (int64_t)nrhs, LU, (int64_t)lda, perm, B,
                (int64_t)ldb, X, (int64_t)ldx);
+}
+
+int matgb_la_prep(int on) {
+  const int prev = g_la_prep;
+  if (on >= 0) g_la_prep = on ? 1 : 0;
+  return prev;
 }
 
 }  // extern "C"

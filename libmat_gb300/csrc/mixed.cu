@@ -21,34 +21,16 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "lp_pack.cuh"
 
 #include <algorithm>
 
 namespace mgb {
 
 // ---- packing the trailing-update operands -------------------------------------
-template <int BF16>
-__device__ __forceinline__ uint16_t to16(float v) {
-  if (BF16) return __bfloat16_as_ushort(__float2bfloat16_rn(v));
-  return __half_as_ushort(__float2half_rn(v));
-}
-
-__device__ __forceinline__ float fp16_scale(unsigned amax_bits) {
-  const float a = __uint_as_float(amax_bits);
-  if (!(a > 0.f) || isinf(a)) return 1.f;
-  int e;
-  frexpf(a, &e);  // a = f * 2^e, f in [0.5, 1)
-  return ldexpf(1.f, 14 - e);
-}
-
+// to16 / from16 / fp16_scale: lp_pack.cuh.
 // out[i*Kp + k] = A[i + k*lda] for i < m, k < nb (zero for nb <= k < Kp):
 // L21 (column-major, M-contiguous) to a K-contiguous 16-bit operand.
-template <int BF16>
-__device__ __forceinline__ float from16(uint16_t h) {
-  if (BF16) return __bfloat162float(__ushort_as_bfloat16(h));
-  return __half2float(__ushort_as_half(h));
-}
-
 // out_lo (optional): the remainder v - hi(v), also 16-bit (the split form).
 template <int BF16>
 __global__ void pack_l21_kernel(const float *__restrict__ A, int64_t lda,

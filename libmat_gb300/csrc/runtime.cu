@@ -357,6 +357,7 @@ struct KtRec {
   std::string name;
   cudaEvent_t a, b;
   double flops, bytes;
+  cudaStream_t st;  // the stream the scope's work was queued on
 };
 static bool g_kt_on = false;
 bool ktime_on() { return g_kt_on; }
@@ -376,7 +377,7 @@ static cudaEvent_t kt_event() {
 
 KtScope::KtScope(const char *name, double flops, double bytes) : idx(-1) {
   if (!g_kt_on) return;
-  KtRec r{name, kt_event(), kt_event(), flops, bytes};
+  KtRec r{name, kt_event(), kt_event(), flops, bytes, g_ctx.stream};
   cudaEventRecord(r.a, g_ctx.stream);
   g_kt.push_back(r);
   idx = (int)g_kt.size() - 1;
@@ -447,6 +448,36 @@ int matgb_ktime_get(int i, char *name, int cap, long long *launches,
   if (ms) *ms = t;
   if (flops) *flops = f;
   if (bytes) *bytes = by;
+  return 0;
+}
+
+int matgb_ktime_trace(int i, char *name, int cap, double *t0_ms, double *t1_ms,
+                      int *stream) {
+  if (!ctx()) return MATGB_ERR_NO_DEVICE;
+  MGB_CUDA(cudaDeviceSynchronize());
+  if (i < 0 || i >= (int)g_kt.size()) return 1;
+  const KtRec &r = g_kt[i];
+  float a = 0, b = 0;
+  MGB_CUDA(cudaEventElapsedTime(&a, g_kt[0].a, r.a));
+  MGB_CUDA(cudaEventElapsedTime(&b, g_kt[0].a, r.b));
+  // streams numbered by first appearance in the record list
+  int sid = 0;
+  std::vector<cudaStream_t> seen;
+  for (auto &q : g_kt) {
+    bool dup = false;
+    for (auto s : seen) dup |= s == q.st;
+    if (!dup) seen.push_back(q.st);
+    if (q.st == r.st) break;
+  }
+  for (size_t k = 0; k < seen.size(); k++)
+    if (seen[k] == r.st) sid = (int)k;
+  if (name && cap > 0) {
+    strncpy(name, r.name.c_str(), cap - 1);
+    name[cap - 1] = 0;
+  }
+  if (t0_ms) *t0_ms = a;
+  if (t1_ms) *t1_ms = b;
+  if (stream) *stream = sid;
   return 0;
 }
 

@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
     float cur[CH];
     load(cur, 0);
     float rs = 1.f;
-    if constexpr (SC) rs = rok ? __ldg(&rinv[row]) : 1.f;
+    if constexpr (SC) rs = (rok && rinv) ? __ldg(&rinv[row]) : 1.f;
     const bool ready = tc::mbar_wait(&s.done, 0, kTcWaitLimit);
     tc::tc_fence_after();
     if (ready && !s.timeout) {
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB)
       load(c0, 0);
       if (NCH > 1) load(c1, 1);
       float rs = 1.f;
-      if constexpr (SC) rs = rok ? __ldg(&rinv[row]) : 1.f;
+      if constexpr (SC) rs = (rok && rinv) ? __ldg(&rinv[row]) : 1.f;
       const int a = i & 1, au = i >> 1;
       const bool ready = tc::mbar_wait(&s.acc_full[a], au & 1, kTcWaitLimit);
       tc::tc_fence_after();
@@ -662,9 +662,9 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
   KtScope kt(nm, 2.0 * M * N * K * frac * nseg,
              4.0 * (beta != 0.f ? 2.0 : 1.0) * M * N * frac +
                  2.0 * (M + N) * K * (split3 ? 3 : split ? 2 : 1));
-  if ((rinv == nullptr) != (cinv == nullptr))
-    return set_error(MATGB_ERR_ARG, "tc_gemm: row and column scales go together");
-  const bool sc = rinv != nullptr;
+  if (rinv && !cinv)
+    return set_error(MATGB_ERR_ARG, "tc_gemm: row scales need column scales");
+  const bool sc = cinv != nullptr;  // rinv null: rows unscaled
 #define MGB_TC_LAUNCH(ST_, MB_, SC_)                                           \
   tc_gemm_kernel<ST_, MB_, SC_><<<grid, kTcThreads, tc_smem_bytes<ST_>(),      \
                                   cx->stream>>>(                               \

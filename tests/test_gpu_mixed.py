@@ -206,6 +206,46 @@ def test_lp_lu_reconstructs(gpu, lp, n):
     assert np.abs(Lm).max() <= 1.0 + 1e-6  # partial pivoting bound
 
 
+def ktime_names(L):
+    """Names of the library's timed scopes since timing was enabled."""
+    out, i = set(), 0
+    nm = C.create_string_buffer(64)
+    cnt, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+    while L.c.matgb_ktime_get(i, nm, 64, C.byref(cnt), C.byref(ms), C.byref(fl),
+                              C.byref(by)) == 0:
+        out.add(nm.value.decode())
+        i += 1
+    return out
+
+
+@pytest.mark.parametrize("n", [300, 1000, 1537])
+def test_lookahead_prep_in_one_launch(gpu, n):
+    """After a fused 144-column block, the split update's look-ahead runs the
+    next block's row swaps, its U12 solve and both operands' packing as one
+    launch (la_prep; U12 scaled per column).  Its factors reconstruct PA as
+    well as the separate launches' do (n = 300: the last look-ahead has 12
+    columns), and it is the form that ran."""
+    L = gpu["f32"]
+    A = rng.uniform(900 + n, (n, n), -1, 1, np.float32)
+    errs = {}
+    for on in (0, 1):
+        prev = L.c.matgb_la_prep(on)
+        try:
+            L.check(L.c.matgb_ktime_enable(1), "ktime")
+            LU, perm = factor_lp(L, A, 2)
+            names = ktime_names(L)
+        finally:
+            L.c.matgb_ktime_enable(0)
+            L.c.matgb_la_prep(prev)
+        assert ("la_prep" in names) == bool(on), names
+        assert np.array_equal(np.sort(perm), np.arange(n))
+        Lm = np.tril(LU.astype(np.float64), -1) + np.eye(n)
+        Um = np.triu(LU.astype(np.float64))
+        assert np.abs(Lm).max() <= 1.0 + 1e-6
+        errs[on] = np.abs(A[perm].astype(np.float64) - Lm @ Um).max() / np.abs(A).max()
+    assert errs[1] <= 2 * errs[0] + 1e-6, errs
+
+
 def conditioned(n, kappa, seed):
     rs = np.random.default_rng(seed)
     U, _ = np.linalg.qr(rs.standard_normal((n, n)))
