@@ -1400,6 +1400,13 @@ static int trsm_unit_lower(int tb, int64_t ncols, const T *L, int64_t ldl, T *B,
   return trsm_left_t<T>(true, false, true, tb, ncols, L, ldl, B, ldb, nullptr);
 }
 
+// Temporarily route library launches to another stream.
+struct StreamSwap {
+  cudaStream_t saved;
+  explicit StreamSwap(cudaStream_t s) : saved(ctx()->stream) { ctx()->stream = s; }
+  ~StreamSwap() { ctx()->stream = saved; }
+};
+
 // ---- the mixed look-ahead's operands in one launch --------------------------
 // After a fused block (TB pivots, its net row map on the device), the
 // split tensor-core update of the next block's nn columns needs those
@@ -1590,8 +1597,11 @@ __global__ void __launch_bounds__(256)
 // the packed L21 from here.
 static int g_la_prep = 1;
 
+// st: the stream the two launches go to (the buffers are looked up, and
+// grown if needed, with the library stream current, so that a growth waits
+// for that stream's queued users).
 static int la_prep_update(int64_t n, float *A, int64_t lda, int64_t kb, int nn,
-                          const SwapMap *map, const unsigned *amax_l) {
+                          const SwapMap *map, const unsigned *amax_l, cudaStream_t st) {
   constexpr int TB = kFusedMaxBw;
   const int64_t ke = kb + TB, m = n - ke;
   const int Kp = (TB + 63) / 64 * 64;
@@ -1601,6 +1611,7 @@ static int la_prep_update(int64_t n, float *A, int64_t lda, int64_t kb, int nn,
   // (the packing scratch WS_T2 holds the blocks' max slots: a slot of its own)
   float *scb = (float *)ws(WS_LAS, 4096);
   if (!A16 || !B16 || !scb) return MATGB_ERR_NOMEM;
+  StreamSwap sw(st);
   float *linv = scb, *cinv = scb + 32;
   auto k = la_prep_kernel<TB>;
   const size_t smem = ((size_t)TB * (TB + 4) + 4 * kSwapMax + 8 * TB) * sizeof(float);
@@ -1954,13 +1965,6 @@ static int lookahead_setup() {
   return 0;
 }
 
-// Temporarily route library launches to another stream.
-struct StreamSwap {
-  cudaStream_t saved;
-  explicit StreamSwap(cudaStream_t s) : saved(ctx()->stream) { ctx()->stream = s; }
-  ~StreamSwap() { ctx()->stream = saved; }
-};
-
 // Trailing update C[ke:n, c0:c1] -= L21 * U12[:, c0:c1] for outer block
 // [kb, ke): SIMT GEMM in T (lp < 0) or the tensor-core path (lp >= 0, float
 // only: L21 packed to 16 bits on the block's first call, U12 per call, see
@@ -2124,9 +2128,11 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     }
     return 0;
   };
-  // main -> hi: everything queued so far (input copies, perm init, slots)
+  // main -> hi: everything queued so far (input copies, perm init, slots);
+  // ev[3] marks the end of each block's remaining update on main
   MGB_CUDA(cudaEventRecord(g_la.ev[0], main));
   MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[0], 0));
+  MGB_CUDA(cudaEventRecord(g_la.ev[3], main));
   for (int64_t kb = 0; kb < n; kb += NB) {
     const int64_t nb = (n - kb) < NB ? (n - kb) : NB;
     const int64_t ke = kb + nb;
@@ -2152,35 +2158,47 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
     MGB_CUDA(cudaStreamWaitEvent(main, g_la.ev[1], 0));
 
     const int64_t nn = (n - ke) < NB ? (n - ke) : NB;
+    // the one-launch look-ahead (swaps, U12 solve, both operands packed) of
+    // the split update runs on the panel stream, right behind the block
+    const bool prep = ke < n && sizeof(T) == 4 && g_la_prep && bmap && lp == 2 && amax3 &&
+                      l21_ready && nb == kFusedMaxBw;
     // the look-ahead's columns must have joined (a plan that is too late
     // for them costs a wait here, never a wrong result); the look-ahead
     // then packs this block's L21 afresh
     while (arr && joined < arr->nchunks && columns_in() < ke + nn) {
       MGB_CUDA(cudaStreamWaitEvent(main, arr->ev[joined], 0));
       MGB_CUDA(cudaStreamWaitEvent(main, g_chunk.done[joined], 0));
+      if (prep) {
+        MGB_CUDA(cudaStreamWaitEvent(hi, arr->ev[joined], 0));
+        MGB_CUDA(cudaStreamWaitEvent(hi, g_chunk.done[joined], 0));
+      }
       joined++;
     }
-    if (ke < n) {
+    if (prep) {
+      // the previous block's remaining update covered these columns (and
+      // read the packing buffers this launch rewrites): wait for it, then
+      // the look-ahead on the panel stream, no stream hop before the next
+      // block.  Main waits for it before its own swaps: run beside them,
+      // the look-ahead's launches lose their SMs to the swaps' CTAs.
+      MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[3], 0));
+      MGB_TRY(la_prep_update(n, (float *)A, lda, kb, (int)nn, bmap, amax3, hi));
+      MGB_CUDA(cudaEventRecord(g_la.ev[2], hi));
+      MGB_CUDA(cudaStreamWaitEvent(main, g_la.ev[2], 0));
+    } else if (ke < n) {
       // look-ahead: the next block's columns are swapped, solved and updated
       // first, then the panel stream is released; everything else (the other
       // columns, the columns left of the block, the permutation) follows
       // off the critical path
-      if (sizeof(T) == 4 && g_la_prep && bmap && lp == 2 && amax3 && l21_ready &&
-          nb == kFusedMaxBw) {
-        // swaps, U12 solve and both operands' packing in one launch
-        MGB_TRY(la_prep_update(n, (float *)A, lda, kb, (int)nn, bmap, amax3));
-      } else {
-        if (bmap)
-          MGB_TRY(laswp_map<T>(A, lda, ke, ke + nn, 0, 0, bmap, nullptr, nb));
-        else
-          MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
-        bool u12_ready = false;
-        MGB_TRY(trsm_unit_lower<T>((int)nb, nn, A + kb + kb * lda, lda,
-                                   A + kb + ke * lda, lda, amax3 ? amax3 + 1 : nullptr,
-                                   &u12_ready));
-        MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true, amax3,
-                                   l21_ready, u12_ready));
-      }
+      if (bmap)
+        MGB_TRY(laswp_map<T>(A, lda, ke, ke + nn, 0, 0, bmap, nullptr, nb));
+      else
+        MGB_TRY(laswp_t<T>(A, lda, ke, ke + nn, 0, 0, ipiv, kb, ke, nullptr));
+      bool u12_ready = false;
+      MGB_TRY(trsm_unit_lower<T>((int)nb, nn, A + kb + kb * lda, lda,
+                                 A + kb + ke * lda, lda, amax3 ? amax3 + 1 : nullptr,
+                                 &u12_ready));
+      MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke, ke + nn, lp, true, amax3,
+                                 l21_ready, u12_ready));
       MGB_CUDA(cudaEventRecord(g_la.ev[2], main));
       MGB_CUDA(cudaStreamWaitEvent(hi, g_la.ev[2], 0));
     }
@@ -2207,6 +2225,7 @@ int getrf_t(int64_t n, T *A, int64_t lda, int32_t *ipiv, int32_t *perm, T eps,
       MGB_TRY(trailing_update<T>(n, A, lda, kb, ke, ke + nn, r1, lp, false, amax3,
                                  l21_ready, u12_ready));
     }
+    MGB_CUDA(cudaEventRecord(g_la.ev[3], main));
   }
   if (defer) MGB_TRY(apply_deferred_swaps<T>(A, lda, n, NB, nblk, maps, gmap));
   return 0;
