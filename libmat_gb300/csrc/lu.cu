@@ -1303,63 +1303,92 @@ __global__ void __launch_bounds__(NT, 1)
 }
 
 // ---- U12 = L11^{-1} A12 with L11 unit lower (TB x TB) ----------------------
-// One warp per right-hand-side column: lane l holds rows l, l+32, ... of the
-// column in registers, L11 sits in shared memory; step k broadcasts x_k by a
-// shuffle and every lane updates its rows below k -- the reference's axpy
-// order (mat.h:4264-4271).  Loads and stores of a column are coalesced.
-template <typename T, int TB>
+// A warp solves CPW right-hand-side columns at once: lane l holds rows l,
+// l+32, ... of each in registers, L11 sits in shared memory; step k
+// broadcasts each column's x_k by a shuffle and every lane updates its rows
+// below k -- per column the reference's axpy order (mat.h:4264-4271); the
+// CPW columns' chains interleave and share each L11 load.  Loads and stores
+// of a column are coalesced.  The CTAs stride over the columns (at most two
+// per SM), so that each stages L11 once for many columns; the staging copies
+// 16 bytes at a time when the columns start on 16-byte boundaries.
+template <typename T, int TB, int CPW>
 __global__ void __launch_bounds__(256)
     trsm_unit_warp_kernel(const T *__restrict__ L, int64_t ldl,
                           T *__restrict__ B, int64_t ldb, int64_t ncols,
                           unsigned *__restrict__ amax) {
   constexpr int RPL = (TB + 31) / 32;
+  constexpr int VE = 16 / (int)sizeof(T);  // elements per 16-byte copy
+  constexpr int LS = TB + VE;               // staged column stride (16-byte)
+  static_assert(TB % VE == 0, "16-byte columns of L11");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *Ls = (T *)smem_raw;  // Ls[k*(TB+1) + i] = L(i, k)
-  // L11 staged by asynchronous copies: every element's load in flight at
-  // once instead of a load-store round trip per element
-  for (int e = threadIdx.x; e < TB * TB; e += 256) {
-    const int i = e % TB, k = e / TB;
-    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&Ls[k * (TB + 1) + i]);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst),
-                 "l"(&L[i + (int64_t)k * ldl]), "n"(sizeof(T))
-                 : "memory");
+  T *Ls = (T *)smem_raw;  // Ls[k*LS + i] = L(i, k)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // L11 staged by asynchronous copies, a warp per column
+  if (ldl % VE == 0 && (reinterpret_cast<uintptr_t>(L) & 15) == 0) {
+    for (int k = warp; k < TB; k += 8)
+      for (int c = lane; c < TB / VE; c += 32) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&Ls[k * LS + VE * c]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
+                     "l"(&L[VE * c + (int64_t)k * ldl])
+                     : "memory");
+      }
+  } else {
+    for (int k = warp; k < TB; k += 8)
+      for (int i = lane; i < TB; i += 32) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&Ls[k * LS + i]);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(dst),
+                     "l"(&L[i + (int64_t)k * ldl]), "n"(sizeof(T))
+                     : "memory");
+      }
   }
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int64_t col = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (col >= ncols) return;
-  T *b = B + col * ldb;
-  T x[RPL];
+  float m = 0.f;  // max |U12| over the warp's columns (float builds)
+  const int64_t step = (int64_t)gridDim.x * 8 * CPW;
+  for (int64_t c0 = ((int64_t)blockIdx.x * 8 + warp) * CPW; c0 < ncols; c0 += step) {
+    T x[CPW][RPL];
 #pragma unroll
-  for (int r = 0; r < RPL; r++) {
-    const int i = lane + 32 * r;
-    x[r] = i < TB ? b[i] : T(0);
-  }
+    for (int c = 0; c < CPW; c++) {
+      const T *b = B + (c0 + c) * ldb;
 #pragma unroll
-  for (int k = 0; k < TB - 1; k++) {
-    const T xk = __shfl_sync(0xffffffffu, x[k / 32], k % 32);
+      for (int r = 0; r < RPL; r++) {
+        const int i = lane + 32 * r;
+        x[c][r] = (c0 + c < ncols && i < TB) ? b[i] : T(0);
+      }
+    }
 #pragma unroll
-    for (int r = k / 32; r < RPL; r++) {
-      const int i = lane + 32 * r;
-      if (i > k && i < TB) x[r] = fma(-Ls[k * (TB + 1) + i], xk, x[r]);
+    for (int k = 0; k < TB - 1; k++) {
+      T xk[CPW];
+#pragma unroll
+      for (int c = 0; c < CPW; c++) xk[c] = __shfl_sync(0xffffffffu, x[c][k / 32], k % 32);
+#pragma unroll
+      for (int r = k / 32; r < RPL; r++) {
+        const int i = lane + 32 * r;
+        if (i > k && i < TB) {
+          const T l = Ls[k * LS + i];
+#pragma unroll
+          for (int c = 0; c < CPW; c++) x[c][r] = fma(-l, xk[c], x[c][r]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CPW; c++) {
+      if (c0 + c >= ncols) break;
+      T *b = B + (c0 + c) * ldb;
+#pragma unroll
+      for (int r = 0; r < RPL; r++) {
+        const int i = lane + 32 * r;
+        if (i > 0 && i < TB) b[i] = x[c][r];
+        // the FP16 scale of the tensor-core operand; NaN ignored as in
+        // amax_kernel
+        if (sizeof(T) == 4 && i < TB) m = fmaxf(m, fabsf((float)x[c][r]));
+      }
     }
   }
-#pragma unroll
-  for (int r = 0; r < RPL; r++) {
-    const int i = lane + 32 * r;
-    if (i > 0 && i < TB) b[i] = x[r];
-  }
   if constexpr (sizeof(T) == 4) {
-    // max |U12| of the column (the FP16 scale of the tensor-core operand),
-    // NaN ignored as in amax_kernel
     if (amax) {
-      float m = 0.f;
-#pragma unroll
-      for (int r = 0; r < RPL; r++)
-        if (lane + 32 * r < TB) m = fmaxf(m, fabsf((float)x[r]));
       for (int off = 16; off; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
-      if (lane == 0) atomicMax(amax, __float_as_uint(m));
+      if (lane == 0 && m > 0.f) atomicMax(amax, __float_as_uint(m));
     }
   }
 }
@@ -1367,17 +1396,21 @@ __global__ void __launch_bounds__(256)
 template <typename T, int TB>
 static int launch_trsm_warp(int64_t ncols, const T *L, int64_t ldl, T *B,
                             int64_t ldb, unsigned *amax) {
-  auto k = trsm_unit_warp_kernel<T, TB>;
-  const size_t smem = (size_t)TB * (TB + 1) * sizeof(T);
-  static bool attr = false;
-  if (!attr) {
+  // four columns per warp once every warp of two CTAs per SM has that many
+  const int64_t cap = 2 * (int64_t)ctx()->sms;
+  const bool wide = ncols >= cap * 8 * 4;
+  auto k = wide ? trsm_unit_warp_kernel<T, TB, 4> : trsm_unit_warp_kernel<T, TB, 1>;
+  const size_t smem = (size_t)TB * (TB + 16 / sizeof(T)) * sizeof(T);
+  static bool attr[2] = {false, false};
+  if (!attr[wide]) {
     MGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
-    attr = true;
+    attr[wide] = true;
   }
+  int64_t blocks = (ncols + 8 * (wide ? 4 : 1) - 1) / (8 * (wide ? 4 : 1));
+  if (blocks > cap) blocks = cap;
   KtScope kt("trsm_lu", (double)TB * TB * ncols, (double)sizeof(T) * 2.0 * TB * ncols);
-  k<<<(unsigned)((ncols + 7) / 8), 256, smem, ctx()->stream>>>(L, ldl, B, ldb, ncols,
-                                                                amax);
+  k<<<(unsigned)blocks, 256, smem, ctx()->stream>>>(L, ldl, B, ldb, ncols, amax);
   MGB_LAUNCHED("trsm_lu");
   return 0;
 }
