@@ -299,6 +299,12 @@ int matgb_tc_persistent(int on);
  * swap, solve and packing launches with one U12 scale.  -1 queries.
  * Returns the previous setting. */
 int matgb_la_prep(int on);
+/* The tensor-core Cholesky (mixed SPD solve, plain float Cholesky from order
+ * 1024): 1 (default) = look-ahead, the diagonal block, its column solve and
+ * the next block's columns on a high-priority stream while the library
+ * stream updates the rest of the trailing matrix; 0 = every step in turn on
+ * the library stream.  -1 queries.  Returns the previous setting. */
+int matgb_chol_lookahead(int on);
 
 /* y = alpha*A*x + beta*y like matgb_gemv_dev, for callers that must not
  * allocate device memory -- e.g. code that runs inside another runtime's

@@ -160,6 +160,7 @@ class Lib:
             "matgb_tc_status": (_I, []),
             "matgb_tc_persistent": (_I, [_I]),
             "matgb_la_prep": (_I, [_I]),
+            "matgb_chol_lookahead": (_I, [_I]),
             "matgb_tc_gemm_split_dev": (_I, [_S, _S, _S, _P, _P, _S, _P, _P, _S,
                                              C.c_float, C.c_float, _P, _S]),
             "matgb_getrf_lp_dev": (_I, [_S, _P, _S, _P, _P, _I]),

@@ -215,6 +215,139 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// The diagonal block [kb, kb+nb) and the column solve below it, on the
+// current library stream.
+template <typename T>
+static int chol_panel(int64_t n, T *A, int64_t lda, int32_t *info, int64_t kb, int nb) {
+  Ctx *cx = ctx();
+  T *A11 = A + kb + kb * lda;
+  {
+    KtScope kt("potrf_diag", nb * (double)nb * nb / 3.0,
+               (double)nb * nb * sizeof(T));
+    if (sizeof(T) == 4 && nb > 64) {
+      if (nb > kCholBlock) {
+        potrf_diag_rows_kernel<kCholBlockLp><<<1, kCholBlockLp, 0, cx->stream>>>(
+            nb, (float *)A11, lda, info, kb);
+        MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlockLp>,
+                             "potrf_diag_rows", 0));
+      } else {
+        potrf_diag_rows_kernel<kCholBlock><<<1, kCholBlock, 0, cx->stream>>>(
+            nb, (float *)A11, lda, info, kb);
+        MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlock>,
+                             "potrf_diag_rows", 0));
+      }
+    } else {
+      auto kdiag = potrf_diag_kernel<T>;
+      kdiag<<<1, 256, diag_smem<T>(nb), cx->stream>>>(nb, A11, lda, info, kb);
+      MGB_TRY(launch_check((const void *)kdiag, "potrf_diag", diag_smem<T>(nb)));
+    }
+  }
+  const int64_t m = n - kb - nb;
+  if (m <= 0) return 0;
+  T *A21 = A + (kb + nb) + kb * lda;
+  KtScope kt2("chol_trsm", (double)m * nb * nb, 2.0 * m * nb * sizeof(T));
+  if constexpr (sizeof(T) == 4) {
+    if (nb == kCholBlockLp || nb == kCholBlock) {
+      const size_t sm = nb == kCholBlockLp ? rows_smem(kCholBlockLp) : rows_smem(kCholBlock);
+      const void *kr = nb == kCholBlockLp ? (const void *)chol_trsm_rows_kernel<kCholBlockLp>
+                                          : (const void *)chol_trsm_rows_kernel<kCholBlock>;
+      MGB_CUDA(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      if (nb == kCholBlockLp)
+        chol_trsm_rows_kernel<kCholBlockLp><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
+            nb, (const float *)A11, (float *)A21, lda, m, info);
+      else
+        chol_trsm_rows_kernel<kCholBlock><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
+            nb, (const float *)A11, (float *)A21, lda, m, info);
+      return launch_check(kr, "chol_trsm_rows", sm);
+    }
+  }
+  auto ktrsm = chol_trsm_kernel<T>;
+  ktrsm<<<(unsigned)((m + 31) / 32), 256, ctrsm_smem<T>(nb), cx->stream>>>(nb, A11, A21, lda,
+                                                                         m, info);
+  return launch_check((const void *)ktrsm, "chol_trsm", ctrsm_smem<T>(nb));
+}
+
+// Look-ahead for the tensor-core Cholesky (float, lp >= 0).  The panel chain
+// runs on a high-priority stream: block k's diagonal factor, its column
+// solve, its L21 packed (buffer set k % 2), then the next block's columns
+// updated with it; the library stream updates the rest of the trailing
+// matrix with the same packed operand meanwhile.  The next block's columns
+// are also written by the previous block's rest update, so the panel stream
+// waits for that one (evr) before its own update of them; the rest update
+// waits for the packing (evp).  A packing buffer is rewritten two blocks
+// later, after the panel stream has waited for the rest update that read it.
+struct CholLookAhead {
+  cudaStream_t hi = nullptr;
+  cudaEvent_t ev0 = nullptr, evp = nullptr, evr = nullptr, evend = nullptr;
+  bool ready = false;
+};
+static CholLookAhead g_cla;
+static int g_chol_la = 1;
+
+static int chol_la_setup() {
+  if (g_cla.ready) return 0;
+  int lo = 0, hi = 0;
+  MGB_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  MGB_CUDA(cudaStreamCreateWithPriority(&g_cla.hi, cudaStreamNonBlocking, hi));
+  for (cudaEvent_t *e : {&g_cla.ev0, &g_cla.evp, &g_cla.evr, &g_cla.evend})
+    MGB_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  g_cla.ready = true;
+  return 0;
+}
+
+struct CholStreamSwap {
+  cudaStream_t saved;
+  explicit CholStreamSwap(cudaStream_t s) : saved(ctx()->stream) { ctx()->stream = s; }
+  ~CholStreamSwap() { ctx()->stream = saved; }
+};
+
+static int potrf_la(int64_t n, float *A, int64_t lda, int32_t *info, int lp) {
+  MGB_TRY(chol_la_setup());
+  const int NB = kCholBlockLp;
+  cudaStream_t main = ctx()->stream, hi = g_cla.hi;
+  if (n > NB) {
+    // both packing sets at their largest (block 0's) size, grown here while
+    // the library stream is current (a growth waits for its users first)
+    const size_t bytes = (size_t)(n - NB) * ((NB + 63) / 64 * 64) * 2 * (lp == 2 ? 2 : 1);
+    if (!ws(WS_T0, bytes) || !ws(WS_CU0, bytes) || !ws(WS_T2, 64) || !ws(WS_CU0 + 2, 64))
+      return MATGB_ERR_NOMEM;
+  }
+  MGB_CUDA(cudaEventRecord(g_cla.ev0, main));
+  MGB_CUDA(cudaStreamWaitEvent(hi, g_cla.ev0, 0));
+  MGB_CUDA(cudaEventRecord(g_cla.evr, main));
+  for (int64_t kb = 0, k = 0; kb < n; kb += NB, k++) {
+    const int nb = (int)((n - kb) < NB ? (n - kb) : NB);
+    const int64_t m = n - kb - nb;
+    const int64_t nn = m < NB ? m : NB;  // the next block's width
+    float *A21 = A + (kb + nb) + kb * lda;
+    SyrkOperand op{};
+    {
+      CholStreamSwap sw(hi);
+      MGB_TRY(chol_panel<float>(n, A, lda, info, kb, nb));
+      if (m > 0) {
+        // (set k % 2 was last read by block k-2's rest update, which the
+        // panel stream waited for before block k-1's look-ahead update)
+        MGB_TRY(lp_syrk_pack(m, nb, A21, lda, lp, (int)(k & 1), &op));
+        MGB_CUDA(cudaEventRecord(g_cla.evp, hi));
+        MGB_CUDA(cudaStreamWaitEvent(hi, g_cla.evr, 0));
+        MGB_TRY(lp_syrk_apply(op, 0, m, 0, nn, A + (kb + nb) + (kb + nb) * lda, lda, info));
+      }
+    }
+    if (m > nn) {
+      // one CTA per tile: the persistent form would hold every SM for the
+      // whole update and starve the panel chain beside it
+      MGB_CUDA(cudaStreamWaitEvent(main, g_cla.evp, 0));
+      MGB_TRY(lp_syrk_apply(op, nn, m - nn, nn, m - nn,
+                            A + (kb + nb + nn) + (kb + nb + nn) * lda, lda, info, 0));
+      MGB_CUDA(cudaEventRecord(g_cla.evr, main));
+    }
+  }
+  // the library stream resumes after the panel stream's last work
+  MGB_CUDA(cudaEventRecord(g_cla.evend, hi));
+  MGB_CUDA(cudaStreamWaitEvent(main, g_cla.evend, 0));
+  return 0;
+}
+
 template <typename T>
 int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
   Ctx *cx = ctx();
@@ -226,64 +359,21 @@ int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp) {
   const int NB = lp >= 0 ? kCholBlockLp : kCholBlock;
   // the shared-memory opt-in is set on every call (a host-side attribute
   // write), through the same function pointers the launches use
-  auto kdiag = potrf_diag_kernel<T>;
-  auto ktrsm = chol_trsm_kernel<T>;
-  MGB_CUDA(cudaFuncSetAttribute(kdiag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  MGB_CUDA(cudaFuncSetAttribute(potrf_diag_kernel<T>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)diag_smem<T>(NB)));
-  MGB_CUDA(cudaFuncSetAttribute(ktrsm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  MGB_CUDA(cudaFuncSetAttribute(chol_trsm_kernel<T>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)ctrsm_smem<T>(NB)));
+  if constexpr (sizeof(T) == 4) {
+    if (lp >= 0 && g_chol_la) return potrf_la(n, (float *)A, lda, info, lp);
+  }
   for (int64_t kb = 0; kb < n; kb += NB) {
     const int nb = (int)((n - kb) < NB ? (n - kb) : NB);
-    T *A11 = A + kb + kb * lda;
-    {
-      KtScope kt("potrf_diag", nb * (double)nb * nb / 3.0,
-                 (double)nb * nb * sizeof(T));
-      if (sizeof(T) == 4 && nb > 64) {
-        if (nb > kCholBlock) {
-          potrf_diag_rows_kernel<kCholBlockLp><<<1, kCholBlockLp, 0, cx->stream>>>(
-              nb, (float *)A11, lda, info, kb);
-          MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlockLp>,
-                               "potrf_diag_rows", 0));
-        } else {
-          potrf_diag_rows_kernel<kCholBlock><<<1, kCholBlock, 0, cx->stream>>>(
-              nb, (float *)A11, lda, info, kb);
-          MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlock>,
-                               "potrf_diag_rows", 0));
-        }
-      } else {
-        kdiag<<<1, 256, diag_smem<T>(nb), cx->stream>>>(nb, A11, lda, info, kb);
-        MGB_TRY(launch_check((const void *)kdiag, "potrf_diag", diag_smem<T>(nb)));
-      }
-    }
+    MGB_TRY(chol_panel<T>(n, A, lda, info, kb, nb));
     const int64_t m = n - kb - nb;
     if (m > 0) {
       T *A21 = A + (kb + nb) + kb * lda;
-      {
-        KtScope kt2("chol_trsm", (double)m * nb * nb,
-                    2.0 * m * nb * sizeof(T));
-        bool done = false;
-        if constexpr (sizeof(T) == 4) {
-          if (nb == kCholBlockLp || nb == kCholBlock) {
-            const size_t sm = nb == kCholBlockLp ? rows_smem(kCholBlockLp) : rows_smem(kCholBlock);
-            const void *kr = nb == kCholBlockLp ? (const void *)chol_trsm_rows_kernel<kCholBlockLp>
-                                                : (const void *)chol_trsm_rows_kernel<kCholBlock>;
-            MGB_CUDA(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            if (nb == kCholBlockLp)
-              chol_trsm_rows_kernel<kCholBlockLp><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
-                  nb, (const float *)A11, (float *)A21, lda, m, info);
-            else
-              chol_trsm_rows_kernel<kCholBlock><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
-                  nb, (const float *)A11, (float *)A21, lda, m, info);
-            MGB_TRY(launch_check(kr, "chol_trsm_rows", sm));
-            done = true;
-          }
-        }
-        if (!done) {
-          ktrsm<<<(unsigned)((m + 31) / 32), 256, ctrsm_smem<T>(nb), cx->stream>>>(
-              nb, A11, A21, lda, m, info);
-          MGB_TRY(launch_check((const void *)ktrsm, "chol_trsm", ctrsm_smem<T>(nb)));
-        }
-      }
       T *A22 = A + (kb + nb) + (kb + nb) * lda;
       if (lp < 0)
         MGB_TRY(gemm_skip_t<T>(false, true, m, m, nb, T(-1), A21, lda, A21, lda,
@@ -351,6 +441,12 @@ int matgb_potrf_lp_dev(size_t n, float *A, size_t lda, int32_t *info,
   if (lp_format < -1 || lp_format > 2)
     return set_error(MATGB_ERR_ARG, "potrf_lp: lp_format");
   return potrf_t<float>((int64_t)n, A, (int64_t)lda, info, lp_format);
+}
+
+int matgb_chol_lookahead(int on) {
+  const int prev = g_chol_la;
+  if (on >= 0) g_chol_la = on ? 1 : 0;
+  return prev;
 }
 
 }  // extern "C"

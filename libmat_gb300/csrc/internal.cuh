@@ -175,14 +175,16 @@ int getrs_t(int64_t n, int64_t nrhs, const T *LU, int64_t lda,
 // lower: 0 every element, 1 lower triangle, 2 upper triangle (tiles and
 // elements outside it are skipped); rinv/cinv (may be null): per-row and
 // per-column power-of-two factors applied to the product before alpha (rinv
-// only together with cinv).
+// only together with cinv); persist: 1 the persistent short-K form, 0 one
+// CTA per tile (its CTAs retire tile by tile, so that kernels of a
+// higher-priority stream find SMs meanwhile), -1 the library setting.
 int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             int64_t lda, const void *B, int64_t ldb, float alpha,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
             int lower, const int32_t *skip, const void *Alo = nullptr,
             const void *Blo = nullptr, const float *rinv = nullptr,
             const float *cinv = nullptr, const void *Amid = nullptr,
-            const void *Bmid = nullptr);
+            const void *Bmid = nullptr, int persist = -1);
 // FP32-accurate float GEMM / SYRK on the tensor cores (tc_sgemm.cu): op(A)
 // and op(B) packed to FP16 hi + remainder under per-row / per-column
 // power-of-two scales, three products per update; tri as tc_gemm's lower.
@@ -205,6 +207,20 @@ int resid64(int64_t n, int64_t nrhs, const double *A, const double *X, int64_t l
 // Cholesky trailing update C22 -= L21 L21^T on the tensor cores (mixed.cu).
 int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
                    float *C22, int64_t ldc, int lp, const int32_t *info);
+// The same in two steps: L21 packed once (buffer set 0 or 1), then any
+// lower-triangular block of the product applied (C relative to its origin:
+// rows [r0, r0+M) of the operand against rows [c0, c0+N)).
+struct SyrkOperand {
+  uint16_t *hi, *lo;  // m x Kp, K-contiguous; lo null unless split
+  float *sc;          // scale slots: [0] s, [1] 1/s, [2] 1/s^2
+  int Kp;
+  int64_t m;
+  int lp;
+};
+int lp_syrk_pack(int64_t m, int nb, const float *L21, int64_t lda, int lp, int set,
+                 SyrkOperand *op);
+int lp_syrk_apply(const SyrkOperand &op, int64_t r0, int64_t M, int64_t c0, int64_t N,
+                  float *C, int64_t ldc, const int32_t *info, int persist = -1);
 template <typename T>
 int potrf_t(int64_t n, T *A, int64_t lda, int32_t *info, int lp);
 // Single-launch triangular solve with one right-hand side (trsv.cu); inv

@@ -218,35 +218,57 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
 // Cholesky: C22 (lower) -= L21 L21^T with L21 packed once to 16 bits and used
 // as both operands; FP16 scales L21 by a power of two s and the epilogue
 // multiplies by 1/s^2; the split form (lp 2) also packs the remainders.
-int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
-                   float *C22, int64_t ldc, int lp, const int32_t *info) {
+// lp_syrk_pack packs into buffer set `set` (0 or 1, so that a look-ahead can
+// pack the next block's operand while the current one is still read);
+// lp_syrk_apply runs C (lower, relative to C's origin) -= rows [r0, r0+M)
+// of the operand times rows [c0, c0+N) transposed.
+int lp_syrk_pack(int64_t m, int nb, const float *L21, int64_t lda, int lp, int set,
+                 SyrkOperand *op) {
   const int Kp = (nb + 63) / 64 * 64;
   const bool split = lp == 2;
   const size_t an = (size_t)m * Kp;
-  uint16_t *A16 = (uint16_t *)ws(WS_T0, an * 2 * (split ? 2 : 1));
-  float *sc = (float *)ws(WS_T2, 64);
+  const int s0 = set == 0 ? WS_T0 : WS_CU0, s2 = set == 0 ? WS_T2 : WS_CU0 + 2;
+  uint16_t *A16 = (uint16_t *)ws(s0, an * 2 * (split ? 2 : 1));
+  float *sc = (float *)ws(s2, 64);
   if (!A16 || !sc) return MATGB_ERR_NOMEM;
-  uint16_t *A16lo = split ? A16 + an : nullptr;
+  op->hi = A16;
+  op->lo = split ? A16 + an : nullptr;
+  op->sc = sc;
+  op->Kp = Kp;
+  op->m = m;
+  op->lp = lp;
   unsigned *amax = (unsigned *)(sc + 4);
   cudaStream_t st = ctx()->stream;
-  {
-    KtScope kt("lp_pack", 0.0, (split ? 8.0 : 6.0) * m * nb);
-    dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
-    if (lp == 1) {
-      pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
-    } else {
-      MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
-      amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
-          L21, lda, (int)m, nb, amax);
-      MGB_LAUNCHED("l21_amax");
-      pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc,
-                                            A16lo);
-    }
-    MGB_LAUNCHED("pack_l21");
+  KtScope kt("lp_pack", 0.0, (split ? 8.0 : 6.0) * m * nb);
+  dim3 g((unsigned)((m + 31) / 32), (unsigned)(Kp / 32));
+  if (lp == 1) {
+    pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
+  } else {
+    MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
+    amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
+        L21, lda, (int)m, nb, amax);
+    MGB_LAUNCHED("l21_amax");
+    pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc, op->lo);
   }
-  return tc_gemm(lp == 1, m, m, Kp, A16, Kp, A16, Kp, -1.f,
-                 lp != 1 ? sc + 2 : nullptr, 1.f, C22, ldc, 1, info, A16lo,
-                 A16lo);
+  MGB_LAUNCHED("pack_l21");
+  return 0;
+}
+
+int lp_syrk_apply(const SyrkOperand &op, int64_t r0, int64_t M, int64_t c0, int64_t N,
+                  float *C, int64_t ldc, const int32_t *info, int persist) {
+  if (M <= 0 || N <= 0) return 0;
+  const int64_t Kp = op.Kp;
+  return tc_gemm(op.lp == 1, M, N, Kp, op.hi + r0 * Kp, Kp, op.hi + c0 * Kp, Kp, -1.f,
+                 op.lp != 1 ? op.sc + 2 : nullptr, 1.f, C, ldc, 1, info,
+                 op.lo ? op.lo + r0 * Kp : nullptr, op.lo ? op.lo + c0 * Kp : nullptr,
+                 nullptr, nullptr, nullptr, nullptr, persist);
+}
+
+int lp_syrk_update(int64_t m, int nb, const float *L21, int64_t lda,
+                   float *C22, int64_t ldc, int lp, const int32_t *info) {
+  SyrkOperand op;
+  MGB_TRY(lp_syrk_pack(m, nb, L21, lda, lp, 0, &op));
+  return lp_syrk_apply(op, 0, m, 0, m, C22, ldc, info);
 }
 
 // ---- refinement kernels ------------------------------------------------------------

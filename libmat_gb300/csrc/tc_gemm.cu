@@ -610,7 +610,7 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
             const float *alpha_scale, float beta, float *C, int64_t ldc,
             int lower, const int32_t *skip, const void *Alo, const void *Blo,
             const float *rinv, const float *cinv, const void *Amid,
-            const void *Bmid) {
+            const void *Bmid, int persist) {
   Ctx *cx = ctx();
   if (!cx) return MATGB_ERR_NO_DEVICE;
   if (M <= 0 || N <= 0) return 0;
@@ -671,7 +671,8 @@ int tc_gemm(int bf16, int64_t M, int64_t N, int64_t K, const void *A,
       ma, mal, mam, mb, mbl, mbm, (int)M, (int)N, (int)(K / kTcBK), nseg,      \
       amask, bmask,                                                            \
       alpha, alpha_scale, beta, C, ldc, idesc, lower, skip, rinv, cinv, g_tc_err)
-  int *ctr = (!deep && g_tc_persistent) ? tile_counter(cx->stream) : nullptr;
+  const bool pers = persist < 0 ? g_tc_persistent != 0 : persist != 0;
+  int *ctr = (!deep && pers) ? tile_counter(cx->stream) : nullptr;
   if (ctr) {
     CUtensorMap pb, pbl, pbm;  // B boxes of the persistent form's tile width
     MGB_TRY(make_map(&pb, B, bf16, N, K, ldb, kTcPBN));

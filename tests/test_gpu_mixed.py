@@ -421,6 +421,53 @@ def test_lp_cholesky_reconstructs(gpu):
         assert err <= tol, (lp, err)
 
 
+def potrf_lp(L, A, lp):
+    n = A.shape[0]
+    dA = L.dalloc(A.nbytes)
+    di = L.dalloc(4)
+    try:
+        L.h2d(dA, np.asfortranarray(A, np.float32))
+        L.check(L.c.matgb_potrf_lp_dev(n, dA, n, di, lp), "potrf_lp")
+        F = np.empty((n, n), np.float32, order="F")
+        L.d2h(F, dA)
+        info = np.zeros(1, np.int32)
+        L.d2h(info, di)
+        L.check(L.c.matgb_tc_status(), "tc_status")
+    finally:
+        L.dfree(dA)
+        L.dfree(di)
+    return F, int(info[0])
+
+
+@pytest.mark.parametrize("lp", [2, 1])
+@pytest.mark.parametrize("n", [129, 300, 1000, 1537])
+def test_cholesky_lookahead_identical(gpu, lp, n):
+    """The tensor-core Cholesky's look-ahead (diagonal block, column solve
+    and the next block's update on the panel stream, the rest of the
+    trailing update beside it) computes every entry with the same operands
+    and the same products as the one-stream order: the factors agree bit for
+    bit, and so does the not-SPD report (a negative pivot in block 3)."""
+    L = gpu["f32"]
+    A = spd_conditioned(n, 1e3, 70 + n).astype(np.float32)
+    bad = A.copy()
+    if n > 400:
+        bad[400, 400] = -1.0
+    out = {}
+    for on in (0, 1):
+        prev = L.c.matgb_chol_lookahead(on)
+        try:
+            out[on] = (potrf_lp(L, A, lp), potrf_lp(L, bad, lp))
+        finally:
+            L.c.matgb_chol_lookahead(prev)
+    (F0, i0), (G0, j0) = out[0]
+    (F1, i1), (G1, j1) = out[1]
+    assert i0 == i1 == 0
+    assert np.array_equal(np.tril(F0), np.tril(F1))
+    assert j0 == j1 and (j0 == 401 if n > 400 else j0 == 0), (j0, j1)
+    if j0 == 0:
+        assert np.array_equal(np.tril(G0), np.tril(G1))
+
+
 @pytest.mark.parametrize("n", [100, 1030, 2100])
 @pytest.mark.parametrize("nrhs", [1, 7, 64, 65])
 def test_resid64_matches_fp64(gpu, n, nrhs):
