@@ -85,7 +85,11 @@ __global__ void __launch_bounds__(256)
 template <int NB>
 __global__ void __launch_bounds__(NB)
     potrf_diag_rows_kernel(int nb, float *__restrict__ A, int64_t lda,
-                           int32_t *__restrict__ info, int64_t kb) {
+                           int32_t *__restrict__ info, int64_t kb,
+                           unsigned *__restrict__ zero = nullptr) {
+  // zero (may be null): the max slot that the column solve after this
+  // kernel fills, cleared here instead of by a launch of its own
+  if (zero && threadIdx.x == 0) *zero = 0u;
   if (*info != 0) return;
   __shared__ __align__(16) float colb[2][NB + 8];  // colb[.][3 + (i - j)] = A^(j)(i, j)
   const int i = threadIdx.x;
@@ -179,7 +183,8 @@ __global__ void __launch_bounds__(256)
 template <int NB>
 __global__ void __launch_bounds__(128)
     chol_trsm_rows_kernel(int nb, const float *__restrict__ L11, float *__restrict__ A21,
-                          int64_t lda, int64_t m, const int32_t *__restrict__ info) {
+                          int64_t lda, int64_t m, const int32_t *__restrict__ info,
+                          unsigned *__restrict__ amax = nullptr) {
   if (*info != 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float (*Lt)[NB + 4] = reinterpret_cast<float (*)[NB + 4]>(smem_raw);  // Lt[j][k] = L11(j+1+k, j)
@@ -195,9 +200,11 @@ __global__ void __launch_bounds__(128)
   float a[NB];
 #pragma unroll
   for (int j = 0; j < NB; j++) a[j] = (act && j < nb) ? A21[r + (int64_t)j * lda] : 0.f;
+  float mx = 0.f;  // max |L21| over the row (amax given); NaN ignored as in amax_kernel
   for (int j = 0; j < nb; j++) {
     const float x = a[0] * rinv[j];
     if (act) A21[r + (int64_t)j * lda] = x;
+    if (act) mx = fmaxf(mx, fabsf(x));
     const int n_out = nb - 1 - j;  // pending columns after this step
 #pragma unroll
     for (int c = 0; c < NB / 32; c++) {
@@ -213,12 +220,21 @@ __global__ void __launch_bounds__(128)
       }
     }
   }
+  if (amax) {
+    for (int off = 16; off; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    if ((tid & 31) == 0) atomicMax(amax, __float_as_uint(mx));
+  }
 }
 
 // The diagonal block [kb, kb+nb) and the column solve below it, on the
 // current library stream.
+// amax (may be null): for a float block of 96 or 128 columns the kernels
+// also leave max |L21| there (zeroed by the diagonal kernel); *amax_done
+// says whether they did.
 template <typename T>
-static int chol_panel(int64_t n, T *A, int64_t lda, int32_t *info, int64_t kb, int nb) {
+static int chol_panel(int64_t n, T *A, int64_t lda, int32_t *info, int64_t kb, int nb,
+                      unsigned *amax = nullptr, bool *amax_done = nullptr) {
+  if (amax_done) *amax_done = false;
   Ctx *cx = ctx();
   T *A11 = A + kb + kb * lda;
   {
@@ -227,12 +243,12 @@ static int chol_panel(int64_t n, T *A, int64_t lda, int32_t *info, int64_t kb, i
     if (sizeof(T) == 4 && nb > 64) {
       if (nb > kCholBlock) {
         potrf_diag_rows_kernel<kCholBlockLp><<<1, kCholBlockLp, 0, cx->stream>>>(
-            nb, (float *)A11, lda, info, kb);
+            nb, (float *)A11, lda, info, kb, amax);
         MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlockLp>,
                              "potrf_diag_rows", 0));
       } else {
         potrf_diag_rows_kernel<kCholBlock><<<1, kCholBlock, 0, cx->stream>>>(
-            nb, (float *)A11, lda, info, kb);
+            nb, (float *)A11, lda, info, kb, amax);
         MGB_TRY(launch_check((const void *)potrf_diag_rows_kernel<kCholBlock>,
                              "potrf_diag_rows", 0));
       }
@@ -254,11 +270,14 @@ static int chol_panel(int64_t n, T *A, int64_t lda, int32_t *info, int64_t kb, i
       MGB_CUDA(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       if (nb == kCholBlockLp)
         chol_trsm_rows_kernel<kCholBlockLp><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
-            nb, (const float *)A11, (float *)A21, lda, m, info);
+            nb, (const float *)A11, (float *)A21, lda, m, info, amax);
       else
         chol_trsm_rows_kernel<kCholBlock><<<(unsigned)((m + 127) / 128), 128, sm, cx->stream>>>(
-            nb, (const float *)A11, (float *)A21, lda, m, info);
-      return launch_check(kr, "chol_trsm_rows", sm);
+            nb, (const float *)A11, (float *)A21, lda, m, info, amax);
+      MGB_TRY(launch_check(kr, "chol_trsm_rows", sm));
+      // both kernels ran in their row forms (nb > 64): the max is there
+      if (amax_done) *amax_done = amax != nullptr && nb > 64;
+      return 0;
     }
   }
   auto ktrsm = chol_trsm_kernel<T>;
@@ -323,11 +342,14 @@ static int potrf_la(int64_t n, float *A, int64_t lda, int32_t *info, int lp) {
     SyrkOperand op{};
     {
       CholStreamSwap sw(hi);
-      MGB_TRY(chol_panel<float>(n, A, lda, info, kb, nb));
+      // the FP16 scale's max comes from the block's own kernels
+      unsigned *slot = (m > 0 && lp != 1) ? lp_syrk_amax_slot((int)(k & 1)) : nullptr;
+      bool amax_done = false;
+      MGB_TRY(chol_panel<float>(n, A, lda, info, kb, nb, slot, &amax_done));
       if (m > 0) {
         // (set k % 2 was last read by block k-2's rest update, which the
         // panel stream waited for before block k-1's look-ahead update)
-        MGB_TRY(lp_syrk_pack(m, nb, A21, lda, lp, (int)(k & 1), &op));
+        MGB_TRY(lp_syrk_pack(m, nb, A21, lda, lp, (int)(k & 1), &op, amax_done));
         MGB_CUDA(cudaEventRecord(g_cla.evp, hi));
         MGB_CUDA(cudaStreamWaitEvent(hi, g_cla.evr, 0));
         MGB_TRY(lp_syrk_apply(op, 0, m, 0, nn, A + (kb + nb) + (kb + nb) * lda, lda, info));

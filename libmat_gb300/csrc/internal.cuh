@@ -217,8 +217,10 @@ struct SyrkOperand {
   int64_t m;
   int lp;
 };
+// amax_ready: the set's max slot (lp_syrk_amax_slot) already holds max|L21|.
 int lp_syrk_pack(int64_t m, int nb, const float *L21, int64_t lda, int lp, int set,
-                 SyrkOperand *op);
+                 SyrkOperand *op, bool amax_ready = false);
+unsigned *lp_syrk_amax_slot(int set);
 int lp_syrk_apply(const SyrkOperand &op, int64_t r0, int64_t M, int64_t c0, int64_t N,
                   float *C, int64_t ldc, const int32_t *info, int persist = -1);
 template <typename T>

@@ -222,8 +222,15 @@ int lp_trailing_update(int64_t n, float *A, int64_t lda, int64_t kb,
 // pack the next block's operand while the current one is still read);
 // lp_syrk_apply runs C (lower, relative to C's origin) -= rows [r0, r0+M)
 // of the operand times rows [c0, c0+N) transposed.
+// The max slot of set s (zeroed and filled by the Cholesky's own kernels
+// when amax_ready).
+unsigned *lp_syrk_amax_slot(int set) {
+  float *sc = (float *)ws(set == 0 ? WS_T2 : WS_CU0 + 2, 64);
+  return sc ? reinterpret_cast<unsigned *>(sc + 4) : nullptr;
+}
+
 int lp_syrk_pack(int64_t m, int nb, const float *L21, int64_t lda, int lp, int set,
-                 SyrkOperand *op) {
+                 SyrkOperand *op, bool amax_ready) {
   const int Kp = (nb + 63) / 64 * 64;
   const bool split = lp == 2;
   const size_t an = (size_t)m * Kp;
@@ -244,10 +251,12 @@ int lp_syrk_pack(int64_t m, int nb, const float *L21, int64_t lda, int lp, int s
   if (lp == 1) {
     pack_l21_kernel<1><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, nullptr, sc);
   } else {
-    MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
-    amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
-        L21, lda, (int)m, nb, amax);
-    MGB_LAUNCHED("l21_amax");
+    if (!amax_ready) {
+      MGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
+      amax_kernel<<<grid_cap(32 * (int64_t)nb * ((m + 1023) / 1024)), 256, 0, st>>>(
+          L21, lda, (int)m, nb, amax);
+      MGB_LAUNCHED("l21_amax");
+    }
     pack_l21_kernel<0><<<g, 256, 0, st>>>(L21, lda, m, nb, Kp, A16, amax, sc, op->lo);
   }
   MGB_LAUNCHED("pack_l21");
