@@ -314,12 +314,6 @@ static int chol_la_setup() {
   return 0;
 }
 
-struct CholStreamSwap {
-  cudaStream_t saved;
-  explicit CholStreamSwap(cudaStream_t s) : saved(ctx()->stream) { ctx()->stream = s; }
-  ~CholStreamSwap() { ctx()->stream = saved; }
-};
-
 static int potrf_la(int64_t n, float *A, int64_t lda, int32_t *info, int lp) {
   MGB_TRY(chol_la_setup());
   const int NB = kCholBlockLp;
@@ -341,7 +335,7 @@ static int potrf_la(int64_t n, float *A, int64_t lda, int32_t *info, int lp) {
     float *A21 = A + (kb + nb) + kb * lda;
     SyrkOperand op{};
     {
-      CholStreamSwap sw(hi);
+      StreamSwap sw(hi);
       // the FP16 scale's max comes from the block's own kernels
       unsigned *slot = (m > 0 && lp != 1) ? lp_syrk_amax_slot((int)(k & 1)) : nullptr;
       bool amax_done = false;

@@ -26,6 +26,14 @@ struct Ctx {
 // Lazily initialised context (device 0 unless matgb_init chose another).
 Ctx *ctx();
 
+// Route the library's launches to another stream for a scope (the panel
+// streams of the look-aheads).
+struct StreamSwap {
+  cudaStream_t saved;
+  explicit StreamSwap(cudaStream_t s) : saved(ctx()->stream) { ctx()->stream = s; }
+  ~StreamSwap() { ctx()->stream = saved; }
+};
+
 // Record an error; returns `code`.  Never aborts (callers decide).
 int set_error(int code, const char *fmt, ...);
 // Record a CUDA failure with its call site.

@@ -1433,13 +1433,6 @@ static int trsm_unit_lower(int tb, int64_t ncols, const T *L, int64_t ldl, T *B,
   return trsm_left_t<T>(true, false, true, tb, ncols, L, ldl, B, ldb, nullptr);
 }
 
-// Temporarily route library launches to another stream.
-struct StreamSwap {
-  cudaStream_t saved;
-  explicit StreamSwap(cudaStream_t s) : saved(ctx()->stream) { ctx()->stream = s; }
-  ~StreamSwap() { ctx()->stream = saved; }
-};
-
 // ---- the mixed look-ahead's operands in one launch --------------------------
 // After a fused block (TB pivots, its net row map on the device), the
 // split tensor-core update of the next block's nn columns needs those
