@@ -218,13 +218,13 @@ def ktime_names(L):
     return out
 
 
-@pytest.mark.parametrize("n", [300, 1000, 1537])
+@pytest.mark.parametrize("n", [291, 300, 433, 1000, 1537])
 def test_lookahead_prep_in_one_launch(gpu, n):
     """After a fused 144-column block, the split update's look-ahead runs the
     next block's row swaps, its U12 solve and both operands' packing as one
     launch (la_prep; U12 scaled per column).  Its factors reconstruct PA as
     well as the separate launches' do (n = 300: the last look-ahead has 12
-    columns), and it is the form that ran."""
+    columns; n = 291 and 433: 3 and 1), and it is the form that ran."""
     L = gpu["f32"]
     A = rng.uniform(900 + n, (n, n), -1, 1, np.float32)
     errs = {}
