@@ -1,7 +1,7 @@
 """GPU: the reference's own unit tests for the hot path (and the rows beside
 it: det, inv, full-pivoting LU, QR), compiled unchanged against
 include/mat.h, linked against libmatgb_f32 and RUN on the GPU -- the drop-in
-at the source level, judged by the reference's own assertions (its test.h
+at the source level, checked by the reference's own assertions (its test.h
 harness: "N passed, 0 failed", exit status 0).
 
 The test sources are read from the reference tree, or from the copy that
